@@ -1,0 +1,398 @@
+/*
+ * vt.h — C ABI of the GB300 voxel path tracer and mesh voxelizer.
+ *
+ * This is the drop-in boundary for the progressive path-tracing pass and the
+ * mesh voxelizer of voxelToy.  The reference exposes that path as the C++
+ * class `Renderer` (src/renderer/renderer.h:23-221) driving OpenGL shaders;
+ * here the same verbs are plain C functions over opaque handles, with host
+ * pointers and sizes only.  Every entry point cites the reference interface
+ * it replaces.
+ *
+ * Conventions
+ *   - Every function returns a vt_status (VT_OK == 0, errors < 0).  The text
+ *     of the last error on the calling thread is available from
+ *     vt_last_error().  No C++ exception crosses this boundary.
+ *   - Host pointers are borrowed for the duration of the call and copied; the
+ *     library keeps no reference to caller memory.  The library owns all
+ *     device memory; handles are released with the matching *_destroy.
+ *   - A context and the handles created from it are used by one host thread
+ *     at a time.  vt_server_* calls are thread safe.
+ *   - World space, voxel space and the material layout follow the reference:
+ *     the volume is centred at the origin and scaled so that its largest axis
+ *     spans 1000 world units (src/renderer/renderer.cpp:845-850); voxel
+ *     (x, y, z) has linear index x + y*rx + z*rx*ry
+ *     (src/shaders/shared/coordinates.h:118-127).
+ */
+#ifndef VT_H
+#define VT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define VT_API __attribute__((visibility("default")))
+#else
+#define VT_API
+#endif
+
+/* ---------------------------------------------------------------- status -- */
+typedef enum vt_status {
+  VT_OK = 0,
+  VT_EINVAL = -1,       /* bad argument (null handle, size, unknown material) */
+  VT_ENOMEM = -2,       /* host or device allocation failed                    */
+  VT_EBUDGET = -3,      /* request exceeds the context's device-memory budget  */
+  VT_EDEVICE = -4,      /* CUDA error or device-side error word set             */
+  VT_ETIMEOUT = -5,     /* a bounded wait ran out                               */
+  VT_ECANCELLED = -6,   /* job cancelled                                        */
+  VT_ENOTREADY = -7,    /* result not available yet                             */
+  VT_EUNSUPPORTED = -8  /* feature not available in this build                  */
+} vt_status;
+
+/* Renderer::RenderResult (src/renderer/renderer.h:45-49). */
+enum { VT_SAMPLES_PENDING = 0, VT_FINISHED_RENDERING = 1 };
+
+/* --------------------------------------------------------------- handles -- */
+typedef struct vt_context vt_context; /* Renderer + its GL context            */
+typedef struct vt_scene vt_scene;     /* voxel volume, palette, emissive list  */
+typedef struct vt_env vt_env;         /* HDR environment image + its CDFs      */
+typedef struct vt_job vt_job;         /* camera, settings, accumulation buffer */
+typedef struct vt_server vt_server;   /* continuous-batching render server     */
+
+/* -------------------------------------------------------------- context -- */
+typedef struct vt_device_opts {
+  int32_t device;            /* CUDA ordinal                                  */
+  uint64_t hbm_budget_bytes; /* 0 = no budget; allocations beyond it fail     */
+  uint32_t flags;            /* reserved, 0                                   */
+} vt_device_opts;
+
+/* Renderer::initialize (src/renderer/renderer.h:31, renderer.cpp:76-140).
+ * opts may be NULL (device 0, no budget). */
+VT_API int vt_create(const vt_device_opts* opts, vt_context** out);
+/* Renderer::~Renderer (src/renderer/renderer.h:28). */
+VT_API int vt_destroy(vt_context* ctx);
+/* Text of the last error raised on the calling thread ("" if none). */
+VT_API const char* vt_last_error(void);
+/* Renderer::setLogger (src/renderer/renderer.h:99; src/log/logger.h:7-11). */
+typedef void (*vt_log_fn)(const char* message, void* user);
+VT_API int vt_set_log_callback(vt_context* ctx, vt_log_fn fn, void* user);
+/* Bytes of device memory the context currently holds. */
+VT_API int vt_context_memory(const vt_context* ctx, uint64_t* bytes_in_use);
+
+/* ------------------------------------------------------------- materials -- */
+/* Material::MaterialType (src/renderer/material/material.h:8-13). */
+enum { VT_MATERIAL_LAMBERT = 0, VT_MATERIAL_METAL = 1, VT_MATERIAL_PLASTIC = 2 };
+
+/* One palette record: LambertMaterialData / MetalMaterialData /
+ * PlasticMaterialData (src/renderer/material/material.h:15-33) behind their
+ * type tag (src/renderer/loaders/voxLoader.cpp:54-66).  albedo is the Lambert
+ * albedo, the metal reflectance (Fresnel F0 when VT_QUIRK_FIXED_IOR is off)
+ * or the plastic diffuse albedo (unused by the reference's plastic BSDF,
+ * src/shaders/materials/plastic.h:15).  The device stores each record as
+ * eight IEEE half floats. */
+typedef struct vt_material {
+  int32_t type;
+  float emission[3];
+  float albedo[3];
+  float roughness;
+} vt_material;
+
+/* ---------------------------------------------------------------- scenes -- */
+enum {
+  VT_SCENE_PRUNE_EMISSIVE = 1u << 0, /* drop emissive voxels with no empty 6-neighbour
+                                        (Renderer::pruneInteriorEmissiveVoxels,
+                                        src/renderer/import.cpp:180-203)          */
+  VT_SCENE_AUTO_EMISSIVE = 1u << 1   /* build the emissive list from the palette:
+                                        every voxel whose material emits          */
+};
+
+/* Upload a dense volume.  voxels[i] == 0 is empty, voxels[i] == k (1..255)
+ * uses palette[k-1].  emissive_indices are linear voxel indices sampled by
+ * next-event estimation (may be NULL when n_emissive == 0).
+ * Replaces Renderer::createVoxelDataTexture (src/renderer/renderer.h:129-134,
+ * renderer.cpp:833-940) for the byte-per-voxel palette layout. */
+VT_API int vt_scene_create(vt_context* ctx, int32_t rx, int32_t ry, int32_t rz,
+                           const uint8_t* voxels, const vt_material* palette,
+                           int32_t n_palette, const int32_t* emissive_indices,
+                           int64_t n_emissive, uint32_t flags, vt_scene** out);
+
+/* Upload a volume in the reference's own layout: one int32 material-table
+ * offset per voxel (-1 = empty) and a flat float material table of
+ * [type, emission[3], albedo[3] (, roughness)] records
+ * (Renderer::createVoxelDataTexture, src/renderer/renderer.cpp:833-940;
+ * record layout src/renderer/loaders/voxLoader.cpp:54-66).  At most 255
+ * distinct records may be referenced. */
+VT_API int vt_scene_create_from_offsets(vt_context* ctx, int32_t rx, int32_t ry,
+                                        int32_t rz, const int32_t* material_offsets,
+                                        const float* material_data,
+                                        int64_t material_data_size,
+                                        const int32_t* emissive_indices,
+                                        int64_t n_emissive, uint32_t flags,
+                                        vt_scene** out);
+
+/* Voxelizer coverage rule (src/shaders/shared/voxelize.gs:14-19). */
+enum { VT_VOXELIZE_THIN = 0, VT_VOXELIZE_FAT = 1 };
+enum { VT_MESH_VOXEL_SPACE = 0, VT_MESH_FIT_UNIT_CUBE = 1 };
+
+/* Voxelize a triangle mesh on the GPU into a new scene whose occupied voxels
+ * use palette[0].  vertices: n_vertices * 3 floats; indices: n_triangles * 3.
+ * With VT_MESH_FIT_UNIT_CUBE the mesh is first fitted into the unit cube with
+ * a one-voxel margin (computeMeshTransform, src/renderer/import.cpp:46-64)
+ * and scaled to voxel space (src/shaders/shared/voxelize.vs:20-27); with
+ * VT_MESH_VOXEL_SPACE the vertices are already in voxel units.
+ * Replaces Renderer::loadMesh + GPUVoxelizer::voxelizeMesh
+ * (src/renderer/import.cpp:66-131, src/voxelize/gpuVoxelizer.cpp:46-72). */
+VT_API int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices,
+                                  int64_t n_vertices, const uint32_t* indices,
+                                  int64_t n_triangles, int32_t rx, int32_t ry,
+                                  int32_t rz, int32_t mode, int32_t placement,
+                                  const vt_material* palette, int32_t n_palette,
+                                  vt_scene** out);
+
+typedef struct vt_scene_info {
+  int32_t resolution[3];
+  float bounds_min[3];
+  float bounds_max[3];
+  float voxel_size[3];
+  int64_t n_emissive;     /* after pruning */
+  int32_t n_palette;
+  uint64_t device_bytes;
+} vt_scene_info;
+VT_API int vt_scene_get_info(const vt_scene* scene, vt_scene_info* info);
+/* Copy the byte-per-voxel grid back to the host (rx*ry*rz bytes). */
+VT_API int vt_scene_read_voxels(const vt_scene* scene, uint8_t* out, size_t bytes);
+/* Copy the (pruned) emissive list back; *n receives its length. */
+VT_API int vt_scene_read_emissive(const vt_scene* scene, int32_t* out,
+                                  int64_t capacity, int64_t* n);
+VT_API int vt_scene_destroy(vt_scene* scene);
+
+/* ------------------------------------------------------------ environment -- */
+/* Upload a linear RGB float image (width*height*3, row 0 = zenith) as the
+ * background, stored as FP16 RGBA, and build its importance-sampling CDFs on
+ * the GPU with FP64 prefix sums at full resolution.
+ * Replaces Renderer::loadBackgroundImage + calculateCDF
+ * (src/renderer/renderer.cpp:947-1055, src/renderer/image.cpp:68-389). */
+VT_API int vt_env_create_image(vt_context* ctx, const float* rgb, int32_t width,
+                               int32_t height, vt_env** out);
+/* Copy back the CDFs: cdf_u (width+1)*height floats, cdf_v height+1 floats
+ * and the radiance integral (image.cpp:349-389).  Any output may be NULL. */
+VT_API int vt_env_read_cdf(const vt_env* env, float* cdf_u, size_t cdf_u_bytes,
+                           float* cdf_v, size_t cdf_v_bytes, float* integral);
+VT_API int vt_env_destroy(vt_env* env);
+
+/* ---------------------------------------------------------------- camera -- */
+/* CameraParameters::CameraLensModel (src/camera/cameraParameters.h:23-28). */
+enum { VT_LENS_PINHOLE = 0, VT_LENS_THIN_LENS = 1, VT_LENS_ORTHOGRAPHIC = 2 };
+
+/* CameraParameters (src/camera/cameraParameters.h:117-129) with the focus
+ * distance and lens radius in world units. */
+typedef struct vt_camera {
+  float eye[3];
+  float target[3];
+  float fov_y;          /* vertical field of view, radians                     */
+  float near_distance;  /* reference default 0.1                               */
+  float far_distance;   /* reference default 10000                             */
+  float focal_distance; /* thin-lens focus distance, world units               */
+  float lens_radius;    /* thin-lens aperture radius, world units              */
+  int32_t lens_model;
+} vt_camera;
+
+/* CameraParameters::CameraParameters + Renderer::Renderer defaults
+ * (src/camera/cameraParameters.cpp:7-17, src/renderer/renderer.cpp:43-45). */
+VT_API int vt_camera_default(vt_camera* cam);
+/* CameraParameters::orbitAroundTarget: eye = target - r * sph(theta, phi)
+ * (src/camera/cameraParameters.cpp:90-94). */
+VT_API int vt_camera_orbit(vt_camera* cam, float theta, float phi);
+/* CameraParameters::orbitAroundEye (cameraParameters.cpp:96-100). */
+VT_API int vt_camera_orbit_eye(vt_camera* cam, float theta, float phi);
+/* CameraParameters::setDistanceFromTarget (cameraParameters.cpp:38-41). */
+VT_API int vt_camera_set_distance(vt_camera* cam, float distance);
+/* CameraParameters::setFocalLength with the 35 mm film rule of
+ * Renderer::render (cameraParameters.cpp:139-142, renderer.cpp:573-580). */
+VT_API int vt_camera_set_focal_length(vt_camera* cam, float focal_length_mm,
+                                      int32_t width, int32_t height);
+/* CameraParameters::setFStop: lens radius = focal length / f-stop / 2
+ * (cameraParameters.cpp:172-175), focal length from fov and film. */
+VT_API int vt_camera_set_fstop(vt_camera* cam, float fstop, int32_t width,
+                               int32_t height);
+/* CameraController::focusOnBounds (src/camera/cameraController.cpp:16-23). */
+VT_API int vt_camera_focus_on_bounds(vt_camera* cam, const float bounds_min[3],
+                                     const float bounds_max[3]);
+/* Orbit / fly controllers: mouse deltas normalised by the image size
+ * (src/camera/orbitCameraController.cpp:15-41,
+ * src/camera/flyCameraController.cpp:15-73).  buttons: 1 = rotate (right
+ * button), 2 = dolly/pan (middle button). */
+enum { VT_BUTTON_ROTATE = 1, VT_BUTTON_PAN = 2 };
+enum { VT_KEY_FORWARD = 0, VT_KEY_BACK = 1, VT_KEY_RIGHT = 2, VT_KEY_LEFT = 3 };
+VT_API int vt_camera_orbit_mouse(vt_camera* cam, float ndx, float ndy, int32_t buttons);
+VT_API int vt_camera_fly_mouse(vt_camera* cam, float ndx, float ndy, int32_t buttons);
+VT_API int vt_camera_fly_key(vt_camera* cam, int32_t key);
+
+/* Shader uniforms derived from a camera (Renderer::updateCamera,
+ * src/renderer/renderer.cpp:343-446): row-major 4x4 matrices as uploaded
+ * with transpose = GL_TRUE. */
+typedef struct vt_camera_uniforms {
+  float proj[16];
+  float inv_proj[16];
+  float inv_model_view[16];
+  float viewport[4];
+} vt_camera_uniforms;
+VT_API int vt_camera_compute_uniforms(const vt_camera* cam, int32_t width,
+                                      int32_t height, vt_camera_uniforms* out);
+
+/* -------------------------------------------------------------- settings -- */
+/* Behaviours of the reference kept behind flags.  VT_QUIRKS_REFERENCE
+ * reproduces the reference pass; the physically based configurations clear
+ * them. */
+#define VT_QUIRK_GAMMA_BEFORE_AVERAGE  (1u << 0) /* pathTracer.fs:294-295 + accumulation.fs:17 */
+#define VT_QUIRK_GROUND                (1u << 1) /* exit through y<0 hits ground, dda.h:74-78   */
+#define VT_QUIRK_GRADIENT_PDF_MISMATCH (1u << 2) /* lights.h:30 (1/4pi) vs sampling.h:34 (1/2pi) */
+#define VT_QUIRK_DOUBLE_REFLECTANCE    (1u << 3) /* microfacet.h:57 + :116                      */
+#define VT_QUIRK_FIXED_IOR             (1u << 4) /* Schlick with IOR 7.3, microfacet.h:2,64-69   */
+#define VT_QUIRK_EXPONENT_IS_ROUGHNESS (1u << 5) /* Blinn exponent = roughness, metal.h:13-14    */
+#define VT_QUIRK_THINLENS_NO_JITTER    (1u << 6) /* no pixel jitter, generateRay.h:83            */
+#define VT_QUIRK_UNGUARDED_SAMPLES     (1u << 7) /* zero-pdf / below-surface samples propagate,  */
+                                                 /* pathTracer.fs:164,276 divide by the pdf     */
+#define VT_QUIRKS_REFERENCE 0xffu
+
+/* Random-number source.  VT_RNG_NOISE_TABLE walks a 1024x1024 RGBA table
+ * from a per-pixel hashed offset (src/shaders/shared/random.h:3-27,
+ * renderer.cpp:739-760); VT_RNG_PHILOX draws Philox-4x32-10 blocks keyed by
+ * (seed, pixel) with counter (sample, call). */
+enum { VT_RNG_PHILOX = 0, VT_RNG_NOISE_TABLE = 1 };
+
+/* RenderSettings (src/renderer/renderSettings.h:6-29) plus the uniforms of
+ * src/shaders/integrator/pathTracer.fs:25-44. */
+typedef struct vt_render_settings {
+  int32_t max_bounces;          /* m_pathtracerMaxNumBounces                    */
+  int32_t max_samples;          /* m_pathtracerMaxSamples                       */
+  int32_t rr_start_bounce;      /* Russian roulette from this bounce; -1 = off  */
+  float gamma;                  /* tonemappingGamma (2.2)                       */
+  float exposure;               /* tonemappingExposure (1)                      */
+  float nee_emission_scale;     /* emissive light-sample scale (reference 10)   */
+  float wireframe_opacity;      /* m_wireframeOpacity                           */
+  float wireframe_thickness;    /* m_wireframeThickness                         */
+  float background_top[3];      /* m_backgroundColor[0]                         */
+  float background_bottom[3];   /* m_backgroundColor[1]                         */
+  float background_rotation;    /* radians (m_backgroundRotationDegrees)         */
+  int32_t selected_voxel[3];    /* SelectVoxelData.index (drawn red)            */
+  int32_t select_enabled;
+  int32_t ground_material;      /* palette entry used by VT_QUIRK_GROUND hits   */
+  uint32_t quirks;              /* VT_QUIRK_* bits                              */
+  int32_t rng_mode;             /* VT_RNG_*                                     */
+  uint32_t seed;
+} vt_render_settings;
+
+/* RenderSettings defaults of Renderer::Renderer (renderer.cpp:49-53) and the
+ * uniform initialisers of pathTracer.fs:25-44, all quirks on. */
+VT_API int vt_settings_default(vt_render_settings* s);
+
+/* ------------------------------------------------------------------- jobs -- */
+/* A job is one progressive render: camera, settings, a scene, an optional
+ * environment image (NULL = gradient background from the settings) and its
+ * accumulation buffer.  Replaces Renderer::resizeFrame + updateCamera +
+ * updateRenderSettings (src/renderer/renderer.cpp:343-554, 1057-1106). */
+VT_API int vt_job_create(vt_context* ctx, const vt_scene* scene, const vt_env* env,
+                         const vt_camera* cam, const vt_render_settings* settings,
+                         int32_t width, int32_t height, vt_job** out);
+/* Renderer::updateCamera + resetRender (renderer.cpp:343-446, 941-945). */
+VT_API int vt_job_set_camera(vt_job* job, const vt_camera* cam);
+/* Renderer::updateRenderSettings (renderer.cpp:1057-1106). */
+VT_API int vt_job_set_settings(vt_job* job, const vt_render_settings* settings);
+VT_API int vt_job_set_scene(vt_job* job, const vt_scene* scene, const vt_env* env);
+/* Renderer::resizeFrame (renderer.cpp:448-554): resets accumulation. */
+VT_API int vt_job_resize(vt_job* job, int32_t width, int32_t height);
+/* Renderer::resetRender (renderer.cpp:941-945). */
+VT_API int vt_job_reset(vt_job* job);
+/* Renderer::render (renderer.cpp:556-645) called `passes` times: each pass
+ * adds one sample per pixel until max_samples are accumulated.  *result
+ * receives VT_SAMPLES_PENDING or VT_FINISHED_RENDERING.  The call queues GPU
+ * work and returns; vt_job_synchronize or a readback waits for it. */
+VT_API int vt_job_render(vt_job* job, int32_t passes, int32_t* result);
+VT_API int vt_job_synchronize(vt_job* job);
+VT_API int vt_job_sample_count(const vt_job* job, int32_t* samples);
+
+enum {
+  VT_READBACK_FLIP_Y = 1u << 0,  /* bottom row first, as saveImage writes (renderer.cpp:1133-1136) */
+  VT_READBACK_TONEMAP = 1u << 1  /* apply pow(x*exposure, 1/gamma) to a linear accumulation  */
+};
+/* Copy the accumulated average image (width*height*4 floats, RGBA) to host
+ * memory.  Replaces the glGetTexImage of Renderer::saveImage
+ * (renderer.cpp:1108-1140). */
+VT_API int vt_job_readback(vt_job* job, float* rgba, size_t bytes, uint32_t flags);
+/* Device pointer of the float4 accumulation sums and the sample count, for
+ * zero-copy consumers (valid until the next render/reset/destroy). */
+VT_API int vt_job_device_buffer(vt_job* job, void** sums, int32_t* samples);
+/* Focal-distance pick: trace the ray through window pixel (x, y) and return
+ * the hit distance (99999999 when nothing is hit) and voxel (-1 if none).
+ * Replaces focalDistance.vs (src/shaders/focalDistance/focalDistance.vs:45-81)
+ * and RendererServiceSetFocalDistance. */
+VT_API int vt_job_pick(vt_job* job, float x, float y, float* distance,
+                       int32_t voxel[3]);
+VT_API int vt_job_destroy(vt_job* job);
+
+/* ------------------------------------------------------------- batching -- */
+/* Trace `passes` samples per pixel for every job in one persistent launch
+ * that pulls (job, pixel-tile) work items from a device queue, instead of one
+ * launch per job and pass.  Results are identical to rendering each job alone
+ * (counter-based random streams, per-pixel sample order).  opts may be NULL
+ * (autotuned defaults). */
+typedef struct vt_batch_opts {
+  int32_t tile_pixels;     /* pixels per work item (multiple of 32), 0 = auto   */
+  int32_t blocks_per_sm;   /* resident blocks per SM, 0 = auto                  */
+  int32_t threads_per_block; /* 0 = auto                                        */
+  int32_t kernel;          /* 0 = auto, 1 = plain per-pixel, 2 = persistent     */
+} vt_batch_opts;
+VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
+                           int32_t passes, const vt_batch_opts* opts,
+                           int32_t* results);
+
+/* -------------------------------------------------------------- serving -- */
+typedef struct vt_server_opts {
+  uint64_t hbm_budget_bytes;   /* admission budget for job buffers + scenes    */
+  int32_t max_active_jobs;     /* slots traced concurrently                     */
+  int32_t passes_per_round;    /* samples per pixel each active job gets per round */
+  int32_t tile_pixels;         /* 0 = auto                                      */
+} vt_server_opts;
+
+enum {
+  VT_REQ_QUEUED = 0, VT_REQ_RUNNING = 1, VT_REQ_DONE = 2,
+  VT_REQ_CANCELLED = 3, VT_REQ_FAILED = 4
+};
+
+typedef struct vt_server_stats {
+  uint64_t submitted, completed, cancelled, failed;
+  uint64_t paths_traced;
+  uint64_t rounds;
+  uint64_t bytes_in_use;
+  int32_t active, queued;
+} vt_server_stats;
+
+/* Start a request loop thread that admits jobs as slots and budget free up
+ * and traces all admitted jobs together each round. */
+VT_API int vt_server_create(vt_context* ctx, const vt_server_opts* opts,
+                            vt_server** out);
+/* Submit a render request; the scene and env must outlive it. */
+VT_API int vt_server_submit(vt_server* srv, const vt_scene* scene, const vt_env* env,
+                            const vt_camera* cam, const vt_render_settings* settings,
+                            int32_t width, int32_t height, int32_t spp_target,
+                            uint64_t* ticket);
+VT_API int vt_server_poll(vt_server* srv, uint64_t ticket, int32_t* state,
+                          int32_t* samples_done);
+/* Wait until the request is done, failed or cancelled (timeout in seconds,
+ * < 0 waits forever); VT_ETIMEOUT if it ran out. */
+VT_API int vt_server_wait(vt_server* srv, uint64_t ticket, double timeout_s);
+/* Copy the finished image (width*height*4 floats) and release the request. */
+VT_API int vt_server_result(vt_server* srv, uint64_t ticket, float* rgba,
+                            size_t bytes, double* seconds_to_target);
+VT_API int vt_server_cancel(vt_server* srv, uint64_t ticket);
+VT_API int vt_server_get_stats(vt_server* srv, vt_server_stats* stats);
+VT_API int vt_server_destroy(vt_server* srv);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VT_H */

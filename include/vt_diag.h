@@ -1,0 +1,79 @@
+/*
+ * vt_diag.h — diagnostic entry points of the GB300 voxel renderer.
+ *
+ * These have no counterpart in the reference's Renderer interface: they
+ * expose intermediate results of the same kernels that vt.h drives (per-sample
+ * radiance, first hits, DDA results of arbitrary rays, event counters, the
+ * environment CDFs of a raw function) so that they can be compared with a CPU
+ * restatement of the reference shaders, and select the kernel form used by
+ * vt_job_render for measurement.
+ */
+#ifndef VT_DIAG_H
+#define VT_DIAG_H
+
+#include "vt.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Event counters (per launch, summed over paths):
+ * [0] paths, [1] DDA cells tested, [2] palette records read,
+ * [3] environment texel evaluations, [4] CDF entries probed,
+ * [5] emissive-list reads, [6] DDA segments started, [7] unused. */
+#define VT_DIAG_NUM_COUNTERS 8
+
+/* Trace caller-supplied rays through the job's scene with the DDA of
+ * src/shaders/shared/dda.h:7-100 (traverse with the default step cap).
+ * origins/dirs: n*3 floats in world space.  out: n*4 int32 =
+ * voxel x, y, z, flags (normal code | hit << 8 | ground << 9 | steps << 10),
+ * normal code = (nx+1) | (ny+1) << 2 | (nz+1) << 4 of the hit face. */
+VT_API int vt_diag_trace_rays(vt_job* job, const float* origins, const float* dirs,
+                              int64_t n, int32_t* out);
+
+/* Trace one sample per pixel with sample index `sample` without touching the
+ * accumulation: rgba receives the per-sample output (width*height*4 floats),
+ * hits (nullable) the first-hit record of each pixel (width*height*4 int32,
+ * same layout as vt_diag_trace_rays), counters (nullable) the event counts. */
+VT_API int vt_diag_samples(vt_job* job, int32_t sample, float* rgba, int32_t* hits,
+                           uint64_t* counters);
+
+/* Render like vt_job_render and also return the event counters of the
+ * launch (counters: VT_DIAG_NUM_COUNTERS entries). */
+VT_API int vt_diag_render_counted(vt_job* job, int32_t passes, uint64_t* counters,
+                                  int32_t* result);
+
+/* Kernel form used by vt_job_render and vt_render_batch when their options
+ * do not say: 1 = plain (one thread per pixel, one launch per pass),
+ * 2 = persistent (work queue over jobs and tiles). */
+VT_API int vt_diag_set_kernel(vt_context* ctx, int32_t kernel);
+
+/* Evaluate a builtin of the renderer on the GPU: fn 0 sin, 1 cos, 2 pow(a, b),
+ * 3 acos, 4 atan2(a, b), 5 log2, 6 exp2, 7 float -> half -> float. */
+VT_API int vt_diag_builtins(vt_context* ctx, int32_t fn, const float* a, const float* b,
+                            float* out, int64_t n);
+
+/* Build the importance-sampling CDFs of a raw non-negative function
+ * (width*height floats) on the GPU, without blur or sin(theta) weight:
+ * the known-answer examples of src/renderer/image.cpp:107-154. */
+VT_API int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int32_t width,
+                                     int32_t height, float* cdf_u, float* cdf_v,
+                                     float* integral);
+
+/* The cudaStream_t on which the context issues its work (for timing with
+ * CUDA events recorded on that stream). */
+VT_API int vt_diag_stream(vt_context* ctx, void** stream);
+
+/* Copy the environment's FP16 RGBA texels (width*height*4 uint16). */
+VT_API int vt_diag_env_texels(const vt_env* env, uint16_t* out, size_t bytes);
+
+/* Replace / read the 1024x1024 RGBA noise table used by VT_RNG_NOISE_TABLE
+ * (src/renderer/renderer.cpp:739-760).  By default the table holds
+ * (splitmix64(seed + i) >> 40) * 2^-24 for i in [0, 4M), seed 0. */
+VT_API int vt_diag_set_noise_table(vt_context* ctx, const float* rgba, size_t bytes);
+VT_API int vt_diag_get_noise_table(vt_context* ctx, float* rgba, size_t bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VT_DIAG_H */

@@ -1,0 +1,415 @@
+"""GPU parity: the CUDA kernels against the CPU restatement of the reference.
+
+Bit-exact for everything integer or index valued (DDA hits and faces,
+voxelizer occupancy, emissive lists) and, because both sides evaluate the
+same IEEE single-precision operations, for per-sample radiance too.  The
+converged image is compared with the FP64 oracle by relative RMSE <= 1e-3.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import close_all, gpu_setup, oracle_setup, reference_config, small_config1, small_config2
+from voxeltoy_gb300 import Env, Job, Scene, Server
+from voxeltoy_gb300 import _lib as L
+from voxeltoy_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+def same_bits(a, b):
+    """Bitwise float equality, any NaN equal to any NaN (NaN payloads differ
+    between the GPU and the host C library)."""
+    return (a.view(np.uint32) == b.view(np.uint32)) | (np.isnan(a) & np.isnan(b))
+
+
+def test_builtins_bitexact(ctx, orc):
+    rng = np.random.default_rng(0)
+    a = np.concatenate([rng.uniform(-30, 30, 100000), rng.uniform(-1, 1, 50000)]).astype(np.float32)
+    b = rng.uniform(0.01, 800, a.size).astype(np.float32)
+    pos = np.abs(a) + np.float32(1e-7)
+    for fn, x, y in [(0, a, None), (1, a, None), (2, pos, b), (3, np.clip(a, -1, 1), None), (4, a, b),
+                     (5, pos, None), (6, a * 4, None), (7, a * 1000, None)]:
+        got = ctx.builtins(fn, x, y)
+        want = orc.builtins(fn, x, y)
+        np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32), err_msg=f"fn {fn}")
+
+
+def _rays(rng, n):
+    """Half the rays start at the volume's entry point of a ray from a shell
+    around it (as the integrator clips primary rays, pathTracer.fs:183-196),
+    half start at random points inside the volume."""
+    d0 = rng.normal(size=(n, 3))
+    d0 /= np.linalg.norm(d0, axis=1, keepdims=True)
+    far = -1500.0 * d0
+    targets = rng.uniform(-450, 450, (n, 3))
+    dirs = targets - far
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    with np.errstate(divide="ignore"):
+        t0 = (-500.0 - far) / dirs
+        t1 = (500.0 - far) / dirs
+    tmin = np.minimum(t0, t1).max(axis=1)
+    origins = far + tmin[:, None] * dirs
+    inside = rng.uniform(-499, 499, (n, 3))
+    half = n // 2
+    origins[half:] = inside[half:]
+    return origins.astype(np.float32), dirs.astype(np.float32)
+
+
+def _special_rays():
+    o, d = [], []
+    for axis in range(3):
+        for s in (-1.0, 1.0):
+            v = np.zeros(3); v[axis] = s
+            o.append(-v * 900 + np.array([3.3, 7.1, -5.5])); d.append(v)
+    for dd in [(1, 1, 1), (-1, 1, -1), (1, -1, 0), (0, 1, 1)]:
+        v = np.array(dd, float); v /= np.linalg.norm(v)
+        o.append(-v * 900); d.append(v)
+    for eps in (1e-6, -1e-6, 5e-6):                       # grazing components
+        v = np.array([1.0, eps, 0.3]); o.append([-800, 12.0, 1.0]); d.append(v / np.linalg.norm(v))
+    o.append([0.0, 0.0, 0.0]); d.append([0.0, -1.0, 0.0])  # inside the volume
+    o.append([15.625, 100.0, 31.25]); d.append([0.0, 1.0, 0.0])  # on voxel faces
+    o.append([600.0, 600.0, 600.0]); d.append([1.0, 0.0, 0.0])   # outside, pointing away
+    return np.array(o, np.float32), np.array(d, np.float32)
+
+
+@pytest.mark.parametrize("quirks", [0, L.VT_QUIRK_GROUND])
+def test_trace_rays_bitexact(ctx, orc, quirks):
+    cfg = small_config1(edge=64)
+    cfg.settings.quirks = quirks
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        rng = np.random.default_rng(11)
+        o, d = _rays(rng, 200000)
+        so, sd = _special_rays()
+        o = np.concatenate([o, so]); d = np.concatenate([d, sd])
+        got = job.trace_rays(o, d)
+        want = orc.trace_rays(orc.Scene(cfg.voxels, cfg.palette), o, d, quirks)
+        np.testing.assert_array_equal(got, want)
+        hits = (got[:, 3] >> 8) & 1
+        assert 0.2 < hits.mean() < 0.95
+    finally:
+        close_all(job, scene, env)
+
+
+def test_env_build_bitexact(ctx, orc):
+    rgb = S.sky_sun_env(96, 48)
+    rgb[3, 5] = 70000.0   # beyond half range: stored as infinity in both
+    rgb[10, 40] = [0.0, 0.0, 0.0]
+    env = Env(ctx, np.ascontiguousarray(rgb))
+    try:
+        cu, cv, integral = env.cdf()
+        ref = orc.Env(rgb, chunk=32)
+        np.testing.assert_array_equal(env.texels(), ref.texels)
+        np.testing.assert_array_equal(cu, ref.cdf_u)
+        np.testing.assert_array_equal(cv, ref.cdf_v)
+        assert integral == np.float32(ref.integral)
+        seq = orc.Env(rgb, chunk=0)   # strictly sequential FP64 sums: within one float ulp
+        assert np.all(np.abs(cu - seq.cdf_u) <= np.spacing(np.float32(1.0)))
+    finally:
+        env.close()
+
+
+def test_gpu_cdf_known_answers(ctx):
+    cu, cv, _ = ctx.cdf_from_function(np.array([[1, 1, 0, 2, 1, 0, 5], [2, 1, 5, 0, 0, 1, 3],
+                                                [128, 0, 0, 0, 0, 0, 0]], np.float32))
+    assert cu[0].tolist() == [np.float32(x) for x in (0, 0.1, 0.2, 0.2, 0.4, 0.5, 0.5, 1.0)]
+    np.testing.assert_array_equal(cv, np.float32([0, 10 / 150, 22 / 150, 1]))
+
+
+def _compare_samples(ctx, orc, cfg, samples=(0, 1, 2), noise=False):
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        osc, oenv = oracle_setup(orc, cfg, scene, env)
+        table = ctx.noise_table() if noise else None
+        for smp in samples:
+            g_rgba, g_hits, g_cnt = job.samples_diag(smp)
+            o_rgba, o_hits, o_cnt = orc.render_samples(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height,
+                                                       smp, 32, noise=table)
+            np.testing.assert_array_equal(g_hits, o_hits, err_msg=f"first hits, sample {smp}")
+            bad = np.argwhere(~same_bits(g_rgba, o_rgba))
+            assert bad.size == 0, f"sample {smp}: {len(bad)} values differ, first {bad[:4].tolist()}"
+            np.testing.assert_array_equal(g_cnt[:7], o_cnt[:7])
+        return g_rgba
+    finally:
+        close_all(job, scene, env)
+
+
+def test_samples_bitexact_config1(ctx, orc):
+    img = _compare_samples(ctx, orc, small_config1())
+    assert np.isfinite(img).all() and img[..., :3].max() > 0.1
+
+
+def test_samples_bitexact_config2(ctx, orc):
+    cfg = small_config2()
+    img = _compare_samples(ctx, orc, cfg, samples=(0, 5))
+    assert np.isfinite(img).all()
+
+
+def test_samples_bitexact_reference_quirks(ctx, orc):
+    cfg = reference_config()
+    _compare_samples(ctx, orc, cfg, samples=(0, 3), noise=True)
+
+
+def test_samples_bitexact_reference_quirks_image_env(ctx, orc):
+    cfg = reference_config(seed=4)
+    cfg.env_rgb = S.sky_sun_env(48, 24, peak=200.0)
+    cfg.settings.background_rotation = 0.7
+    _compare_samples(ctx, orc, cfg, samples=(1,), noise=True)
+
+
+def test_samples_bitexact_ortho_wireframe_selection(ctx, orc):
+    cfg = small_config1(edge=32, w=33, h=29)
+    cfg.camera.lens_model = L.VT_LENS_ORTHOGRAPHIC
+    cfg.settings.wireframe_opacity = 0.6
+    cfg.settings.wireframe_thickness = 0.05
+    occ = np.argwhere(cfg.voxels > 0)
+    z, y, x = occ[len(occ) // 2]
+    cfg.settings.selected_voxel[:] = [int(x), int(y), int(z)]
+    cfg.settings.select_enabled = 1
+    _compare_samples(ctx, orc, cfg, samples=(0, 1))
+
+
+def test_accumulation_matches_oracle_average(ctx, orc):
+    cfg = small_config1(edge=48, w=40, h=32)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        job.render(6)
+        got = job.readback()
+        osc, oenv = oracle_setup(orc, cfg, scene, env)
+        want, _ = orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 6, 32)
+        np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
+        assert job.samples() == 6
+    finally:
+        close_all(job, scene, env)
+
+
+def test_plain_and_persistent_kernels_agree(ctx):
+    cfg = small_config2(edge=40, w=50, h=30)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        ctx.set_kernel(1)
+        job.render(5)
+        a = job.readback().copy()
+        job.reset()
+        ctx.set_kernel(2)
+        job.render(2)
+        job.render(3)
+        b = job.readback()
+        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+    finally:
+        ctx.set_kernel(2)
+        close_all(job, scene, env)
+
+
+def test_batch_equals_alone(ctx):
+    cfgs = [small_config1(edge=40, w=37, h=23, seed=5), small_config2(edge=32, w=64, h=48, seed=6),
+            small_config1(edge=24, w=16, h=70, seed=7)]
+    made = [gpu_setup(ctx, c) for c in cfgs]
+    try:
+        alone = []
+        for _s, _e, j in made:
+            j.render(4)
+            alone.append(j.readback().copy())
+            j.reset()
+        ctx.render_batch([j for _s, _e, j in made], 2, tile_pixels=64)
+        ctx.render_batch([j for _s, _e, j in made], 2, tile_pixels=96)
+        for (_s, _e, j), want in zip(made, alone):
+            np.testing.assert_array_equal(j.readback().view(np.uint32), want.view(np.uint32))
+    finally:
+        for m in made:
+            close_all(m[2], m[0], m[1])
+
+
+def test_server_results_equal_alone(ctx):
+    cfgs = [small_config1(edge=40, w=30, h=20, seed=8), small_config2(edge=32, w=24, h=24, seed=9),
+            small_config1(edge=32, w=40, h=10, seed=10)]
+    spps = [5, 7, 3]
+    made = [gpu_setup(ctx, c) for c in cfgs]
+    srv = Server(ctx, hbm_budget_bytes=1 << 30, max_active_jobs=2, passes_per_round=2)
+    try:
+        alone = []
+        for (_s, _e, j), spp in zip(made, spps):
+            for _ in range(spp):
+                j.render(1)
+            alone.append(j.readback().copy())
+        tickets = [srv.submit(s, e, c.camera, c.settings, c.width, c.height, spp)
+                   for (s, e, _j), c, spp in zip(made, cfgs, spps)]
+        for t, want, c in zip(tickets, alone, cfgs):
+            assert srv.wait(t, 60.0) == L.VT_OK
+            got, secs = srv.result(t, c.width, c.height)
+            assert secs >= 0.0
+            np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+        st = srv.stats()
+        assert st.completed == 3 and st.failed == 0
+    finally:
+        srv.close()
+        for m in made:
+            close_all(m[2], m[0], m[1])
+
+
+def _tri_soup(seed, n_small=3000, n_large=40, res=(96, 80, 64)):
+    rng = np.random.default_rng(seed)
+    ext = np.array(res, float)
+    small = rng.uniform(0, 1, (n_small, 1, 3)) * ext
+    small = small + rng.normal(0, 1.5, (n_small, 3, 3))
+    large = rng.uniform(0, 1, (n_large, 3, 3)) * ext
+    tris = np.concatenate([small, large]).reshape(-1, 3).astype(np.float32)
+    # a few exact axis-aligned and degenerate triangles
+    extra = np.array([[10, 10, 10], [30, 10, 10], [10, 30, 10], [5, 5, 5], [5, 5, 5], [9, 9, 9],
+                      [20.5, 20.5, 20.0], [40.5, 20.5, 20.0], [20.5, 40.5, 20.0]], np.float32)
+    v = np.concatenate([tris, extra])
+    return v, np.arange(len(v), dtype=np.uint32)
+
+
+@pytest.mark.parametrize("mode", [L.VT_VOXELIZE_THIN, L.VT_VOXELIZE_FAT])
+def test_voxelize_bitexact_triangle_soup(ctx, orc, mode):
+    res = (96, 80, 64)
+    v, idx = _tri_soup(3)
+    sc = Scene.voxelize(ctx, v, idx, res, mode=mode, placement=L.VT_MESH_VOXEL_SPACE)
+    try:
+        got = sc.voxels()
+        want = orc.voxelize(v, idx, res, mode, placement=0)
+        np.testing.assert_array_equal(got, want)
+        assert want.sum() > 1000
+    finally:
+        sc.close()
+
+
+@pytest.mark.parametrize("mode", [L.VT_VOXELIZE_THIN, L.VT_VOXELIZE_FAT])
+def test_voxelize_bitexact_icosphere(ctx, orc, mode):
+    v, f = S.fbm_displaced_icosphere(level=5, seed=4)
+    res = (128, 128, 128)
+    sc = Scene.voxelize(ctx, v, f, res, mode=mode, placement=L.VT_MESH_FIT_UNIT_CUBE)
+    try:
+        got = sc.voxels()
+        want = orc.voxelize(v, f, res, mode, placement=1)
+        np.testing.assert_array_equal(got, want)
+    finally:
+        sc.close()
+
+
+def test_emissive_pruning_matches_oracle(ctx, orc):
+    cfg = small_config2(edge=48)
+    sc = Scene.dense(ctx, cfg.voxels, cfg.palette, flags=L.VT_SCENE_AUTO_EMISSIVE | L.VT_SCENE_PRUNE_EMISSIVE)
+    try:
+        got = sc.emissive()
+        cand = np.flatnonzero(cfg.voxels.ravel() == 17).astype(np.int32)
+        want = orc.prune_emissive(cfg.voxels, cand)
+        np.testing.assert_array_equal(got, want)
+        assert 0 < len(got) < len(cand)
+    finally:
+        sc.close()
+
+
+def test_pick_matches_oracle(ctx, orc):
+    cfg = small_config1(edge=64, w=64, h=64)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        osc, _ = oracle_setup(orc, cfg, scene, env)
+        for x, y in [(32.5, 32.5), (10.0, 50.0), (0.5, 0.5), (60.2, 3.7)]:
+            d, vox = job.pick(x, y)
+            import ctypes as C
+            od = C.c_float()
+            ov = (C.c_int32 * 3)()
+            orc.lib().orc_pick(C.byref(orc.camera(cfg.camera)), C.byref(orc.settings(cfg.settings)),
+                               C.byref(osc.s), None, cfg.width, cfg.height, x, y, C.byref(od), ov)
+            assert d == od.value and tuple(vox) == tuple(ov)
+    finally:
+        close_all(job, scene, env)
+
+
+def test_converged_image_rmse_vs_fp64(ctx, orc):
+    cfg = small_config1(edge=64, w=64, h=64)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        job.render(48)
+        got = job.readback()[..., :3].astype(np.float64)
+        osc, oenv = oracle_setup(orc, cfg, scene, env)
+        ref, _ = orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 48, 64)
+        ref = ref[..., :3].astype(np.float64)
+        rel_rmse = np.sqrt(np.mean((got - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
+        assert rel_rmse <= 1e-3, rel_rmse
+    finally:
+        close_all(job, scene, env)
+
+
+def test_white_furnace_convex_box(ctx):
+    """A convex object under a constant environment L = 1 with a Lambert
+    albedo rho reflects exactly rho in expectation (NEE + MIS, no ground)."""
+    g = np.zeros((32, 32, 32), np.uint8)
+    g[8:24, 8:24, 8:24] = 1
+    sc = Scene.dense(ctx, g, [S.lambert(0.6)])
+    s = S.physical_settings(max_bounces=4)
+    cam = S.orbit_camera(distance=1800.0, theta_deg=110.0, phi_deg=30.0)
+    job = Job(ctx, sc, None, cam, s, 64, 64)
+    try:
+        job.render(256)
+        img = job.readback()[..., :3]
+        masks = [((job.samples_diag(k)[1][..., 3] >> 8) & 1).astype(bool) for k in range(8)]
+        any_hit = np.logical_or.reduce(masks)
+        all_hit = np.logical_and.reduce(masks)
+        # pixels whose whole 3x3 neighbourhood always / never hit (silhouettes excluded)
+        pad_any = np.pad(any_hit, 1, constant_values=True)
+        pad_all = np.pad(all_hit, 1, constant_values=False)
+        never = np.ones_like(any_hit)
+        always = np.ones_like(any_hit)
+        for dy in range(3):
+            for dx in range(3):
+                never &= ~pad_any[dy:dy + any_hit.shape[0], dx:dx + any_hit.shape[1]]
+                always &= pad_all[dy:dy + any_hit.shape[0], dx:dx + any_hit.shape[1]]
+        assert always.sum() > 200 and never.sum() > 200
+        np.testing.assert_allclose(img[never], 1.0, rtol=0, atol=1e-6)
+        assert abs(img[always].mean() - 0.6) < 0.01
+    finally:
+        close_all(job, sc)
+
+
+ABLATIONS = ["base", "thinlens", "image_env", "metal", "emissive", "rr", "all"]
+
+
+def _ablation_config(kind):
+    from voxeltoy_gb300 import scenes as S2
+    cfg = small_config1(edge=32, w=24, h=20, seed=12)
+    rng = np.random.default_rng(3)
+    if kind in ("thinlens", "all"):
+        cfg.camera.lens_model = L.VT_LENS_THIN_LENS
+        cfg.camera.lens_radius = 20.0
+    if kind in ("image_env", "all"):
+        cfg.env_rgb = S2.sky_sun_env(32, 16, peak=300.0)
+    if kind in ("metal", "all"):
+        cfg.palette = [S2.lambert(0.7), S2.metal(0.6, 0.2)]
+        cfg.voxels = cfg.voxels * rng.integers(1, 3, size=cfg.voxels.shape, dtype=np.uint8)
+    if kind in ("emissive", "all"):
+        cfg.palette = list(cfg.palette) + [S2.lambert(0.5, emission=(5, 5, 5))]
+        em = (rng.random(cfg.voxels.shape) < 0.05) & (cfg.voxels > 0)
+        cfg.voxels = cfg.voxels.copy()
+        cfg.voxels[em] = len(cfg.palette)
+        cfg.scene_flags = L.VT_SCENE_AUTO_EMISSIVE | L.VT_SCENE_PRUNE_EMISSIVE
+    if kind in ("rr", "all"):
+        cfg.settings.rr_start_bounce = 1
+    return cfg
+
+
+@pytest.mark.parametrize("kind", ABLATIONS)
+def test_samples_bitexact_ablation(ctx, orc, kind):
+    cfg = _ablation_config(kind)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        osc, oenv = oracle_setup(orc, cfg, scene, env)
+        report = []
+        for smp in (0, 1):
+            g, gh, gc = job.samples_diag(smp)
+            o, oh, oc = orc.render_samples(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, smp, 32)
+            diff = ~same_bits(g, o)
+            if diff.any() or not np.array_equal(gh, oh):
+                px = np.argwhere(diff.any(axis=-1))
+                rel = np.abs(g - o) / np.maximum(np.abs(o), 1e-30)
+                y, x = px[0] if len(px) else (0, 0)
+                report.append(f"sample {smp}: {len(px)} px differ, hits equal={np.array_equal(gh, oh)}, "
+                              f"max rel {rel.max():.3e}, first ({x},{y}) gpu {g[y, x].tolist()} cpu {o[y, x].tolist()} "
+                              f"counters gpu {gc[:7].tolist()} cpu {oc[:7].tolist()}")
+        assert not report, "\n".join(report)
+    finally:
+        close_all(job, scene, env)

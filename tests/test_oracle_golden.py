@@ -1,0 +1,123 @@
+"""Known-answer checks of the CPU oracle.
+
+Pins the oracle on the only golden vectors the reference itself documents
+(the CDF worked example of src/renderer/image.cpp:107-154 and the binary
+search example of src/shaders/envLight/envMapSample.h:10-21), on the
+published Philox-4x32-10 known-answer vectors, and on analytic answers.
+"""
+import numpy as np
+import pytest
+
+# image.cpp:107-124 -- one row of intensities and its normalised CDF
+ROW0 = [1, 1, 0, 2, 1, 0, 5]
+ROW0_CDF = [0.0, 0.1, 0.2, 0.2, 0.4, 0.5, 0.5, 1.0]
+# image.cpp:144-154 -- second row (sum 12) and a last row taking the total to 150
+ROW1 = [2, 1, 5, 0, 0, 1, 3]
+
+
+def test_cdf_row_example_reference_float(orc):
+    cu, cv = orc.cdf_reference_float(np.array([ROW0], np.float32))
+    np.testing.assert_allclose(cu[0], ROW0_CDF, rtol=0, atol=1e-7)
+    assert cv.tolist() == [0.0, 1.0]
+
+
+@pytest.mark.parametrize("chunk", [0, 32, 2])
+def test_cdf_row_example_fp64(orc, chunk):
+    cu, cv, _ = orc.cdf_from_function(np.array([ROW0], np.float32), chunk=chunk)
+    assert cu[0].tolist() == [np.float32(x) for x in ROW0_CDF]
+
+
+def test_cdf_marginal_example(orc):
+    last = [128, 0, 0, 0, 0, 0, 0]
+    func = np.array([ROW0, ROW1, last], np.float32)
+    _, cv, _ = orc.cdf_from_function(func)
+    np.testing.assert_array_equal(cv, np.float32([0.0, 10 / 150, 22 / 150, 1.0]))
+    assert f"{cv[1]:.2f}"[:3] == "0.0" and int(cv[1] * 100) == 6      # the comment's 0.06
+    assert int(cv[2] * 100) == 14                                       # the comment's 0.14
+    _, cvr = orc.cdf_reference_float(func)
+    np.testing.assert_allclose(cvr, cv, rtol=0, atol=2e-7)
+
+
+def test_cdf_black_rows_are_uniform(orc):
+    func = np.zeros((3, 4), np.float32)
+    func[1] = [0, 3, 0, 1]
+    cu, cv, integral = orc.cdf_from_function(func)
+    assert cu[0].tolist() == [0.0, 0.25, 0.5, 0.75, 1.0]
+    assert cu[1].tolist() == [0.0, 0.0, 0.75, 0.75, 1.0]
+    assert cv.tolist() == [0.0, 0.0, 1.0, 1.0]
+    allblack, cvb, ib = orc.cdf_from_function(np.zeros((2, 2), np.float32))
+    assert cvb.tolist() == [0.0, 0.5, 1.0] and ib == 0.0
+
+
+def test_binary_search_example(orc):
+    # envMapSample.h:10-21: u = 0.7 lands in the bracket starting at index 3
+    assert orc.binary_search([0, 0.1, 0.5, 0.6, 0.75, 0.9, 1.0], 0.7) == 3
+    cdf = [0, 0.1, 0.5, 0.6, 0.75, 0.9, 1.0]
+    for u, k in [(0.0, 0), (0.09, 0), (0.1, 1), (0.5999, 2), (0.6, 3), (0.95, 5), (0.99999, 5)]:
+        assert orc.binary_search(cdf, u) == k
+
+
+def test_philox_known_answers(orc):
+    # Philox-4x32-10 known-answer vectors published with the algorithm (Salmon et al. 2011)
+    cases = [
+        ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+        ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+        ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+    ]
+    for ctr, key, want in cases:
+        assert orc.philox(ctr, key).tolist() == want
+
+
+def test_constant_env_integral(orc):
+    # a constant image L gives uniform CDFs and integral 2 pi^2 * L * mean(sin theta)
+    w, h = 16, 8
+    rgb = np.full((h, w, 3), 2.0, np.float32)
+    env = orc.Env(rgb, chunk=0)
+    np.testing.assert_allclose(env.cdf_u[0], np.arange(w + 1) / w, atol=1e-7)
+    st = np.sin(np.pi * (np.arange(h) + 0.5) / h)
+    np.testing.assert_allclose(env.cdf_v, np.concatenate([[0], np.cumsum(st) / st.sum()]), atol=2e-7)
+    lum = 2.0 * (0.2126 + 0.7152 + 0.0722)
+    assert env.integral == pytest.approx(2 * np.pi ** 2 * lum * st.mean(), rel=1e-6)
+
+
+def test_delta_env_step_cdf(orc):
+    w, h = 32, 16
+    rgb = np.zeros((h, w, 3), np.float32)
+    rgb[5, 9] = 100.0
+    env = orc.Env(rgb, chunk=32)
+    # after the 3x3 blur only rows 4..6 carry weight and row 5's mass sits in columns 8..10
+    cv = env.cdf_v
+    assert cv[4] == 0.0 and cv[7] == 1.0
+    assert env.cdf_u[5][8] == 0.0 and env.cdf_u[5][11] == 1.0
+
+
+def test_prune_emissive_against_numpy(orc):
+    rng = np.random.default_rng(5)
+    g = (rng.random((12, 10, 9)) < 0.6).astype(np.uint8)
+    g[3:8, 3:8, 3:8] = 1
+    em = np.flatnonzero(g.ravel()).astype(np.int32)
+    rng.shuffle(em)
+    pruned = orc.prune_emissive(g, em)
+
+    def visible(i):
+        z, rem = divmod(int(i), 10 * 9)
+        y, x = divmod(rem, 9)
+        for dx, dy, dz in [(1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1)]:
+            nx, ny, nz = x + dx, y + dy, z + dz
+            if not (0 <= nx < 9 and 0 <= ny < 10 and 0 <= nz < 12) or g[nz, ny, nx] == 0:
+                return True
+        return False
+
+    keep = [v for v in em if visible(v)]
+    assert sorted(pruned.tolist()) == sorted(keep)
+    # swap-with-last removal order (import.cpp:180-203)
+    lst = em.tolist()
+    i = 0
+    while i < len(lst):
+        if not visible(lst[i]):
+            lst[i] = lst[-1]
+            lst.pop()
+        else:
+            i += 1
+    assert pruned.tolist() == lst

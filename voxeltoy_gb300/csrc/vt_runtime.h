@@ -1,0 +1,90 @@
+// vt_runtime.h — host-side objects behind the opaque C handles.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/vt.h"
+#include "vt_internal.h"
+#include "vt_kernels.h"
+
+struct vt_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0;          // 0 = unlimited
+  uint64_t in_use = 0;          // bytes held through alloc()
+  int sm_count = 0;
+  int kernel = 2;               // 1 plain, 2 persistent
+  vt_log_fn log_fn = nullptr;
+  void* log_user = nullptr;
+  std::mutex mu;
+  std::unordered_map<void*, size_t> sizes;
+  float4* noise = nullptr;
+  void* scratch = nullptr;      // reusable device scratch for diagnostics and picks
+  size_t scratch_bytes = 0;
+  vt::JobEntry* d_jobs = nullptr;
+  size_t d_jobs_bytes = 0;
+  unsigned long long* d_counters = nullptr;
+  unsigned long long* d_queue = nullptr;
+  int32_t* d_error = nullptr;
+
+  int alloc(void** ptr, size_t bytes);   // budget-checked cudaMalloc
+  void release(void* ptr);
+  int ensure_scratch(size_t bytes);
+  int ensure_noise();
+  void log(const char* fmt, ...);
+};
+
+struct vt_scene {
+  vt_context* ctx = nullptr;
+  int32_t res[3] = {0, 0, 0};
+  int32_t bdim[3] = {0, 0, 0};
+  float bmin[3], bmax[3], vsize[3];
+  uint8_t* grid = nullptr;
+  unsigned long long* bricks = nullptr;
+  uint4* palette = nullptr;
+  int32_t n_palette = 0;
+  int32_t* emissive = nullptr;
+  int64_t n_emissive = 0;
+  uint64_t bytes = 0;
+  std::vector<vt_material> host_palette;
+  ~vt_scene();
+};
+
+struct vt_env {
+  vt_context* ctx = nullptr;
+  int32_t w = 0, h = 0;
+  uint2* texels = nullptr;
+  float* cdf_u = nullptr;
+  float* cdf_v = nullptr;
+  float integral = 0.0f;
+  ~vt_env();
+};
+
+struct vt_job {
+  vt_context* ctx = nullptr;
+  const vt_scene* scene = nullptr;
+  const vt_env* env = nullptr;
+  vt_camera cam;
+  vt_render_settings set;
+  int32_t w = 0, h = 0;
+  float4* sum = nullptr;
+  float4* comp = nullptr;
+  float4* staging = nullptr;
+  int32_t samples = 0;
+  vt::Frame frame;
+  vt::JobDev dev;
+  ~vt_job();
+};
+
+namespace vt {
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+int build_frame(vt_job* j);
+// passes[i] samples per pixel for jobs[i]; kernel 1 = plain, 2 = persistent.
+int render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int kernel,
+                int tile_pixels, int blocks_per_sm, bool count);
+}  // namespace vt

@@ -1,0 +1,439 @@
+// vt_scene.cu — kernels that build the device-resident scene and environment:
+//   occupancy bit-bricks, emissive-voxel pruning flags and discovery, the
+//   environment map's FP16 texels and importance-sampling CDFs (FP64 prefix
+//   sums), and the triangle/voxel-overlap voxelizer.
+#include <cuda_fp16.h>
+#include "vt_kernels.h"
+#include "vt_builtins.h"
+
+namespace vt {
+
+// ------------------------------------------------------------- bit-bricks
+// One thread per 4x4x4 brick gathers its 64 voxels into one word.
+__global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int32_t ry, int32_t rz,
+                               unsigned long long* __restrict__ bricks, int32_t bx, int32_t by, int32_t bz) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nb = (int64_t)bx * by * bz;
+  if (b >= nb) return;
+  const int x0 = (int)(b % bx) * 4;
+  const int y0 = (int)((b / bx) % by) * 4;
+  const int z0 = (int)(b / ((int64_t)bx * by)) * 4;
+  unsigned long long w = 0ull;
+  for (int dz = 0; dz < 4; ++dz) {
+    const int z = z0 + dz;
+    if (z >= rz) break;
+    for (int dy = 0; dy < 4; ++dy) {
+      const int y = y0 + dy;
+      if (y >= ry) break;
+      const size_t row = (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z);
+      for (int dx = 0; dx < 4; ++dx) {
+        const int x = x0 + dx;
+        if (x >= rx) break;
+        if (grid[row + x] != 0) w |= 1ull << (dx | (dy << 2) | (dz << 4));
+      }
+    }
+  }
+  bricks[b] = w;
+}
+
+cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
+                                unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
+                                cudaStream_t st) {
+  const int64_t nb = (int64_t)bx * by * bz;
+  if (nb <= 0) return cudaSuccess;
+  k_build_bricks<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(grid, rx, ry, rz, bricks, bx, by, bz);
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------- emissive voxels
+// keep[i] = 1 if emissive voxel i has an empty or out-of-range 6-neighbour
+// (anyVisibleFace, src/renderer/import.cpp:133-178).
+__global__ void k_emissive_flags(const uint8_t* __restrict__ grid, int32_t rx, int32_t ry, int32_t rz,
+                                 const int32_t* __restrict__ emissive, int64_t n, uint8_t* __restrict__ keep) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t v = emissive[i];
+  const int64_t sxy = (int64_t)rx * ry;
+  const int z = (int)(v / sxy);
+  const int64_t r = v - (int64_t)z * sxy;
+  const int y = (int)(r / rx);
+  const int x = (int)(r - (int64_t)y * rx);
+  const int off[6][3] = {{1, 0, 0}, {-1, 0, 0}, {0, 1, 0}, {0, -1, 0}, {0, 0, 1}, {0, 0, -1}};
+  bool visible = false;
+  for (int k = 0; k < 6 && !visible; ++k) {
+    const int nx = x + off[k][0], ny = y + off[k][1], nz = z + off[k][2];
+    if (nx < 0 || nx >= rx || ny < 0 || ny >= ry || nz < 0 || nz >= rz) { visible = true; break; }
+    if (grid[(size_t)nx + (size_t)rx * ((size_t)ny + (size_t)ry * (size_t)nz)] == 0) visible = true;
+  }
+  keep[i] = visible ? 1 : 0;
+}
+
+cudaError_t launch_emissive_flags(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
+                                  const int32_t* emissive, int64_t n, uint8_t* keep, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  k_emissive_flags<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(grid, rx, ry, rz, emissive, n, keep);
+  return cudaGetLastError();
+}
+
+// Linear indices of voxels whose palette entry emits (emissive_entry[g] != 0),
+// appended in arbitrary order; the host sorts them.
+__global__ void k_find_emissive(const uint8_t* __restrict__ grid, int64_t n_voxels,
+                                const uint8_t* __restrict__ emissive_entry, int32_t* out,
+                                unsigned long long* count, int64_t capacity) {
+  __shared__ uint8_t s_em[256];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) s_em[i] = emissive_entry[i];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_voxels;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const uint8_t g = grid[i];
+    const bool e = s_em[g] != 0;
+    const unsigned mask = __ballot_sync(__activemask(), e);
+    if (e) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(mask) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(mask));
+      base = __shfl_sync(mask, base, leader);
+      const unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
+      if ((int64_t)slot < capacity) out[slot] = (int32_t)i;
+    }
+  }
+}
+
+cudaError_t launch_find_emissive(const uint8_t* grid, int64_t n_voxels, const uint8_t* emissive_entry,
+                                 int32_t* out, unsigned long long* count, int64_t capacity,
+                                 cudaStream_t st) {
+  if (n_voxels <= 0) return cudaSuccess;
+  int64_t blocks = (n_voxels + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  k_find_emissive<<<(unsigned)blocks, 256, 0, st>>>(grid, n_voxels, emissive_entry, out, count, capacity);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ environment
+// Three-tap Gaussian (sigma = 0.75 px) normalised to sum 1:
+//   w_side = e / (1 + 2e), w_mid = 1 / (1 + 2e), e = exp(-1 / (2 * 0.75^2)).
+#define VT_BLUR_SIDE 0.225604179501533508f
+#define VT_BLUR_MID 0.548791640996932983f
+
+// FP16 texels (A = 1) and the luminance of the quantised RGB
+// (generateImageFunction's channel_sum, src/renderer/image.cpp:326-335).
+__global__ void k_env_texels(const float* __restrict__ rgb, int64_t n, uint2* __restrict__ texels,
+                             float* __restrict__ lum) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint16_t r = vtb::f2h(vtb::clamp_half(rgb[3 * i])), g = vtb::f2h(vtb::clamp_half(rgb[3 * i + 1])),
+                 b = vtb::f2h(vtb::clamp_half(rgb[3 * i + 2]));
+  texels[i] = make_uint2((uint32_t)r | ((uint32_t)g << 16), (uint32_t)b | (0x3c00u << 16));
+  const float fr = vtb::h2f(r), fg = vtb::h2f(g), fb = vtb::h2f(b);
+  lum[i] = (fr * 0.2126f + fg * 0.7152f) + fb * 0.0722f;
+}
+
+// 3x3 separable blur, clamp to edge (image.cpp:337-342), then the sin(theta)
+// weight and the max(0, .) of calculateImageIntegral (image.cpp:361-374).
+// Pass 0: horizontal into tmp; pass 1: vertical, * sin_theta[y] into func.
+__global__ void k_env_blur(const float* __restrict__ src, float* __restrict__ dst, int32_t w, int32_t h,
+                           int pass, const float* __restrict__ sin_theta) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (int64_t)w * h) return;
+  const int x = (int)(i % w), y = (int)(i / w);
+  float a, b, c;
+  if (pass == 0) {
+    const int xm = x > 0 ? x - 1 : 0, xp = x < w - 1 ? x + 1 : w - 1;
+    a = src[(int64_t)y * w + xm]; b = src[i]; c = src[(int64_t)y * w + xp];
+  } else {
+    const int ym = y > 0 ? y - 1 : 0, yp = y < h - 1 ? y + 1 : h - 1;
+    a = src[(int64_t)ym * w + x]; b = src[i]; c = src[(int64_t)yp * w + x];
+  }
+  float v = (VT_BLUR_SIDE * a + VT_BLUR_MID * b) + VT_BLUR_SIDE * c;
+  if (pass == 1) v = vtb::gmax(0.0f, v) * sin_theta[y];
+  dst[i] = v;
+}
+
+// Exclusive prefix sums in FP64 with a fixed association order, so that the
+// CPU restatement reproduces them exactly: consecutive chunks of 32 inputs
+// are summed left to right, chunk offsets are accumulated left to right, and
+// element prefix = chunk offset + in-chunk prefix.  out[0] = 0, out[n] = total.
+// One warp; offs holds ceil(n/32) doubles.
+template <typename T>
+__device__ void warp_chunked_prefix(const T* in, int n, double* out, double* offs) {
+  const int lane = threadIdx.x & 31;
+  const int chunks = (n + 31) / 32;
+  for (int c = lane; c < chunks; c += 32) {
+    double acc = 0.0;
+    const int end = min(n, (c + 1) * 32);
+    for (int j = c * 32; j < end; ++j) { acc = acc + (double)in[j]; out[j + 1] = acc; }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    out[0] = 0.0;
+    double o = 0.0;
+    offs[0] = 0.0;
+    for (int c = 1; c < chunks; ++c) { o = o + out[c * 32]; offs[c] = o; }
+  }
+  __syncwarp();
+  for (int c = lane; c < chunks; c += 32) {
+    if (c == 0) continue;
+    const double o = offs[c];
+    const int end = min(n, (c + 1) * 32);
+    for (int j = c * 32; j < end; ++j) out[j + 1] = o + out[j + 1];
+  }
+  __syncwarp();
+}
+
+// One warp per row (image.cpp:212-247): FP64 prefixes of the row function,
+// normalised conditional CDF (uniform if the row is black), row integral =
+// row sum / width.
+__global__ void k_cdf_rows(const float* __restrict__ func, int32_t w, int32_t h, double* __restrict__ pre_all,
+                           float* __restrict__ cdf_u, double* __restrict__ row_int) {
+  extern __shared__ double s_offs[];
+  const int row = blockIdx.x;
+  const int lane = threadIdx.x & 31;
+  if (row >= h) return;
+  double* pre = pre_all + (int64_t)row * (w + 1);
+  warp_chunked_prefix(func + (int64_t)row * w, w, pre, s_offs);
+  const double total = pre[w];
+  float* out = cdf_u + (int64_t)row * (w + 1);
+  for (int x = lane; x <= w; x += 32) {
+    if (total > 0.0) out[x] = (float)(pre[x] / total);
+    else out[x] = (float)x / (float)w;
+  }
+  if (lane == 0) row_int[row] = total / (double)w;
+}
+
+// Marginal CDF over the row integrals (image.cpp:251-280) and the radiance
+// integral 2 pi^2 * mean(f) (image.cpp:381-386).  One warp.
+__global__ void k_cdf_marginal(const double* __restrict__ row_int, int32_t h, double* __restrict__ pre,
+                               float* __restrict__ cdf_v, float* integral) {
+  extern __shared__ double s_offs[];
+  const int lane = threadIdx.x & 31;
+  warp_chunked_prefix(row_int, h, pre, s_offs);
+  const double total = pre[h];
+  for (int y = lane; y <= h; y += 32) {
+    if (total > 0.0) cdf_v[y] = (float)(pre[y] / total);
+    else cdf_v[y] = (float)y / (float)h;
+  }
+  if (lane == 0 && integral) {
+    *integral = (float)((total / (double)h) * (2.0 * 3.14159265358979323846 * 3.14159265358979323846));
+  }
+}
+
+cudaError_t launch_cdf(const float* func, int32_t w, int32_t h, const EnvScratch& S, float* cdf_u,
+                       float* cdf_v, float* integral, cudaStream_t st) {
+  const size_t sm_rows = sizeof(double) * (size_t)((w + 31) / 32);
+  const size_t sm_marg = sizeof(double) * (size_t)((h + 31) / 32);
+  k_cdf_rows<<<h, 32, sm_rows, st>>>(func, w, h, S.row_pre, cdf_u, S.row_int);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_cdf_marginal<<<1, 32, sm_marg, st>>>(S.row_int, h, S.marg_pre, cdf_v, integral);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, const EnvScratch& S, uint2* texels,
+                             float* cdf_u, float* cdf_v, float* integral, cudaStream_t st) {
+  const int64_t n = (int64_t)w * h;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  k_env_texels<<<blocks, 256, 0, st>>>(rgb, n, texels, S.lum);
+  k_env_blur<<<blocks, 256, 0, st>>>(S.lum, S.tmp, w, h, 0, S.sin_theta);
+  k_env_blur<<<blocks, 256, 0, st>>>(S.tmp, S.func, w, h, 1, S.sin_theta);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_cdf(S.func, w, h, S, cdf_u, cdf_v, integral, st);
+}
+
+// --------------------------------------------------------------- voxelizer
+// Rauwendaal & Bailey, "Hybrid Computational Voxelization Using the Graphics
+// Pipeline" (JCGT 2013) as implemented by src/shaders/shared/voxelize.gs:55-251
+// and src/voxelize/cpuVoxelizer.cpp:42-235: project on the dominant axis,
+// test the XY edge functions per column, derive the Z range from the plane,
+// test the YZ and ZX edge functions per voxel.  mode 0 = THIN (6-separating,
+// figure 18), 1 = FAT (conservative, figure 17).
+struct TriSetup {
+  float d_xy[3], d_yz[3], d_zx[3];
+  float n_xy[3][2], n_yz[3][2], n_zx[3][2];
+  float nproj[3];
+  float dmin, dmax, nz_inv;
+  int perm;           // 0: swizzled yzx, 1: zxy, 2: identity
+  int lo[3], hi[3];   // voxel index range in swizzled space
+  bool valid;
+};
+
+__device__ __forceinline__ int sat_int(float f) {
+  // float -> int with NaN and out-of-range values mapped into +-1e9
+  if (f >= -1.0e9f && f <= 1.0e9f) return (int)f;
+  return f > 0.0f ? 1000000000 : -1000000000;
+}
+
+__device__ __forceinline__ void edge_normal(float ea, float eb, bool pos, float* nrm) {
+  // pos ? vec2(-eb, ea) : vec2(eb, -ea) for an edge (ea, eb)
+  if (pos) { nrm[0] = -eb; nrm[1] = ea; } else { nrm[0] = eb; nrm[1] = -ea; }
+}
+
+__device__ __forceinline__ float edge_d(const float* nrm, float pa, float pb, int mode) {
+  if (mode == 0) {
+    // dot(n, .5 - v) + 0.5 * max(|n.x|, |n.y|)   (voxelize.gs:140-150)
+    return (nrm[0] * (0.5f - pa) + nrm[1] * (0.5f - pb)) + 0.5f * vtb::gmax(fabsf(nrm[0]), fabsf(nrm[1]));
+  }
+  // -dot(n, v) + max(0, n.x) + max(0, n.y)      (voxelize.gs:152-162)
+  return (-(nrm[0] * pa + nrm[1] * pb) + vtb::gmax(0.0f, nrm[0])) + vtb::gmax(0.0f, nrm[1]);
+}
+
+__device__ bool tri_setup(const float* V, const uint32_t* I, int64_t t, int32_t rx, int32_t ry, int32_t rz,
+                          int mode, TriSetup& S) {
+  float v[3][3];
+  for (int k = 0; k < 3; ++k) {
+    const uint32_t vi = I[3 * t + k];
+    v[k][0] = V[3 * (int64_t)vi]; v[k][1] = V[3 * (int64_t)vi + 1]; v[k][2] = V[3 * (int64_t)vi + 2];
+  }
+  // n = cross(v1 - v0, v2 - v1)   (voxelize.gs:62)
+  const float a0 = v[1][0] - v[0][0], a1 = v[1][1] - v[0][1], a2 = v[1][2] - v[0][2];
+  const float b0 = v[2][0] - v[1][0], b1 = v[2][1] - v[1][1], b2 = v[2][2] - v[1][2];
+  float n[3] = {a1 * b2 - b1 * a2, a2 * b0 - b2 * a0, a0 * b1 - b0 * a1};
+  const float ax = fabsf(n[0]), ay = fabsf(n[1]), az = fabsf(n[2]);
+  int perm;
+  if (ax >= ay && ax >= az) perm = 0;        // look down X: xyz <- yzx
+  else if (ay >= ax && ay >= az) perm = 1;   // look down Y: xyz <- zxy
+  else perm = 2;
+  if (perm != 2) {
+    const int i0 = perm == 0 ? 1 : 2, i1 = perm == 0 ? 2 : 0, i2 = perm == 0 ? 0 : 1;
+    for (int k = 0; k < 3; ++k) {
+      const float p0 = v[k][i0], p1 = v[k][i1], p2 = v[k][i2];
+      v[k][0] = p0; v[k][1] = p1; v[k][2] = p2;
+    }
+    const float m0 = n[i0], m1 = n[i1], m2 = n[i2];
+    n[0] = m0; n[1] = m1; n[2] = m2;
+  }
+  S.perm = perm;
+  const int res[3] = {rx, ry, rz};
+  for (int c = 0; c < 3; ++c) {
+    const float mn = vtb::gmin(vtb::gmin(v[0][c], v[1][c]), v[2][c]);
+    const float mx = vtb::gmax(vtb::gmax(v[0][c], v[1][c]), v[2][c]);
+    // ivec3(clamp(floor(min), 0, res)) with the unswizzled resolution (voxelize.gs:247-248)
+    S.lo[c] = min(max(sat_int(floorf(mn)), 0), res[c]);
+    S.hi[c] = min(max(sat_int(ceilf(mx)), 0), res[c]);
+  }
+  float e[3][3];
+  for (int c = 0; c < 3; ++c) {
+    e[0][c] = v[1][c] - v[0][c];
+    e[1][c] = v[2][c] - v[1][c];
+    e[2][c] = v[0][c] - v[2][c];
+  }
+  for (int k = 0; k < 3; ++k) {
+    edge_normal(e[k][0], e[k][1], n[2] >= 0.0f, S.n_xy[k]);   // (x, y)
+    edge_normal(e[k][1], e[k][2], n[0] >= 0.0f, S.n_yz[k]);   // (y, z)
+    edge_normal(e[k][2], e[k][0], n[1] >= 0.0f, S.n_zx[k]);   // (z, x)
+    S.d_xy[k] = edge_d(S.n_xy[k], v[k][0], v[k][1], mode);
+    S.d_yz[k] = edge_d(S.n_yz[k], v[k][1], v[k][2], mode);
+    S.d_zx[k] = edge_d(S.n_zx[k], v[k][2], v[k][0], mode);
+  }
+  const bool neg = n[2] < 0.0f;
+  S.nproj[0] = neg ? -n[0] : n[0]; S.nproj[1] = neg ? -n[1] : n[1]; S.nproj[2] = neg ? -n[2] : n[2];
+  const float dtri = (S.nproj[0] * v[0][0] + S.nproj[1] * v[0][1]) + S.nproj[2] * v[0][2];
+  if (mode == 0) {
+    S.dmin = dtri - (S.nproj[0] * 0.5f + S.nproj[1] * 0.5f);  // voxelize.gs:169
+    S.dmax = S.dmin;
+  } else {
+    S.dmin = (dtri - vtb::gmax(S.nproj[0], 0.0f)) - vtb::gmax(S.nproj[1], 0.0f);   // :171
+    S.dmax = (dtri - vtb::gmin(S.nproj[0], 0.0f)) - vtb::gmin(S.nproj[1], 0.0f);   // :172
+  }
+  S.valid = S.nproj[2] != 0.0f;   // zero-area triangles cover nothing
+  S.nz_inv = 1.0f / S.nproj[2];
+  return S.valid;
+}
+
+__device__ __forceinline__ void tri_column(const TriSetup& S, int px, int py, int mode, int32_t rx, int32_t ry,
+                                           int32_t rz, uint8_t* grid, uint8_t value) {
+  bool xy = true;
+  for (int k = 0; k < 3; ++k) {
+    const float dd = S.d_xy[k] + (S.n_xy[k][0] * (float)px + S.n_xy[k][1] * (float)py);
+    xy = xy && (dd >= 0.0f);
+  }
+  if (!xy) return;
+  const float dnp = S.nproj[0] * (float)px + S.nproj[1] * (float)py;
+  const float zmin_i = (-dnp + S.dmin) * S.nz_inv;
+  const float zmax_i = (-dnp + S.dmax) * S.nz_inv;
+  const float zmin_f = floorf(zmin_i), zmax_c = ceilf(zmax_i);
+  int zmin = sat_int(zmin_f) - (zmin_f == zmin_i ? 1 : 0);
+  int zmax = sat_int(zmax_c) + (zmax_c == zmax_i ? 1 : 0);
+  zmin = max(S.lo[2], zmin);
+  zmax = min(S.hi[2], zmax);
+  for (int pz = zmin; pz < zmax; ++pz) {
+    bool ok = true;
+    for (int k = 0; k < 3; ++k) {
+      const float dyz = S.d_yz[k] + (S.n_yz[k][0] * (float)py + S.n_yz[k][1] * (float)pz);
+      const float dzx = S.d_zx[k] + (S.n_zx[k][0] * (float)pz + S.n_zx[k][1] * (float)px);
+      ok = ok && (dyz >= 0.0f) && (dzx >= 0.0f);
+    }
+    if (!ok) continue;
+    // unswizzle (voxelize.gs:40-48): yzx -> (z, x, y), zxy -> (y, z, x)
+    int ox, oy, oz;
+    if (S.perm == 0) { ox = pz; oy = px; oz = py; }
+    else if (S.perm == 1) { ox = py; oy = pz; oz = px; }
+    else { ox = px; oy = py; oz = pz; }
+    // imageStore outside the image has no effect
+    if (ox < 0 || oy < 0 || oz < 0 || ox >= rx || oy >= ry || oz >= rz) continue;
+    grid[(size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz)] = value;
+  }
+  (void)mode;
+}
+
+constexpr int kLargeColumns = 64;
+
+// One thread per triangle for triangles whose XY footprint is small; larger
+// ones are appended to a list for the block-per-triangle kernel.
+__global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restrict__ I, int64_t n_tris,
+                            int32_t rx, int32_t ry, int32_t rz, int mode, uint8_t* grid, uint8_t value,
+                            int64_t* large, unsigned long long* n_large) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n_tris) return;
+  TriSetup S;
+  if (!tri_setup(V, I, t, rx, ry, rz, mode, S)) return;
+  const int64_t cols = (int64_t)(S.hi[0] - S.lo[0]) * (int64_t)(S.hi[1] - S.lo[1]);
+  if (cols > kLargeColumns) {
+    const unsigned long long slot = atomicAdd(n_large, 1ull);
+    large[slot] = t;
+    return;
+  }
+  for (int px = S.lo[0]; px < S.hi[0]; ++px)
+    for (int py = S.lo[1]; py < S.hi[1]; ++py) tri_column(S, px, py, mode, rx, ry, rz, grid, value);
+}
+
+__global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restrict__ I, const int64_t* large,
+                            const unsigned long long* n_large, int32_t rx, int32_t ry, int32_t rz, int mode,
+                            uint8_t* grid, uint8_t value) {
+  __shared__ TriSetup S;
+  const unsigned long long n = *n_large;
+  for (unsigned long long k = blockIdx.x; k < n; k += gridDim.x) {
+    __syncthreads();
+    if (threadIdx.x == 0) tri_setup(V, I, large[k], rx, ry, rz, mode, S);
+    __syncthreads();
+    const int wx = S.hi[0] - S.lo[0], wy = S.hi[1] - S.lo[1];
+    const int64_t cols = (int64_t)wx * wy;
+    for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) {
+      const int px = S.lo[0] + (int)(c / wy), py = S.lo[1] + (int)(c % wy);
+      tri_column(S, px, py, mode, rx, ry, rz, grid, value);
+    }
+  }
+}
+
+cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indices, int64_t n_tris,
+                            int32_t rx, int32_t ry, int32_t rz, int32_t mode, uint8_t* grid,
+                            uint8_t value, cudaStream_t st) {
+  if (n_tris <= 0) return cudaSuccess;
+  int64_t* large = nullptr;
+  unsigned long long* n_large = nullptr;
+  cudaError_t e = cudaMallocAsync(&large, sizeof(int64_t) * n_tris + 16, st);
+  if (e != cudaSuccess) return e;
+  e = cudaMallocAsync(&n_large, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) { cudaFreeAsync(large, st); return e; }
+  cudaMemsetAsync(n_large, 0, sizeof(unsigned long long), st);
+  k_vox_small<<<(unsigned)((n_tris + 127) / 128), 128, 0, st>>>(verts_voxel_space, indices, n_tris, rx, ry, rz,
+                                                                mode, grid, value, large, n_large);
+  k_vox_large<<<152 * 4, 256, 0, st>>>(verts_voxel_space, indices, large, n_large, rx, ry, rz, mode, grid, value);
+  e = cudaGetLastError();
+  cudaFreeAsync(large, st);
+  cudaFreeAsync(n_large, st);
+  return e;
+}
+
+}  // namespace vt

@@ -1,0 +1,797 @@
+// vt_shade.cuh — device code of one progressive path sample, written as a
+// per-lane state machine: a path alternates between DDA segments (the hot
+// loop) and segment-end events (shading, light sampling, BSDF sampling).
+// Both the plain kernel (one launch per pass) and the persistent kernel
+// (many jobs and passes per launch) drive this same state machine, so every
+// form produces the same bits for the same (job, pixel, sample).
+//
+// Semantics follow the reference integrator pass
+// (src/shaders/integrator/pathTracer.fs:64-296 and the headers it includes);
+// each function cites the lines it implements.  Arithmetic is written in the
+// reference's expression order with multiply-add contraction disabled
+// (-fmad=false) so that the results equal the CPU restatement bit for bit.
+#pragma once
+
+#include <cuda_fp16.h>
+#include "vt_internal.h"
+#include "vt_builtins.h"
+
+namespace vt {
+
+#define VT_D __device__ __forceinline__
+
+// constants.h:1-3 (float literals)
+constexpr float kPI = 3.14159265359f;
+constexpr float kTWO_PI = 6.28318530718f;
+constexpr float kINV_TWOPI = 0.15915494309f;
+
+// ------------------------------------------------------------------ vectors
+struct v3 { float x, y, z; };
+VT_D v3 mk3(float x, float y, float z) { v3 r; r.x = x; r.y = y; r.z = z; return r; }
+VT_D v3 operator+(v3 a, v3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+VT_D v3 operator-(v3 a, v3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+VT_D v3 operator*(v3 a, v3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+VT_D v3 operator/(v3 a, v3 b) { return mk3(a.x / b.x, a.y / b.y, a.z / b.z); }
+VT_D v3 operator*(v3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+VT_D v3 operator*(float s, v3 a) { return mk3(s * a.x, s * a.y, s * a.z); }
+VT_D v3 operator/(v3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+VT_D v3 operator-(v3 a) { return mk3(-a.x, -a.y, -a.z); }
+VT_D float dot(v3 a, v3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+VT_D v3 cross(v3 a, v3 b) {
+  return mk3(a.y * b.z - b.y * a.z, a.z * b.x - b.z * a.x, a.x * b.y - b.x * a.y);
+}
+VT_D float length(v3 a) { return sqrtf(dot(a, a)); }
+VT_D v3 normalize(v3 a) { return a / length(a); }
+VT_D v3 vabs3(v3 a) { return mk3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+VT_D v3 ld3(const float* p) { return mk3(p[0], p[1], p[2]); }
+VT_D bool finite3(v3 a) {
+  const float inf = __int_as_float(0x7f800000);
+  return fabsf(a.x) < inf && fabsf(a.y) < inf && fabsf(a.z) < inf;
+}
+
+// GLSL mat4 * vec4 with the matrix stored row-major (uploaded transposed).
+VT_D float4 mul4(const float* m, float4 v) {
+  float4 r;
+  r.x = ((m[0] * v.x + m[1] * v.y) + m[2] * v.z) + m[3] * v.w;
+  r.y = ((m[4] * v.x + m[5] * v.y) + m[6] * v.z) + m[7] * v.w;
+  r.z = ((m[8] * v.x + m[9] * v.y) + m[10] * v.z) + m[11] * v.w;
+  r.w = ((m[12] * v.x + m[13] * v.y) + m[14] * v.z) + m[15] * v.w;
+  return r;
+}
+
+// ---------------------------------------------------------------- counters
+template <bool kCount>
+struct Cnt {
+  unsigned long long c[C_NUM];
+  VT_D void add(int i, unsigned long long v) { if (kCount) c[i] += v; }
+};
+
+// ---------------------------------------------------------------------- rng
+// Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011): 10 rounds of two 32x32->64 multiplies with a
+// Weyl-sequence key schedule.
+VT_D uint4 philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    const uint32_t lo0 = 0xD2511F53u * c0, hi0 = __umulhi(0xD2511F53u, c0);
+    const uint32_t lo1 = 0xCD9E8D57u * c2, hi1 = __umulhi(0xCD9E8D57u, c2);
+    const uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+  }
+  return make_uint4(c0, c1, c2, c3);
+}
+constexpr uint32_t kPhiloxKey1 = 0x6A09E667u;
+
+VT_D float u01(uint32_t x) { return (float)(x >> 8) * 5.9604644775390625e-8f; }
+
+// Wang hash on a signed int (random.h:3-11): arithmetic shifts, wrapping products.
+VT_D int32_t wang_hash(int32_t s) {
+  s = (s ^ 61) ^ (s >> 16);
+  s = (int32_t)((uint32_t)s * 9u);
+  s = s ^ (s >> 4);
+  s = (int32_t)((uint32_t)s * 0x27d4eb2du);
+  s = s ^ (s >> 15);
+  return s;
+}
+
+struct Rng {
+  uint32_t pixel;   // philox counter word 0
+  uint32_t sample;  // philox counter word 1
+  uint32_t call;    // philox counter word 2 (rand() calls so far)
+  int32_t ox, oy;   // noise-table walk position
+};
+
+// randomNumberGeneratorOffset (random.h:13-18).  The reference takes % of a
+// possibly negative int; the offset is read as unsigned here.
+VT_D void rng_init(const Frame& F, Rng& r, int px, int py, int sample) {
+  r.pixel = (uint32_t)(py * F.width + px);
+  r.sample = (uint32_t)sample;
+  r.call = 0;
+  const uint32_t off = (uint32_t)(wang_hash(px + py * kNoiseW) ^ wang_hash(sample));
+  r.ox = (int32_t)(off % (uint32_t)kNoiseW);
+  r.oy = (int32_t)((off / (uint32_t)kNoiseW) % (uint32_t)kNoiseH);
+}
+
+// rand (random.h:20-27) or one Philox block.
+VT_D float4 rng_next(const Frame& F, const JobDev& J, Rng& r) {
+  if (F.rng_mode == 1) {
+    const float4 v = __ldg(&J.noise[r.oy * kNoiseW + r.ox]);
+    r.ox = (r.ox + 1) % kNoiseW;
+    if (r.ox == 0) r.oy = (r.oy + 1) % kNoiseH;
+    return v;
+  }
+  const uint4 b = philox(r.pixel, r.sample, r.call, 0u, F.seed, kPhiloxKey1);
+  r.call += 1;
+  return make_float4(u01(b.x), u01(b.y), u01(b.z), u01(b.w));
+}
+
+// ----------------------------------------------------------------- palette
+struct Mat {
+  int type;
+  v3 emission;
+  v3 albedo;
+  float roughness;
+};
+VT_D float hf(unsigned short h) { return __half2float(__ushort_as_half(h)); }
+VT_D Mat load_mat(const JobDev& J, int entry) {
+  const uint4 q = __ldg(&J.palette[entry]);
+  Mat m;
+  m.type = (int)hf((unsigned short)(q.x & 0xffffu));
+  m.emission = mk3(hf((unsigned short)(q.x >> 16)), hf((unsigned short)(q.y & 0xffffu)),
+                   hf((unsigned short)(q.y >> 16)));
+  m.albedo = mk3(hf((unsigned short)(q.z & 0xffffu)), hf((unsigned short)(q.z >> 16)),
+                 hf((unsigned short)(q.w & 0xffffu)));
+  m.roughness = hf((unsigned short)(q.w >> 16));
+  return m;
+}
+VT_D Mat empty_mat() {
+  Mat m; m.type = -1; m.emission = mk3(0.f, 0.f, 0.f); m.albedo = mk3(0.f, 0.f, 0.f);
+  m.roughness = 0.f; return m;
+}
+// Material of voxel (x, y, z); the implicit ground below the volume uses the
+// configured ground entry (texelFetch outside the texture is undefined in GL).
+template <bool kCount>
+VT_D Mat voxel_mat(const Frame& F, const JobDev& J, int x, int y, int z, Cnt<kCount>& cnt) {
+  cnt.add(C_PALETTE, 1);
+  if (y < 0) return load_mat(J, F.ground_mat);
+  const uint8_t g = __ldg(&J.grid[(size_t)x + (size_t)F.res[0] * ((size_t)y + (size_t)F.res[1] * (size_t)z)]);
+  if (g == 0) return empty_mat();
+  return load_mat(J, (int)g - 1);
+}
+
+// -------------------------------------------------------------------- aabb
+// rayAABBIntersection (aabb.h:1-32).
+VT_D float ray_aabb(v3 o, v3 d, v3 bmin, v3 bmax) {
+  const v3 inv = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  const v3 t0 = (bmin - o) * inv;
+  const v3 t1 = (bmax - o) * inv;
+  const v3 tmin = mk3(vtb::gmin(t0.x, t1.x), vtb::gmin(t0.y, t1.y), vtb::gmin(t0.z, t1.z));
+  const float tminf = vtb::gmax(tmin.x, vtb::gmax(tmin.y, tmin.z));
+  const v3 tmax = mk3(vtb::gmax(t0.x, t1.x), vtb::gmax(t0.y, t1.y), vtb::gmax(t0.z, t1.z));
+  const float tmaxf = vtb::gmin(tmax.x, vtb::gmin(tmax.y, tmax.z));
+  if (tmaxf < 0.0f) return -1.0f;
+  if (tminf > tmaxf) return -1.0f;
+  return vtb::gmax(0.0f, tminf);
+}
+
+// ------------------------------------------------------------------ basis
+struct Basis { v3 position, tangent, normal, binormal; };
+
+// voxelSpaceToWorldSpace (coordinates.h:59-82).
+VT_D Basis voxel_basis(const Frame& F, int x, int y, int z, v3 ro, v3 rd) {
+  const v3 vs = ld3(F.vsize);
+  const v3 vmin = mk3((float)x, (float)y, (float)z) * vs + ld3(F.bmin);
+  const v3 vmax = vmin + vs;
+  const float t = ray_aabb(ro, rd, vmin, vmax);
+  Basis b;
+  b.position = ro + rd * t;
+  const v3 center = vmin + vs * 0.5f;
+  const v3 c2h = b.position - center;
+  const v3 a = vabs3(c2h);
+  const float mx = (vtb::gstep(a.y, a.x) && vtb::gstep(a.z, a.x)) ? 1.0f : 0.0f;
+  const float my = (vtb::gstep(a.x, a.y) && vtb::gstep(a.z, a.y)) ? 1.0f : 0.0f;
+  const float mz = (vtb::gstep(a.x, a.z) && vtb::gstep(a.y, a.z)) ? 1.0f : 0.0f;
+  b.normal = mk3(mx * vtb::gsign(c2h.x), my * vtb::gsign(c2h.y), mz * vtb::gsign(c2h.z));
+  const float d3 = 0.57735026919f;
+  const v3 tangent = cross(b.normal, mk3(d3, d3, d3));
+  b.binormal = normalize(cross(tangent, b.normal));
+  b.tangent = normalize(cross(b.binormal, b.normal));
+  return b;
+}
+// localToWorld / worldToLocal (coordinates.h:43-57).
+VT_D v3 local_to_world(v3 l, const Basis& b) {
+  return (b.tangent * l.x + b.normal * l.y) + b.binormal * l.z;
+}
+VT_D v3 world_to_local(v3 w, const Basis& b) {
+  return mk3(dot(w, b.tangent), dot(w, b.normal), dot(w, b.binormal));
+}
+
+// -------------------------------------------------------------------- dda
+struct Dda {
+  int32_t x, y, z;
+  float dx, dy, dz;    // distances to the next face crossing (dda.h:34)
+  float ax, ay, az;    // sign(d)/d = |1/d| (dda.h:31-32, 52)
+  int32_t sx, sy, sz;  // sign(d)
+  int32_t steps;
+  int32_t state;       // 0 running, 1 hit voxel, 2 left grid / step cap
+  int32_t cb;          // brick cached in `bits`
+  unsigned long long bits;
+};
+enum { DDA_RUNNING = 0, DDA_HIT = 1, DDA_MISS = 2 };
+
+// raymarch set-up (dda.h:15-34).  An origin outside the grid ends the
+// segment at once with the out-of-grid voxel as position (the reference
+// leaves the out parameter unwritten there).
+VT_D void dda_begin(const Frame& F, Dda& s, v3 o, v3 d) {
+  const v3 bmin = ld3(F.bmin);
+  o = o + mk3(vtb::gsign(d.x), vtb::gsign(d.y), vtb::gsign(d.z)) * 0.001f;
+  const v3 vo = ((o - bmin) * ld3(F.vext)) * mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
+  const v3 vp = mk3(floorf(vo.x), floorf(vo.y), floorf(vo.z));
+  s.x = (int32_t)vp.x; s.y = (int32_t)vp.y; s.z = (int32_t)vp.z;
+  s.steps = 0;
+  s.cb = -1;
+  s.bits = 0ull;
+  if (vp.x < 0.0f || vp.y < 0.0f || vp.z < 0.0f || vp.x >= (float)F.res[0] ||
+      vp.y >= (float)F.res[1] || vp.z >= (float)F.res[2]) {
+    s.state = DDA_MISS;
+    return;
+  }
+  s.state = DDA_RUNNING;
+  d.x = vtb::gstep(fabsf(d.x), 1e-5f) ? 1e-5f : d.x;
+  d.y = vtb::gstep(fabsf(d.y), 1e-5f) ? 1e-5f : d.y;
+  d.z = vtb::gstep(fabsf(d.z), 1e-5f) ? 1e-5f : d.z;
+  const v3 inc = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  const v3 sg = mk3(vtb::gsign(d.x), vtb::gsign(d.y), vtb::gsign(d.z));
+  const v3 dis = (((vp - vo) + mk3(0.5f, 0.5f, 0.5f)) + sg * 0.5f) * inc;
+  s.dx = dis.x; s.dy = dis.y; s.dz = dis.z;
+  s.ax = sg.x * inc.x; s.ay = sg.y * inc.y; s.az = sg.z * inc.z;
+  s.sx = (int32_t)sg.x; s.sy = (int32_t)sg.y; s.sz = (int32_t)sg.z;
+}
+
+// DDA loop (dda.h:38-57): at most `budget` iterations of
+// bounds test -> occupancy test -> advance every minimal axis.
+template <bool kCount>
+VT_D void dda_advance(const Frame& F, const JobDev& J, Dda& s, int budget, Cnt<kCount>& cnt) {
+  const int rx = F.res[0], ry = F.res[1], rz = F.res[2];
+  const int bx = F.bdim[0], bxy = F.bdim[0] * F.bdim[1];
+  int x = s.x, y = s.y, z = s.z, steps = s.steps, cb = s.cb;
+  float dx = s.dx, dy = s.dy, dz = s.dz;
+  unsigned long long bits = s.bits;
+  int state = DDA_RUNNING;
+  const int max_steps = F.max_steps;
+  while (budget-- > 0) {
+    if (steps >= max_steps) { state = DDA_MISS; break; }
+    if ((unsigned)x >= (unsigned)rx || (unsigned)y >= (unsigned)ry || (unsigned)z >= (unsigned)rz) {
+      state = DDA_MISS; break;
+    }
+    cnt.add(C_DDA_CELLS, 1);
+    const int b = (x >> 2) + bx * (y >> 2) + bxy * (z >> 2);
+    if (b != cb) { bits = __ldg(&J.bricks[b]); cb = b; }
+    if ((bits >> ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4))) & 1ull) { state = DDA_HIT; break; }
+    const bool mx = (dy >= dx) && (dz >= dx);
+    const bool my = (dx >= dy) && (dz >= dy);
+    const bool mz = (dy >= dz) && (dx >= dz);
+    if (mx) { dx = dx + s.ax; x += s.sx; }
+    if (my) { dy = dy + s.ay; y += s.sy; }
+    if (mz) { dz = dz + s.az; z += s.sz; }
+    ++steps;
+  }
+  s.x = x; s.y = y; s.z = z; s.steps = steps; s.cb = cb; s.bits = bits;
+  s.dx = dx; s.dy = dy; s.dz = dz;
+  s.state = state;
+}
+
+// traverse (dda.h:63-79): voxel hit, or with the ground quirk an exit below y = 0.
+VT_D bool dda_hit(const Frame& F, const Dda& s) {
+  if (s.state == DDA_HIT) return true;
+  return (F.quirks & Q_GROUND) && s.y < 0;
+}
+
+// --------------------------------------------------------------- sampling
+// sampling.h:2-43
+VT_D float2 sample_disk(float u0, float u1) {
+  const float r = sqrtf(u0);
+  const float theta = (2.0f * kPI) * u1;
+  return make_float2(r * vtb::vcos(theta), r * vtb::vsin(theta));
+}
+VT_D float4 cosine_hemisphere(float u0, float u1) {
+  const float2 p = sample_disk(u0, u1);
+  const float y = sqrtf(vtb::gmax(0.0f, (1.0f - p.x * p.x) - p.y * p.y));
+  return make_float4(p.x, y, p.y, y / kPI);
+}
+VT_D float4 uniform_hemisphere(float u0, float u1) {
+  const float y = u0;
+  const float r = sqrtf(vtb::gmax(0.0f, 1.0f - y * y));
+  const float phi = (u1 * 2.0f) * kPI;
+  return make_float4(r * vtb::vcos(phi), y, r * vtb::vsin(phi), 1.0f / (2.0f * kPI));
+}
+VT_D float power_heuristic(float f, float g) { return (f * f) / ((f * f) + (g * g)); }
+VT_D float luminance(v3 c) { return (c.x * 0.2126f + c.y * 0.7152f) + c.z * 0.0722f; }
+
+// ------------------------------------------------------------------- bsdfs
+struct FPdf { v3 f; float pdf; };
+
+// microfacet.h:5-15
+VT_D float g_term(v3 wo, v3 wi, v3 wh) {
+  const float nh = wh.y, no = wo.y, ni = wi.y;
+  const float woh = fabsf(dot(wo, wh));
+  return vtb::gmin(1.0f, vtb::gmin(((2.0f * nh) * no) / woh, ((2.0f * nh) * ni) / woh));
+}
+// Fresnel: Schlick with IOR 7.3 (microfacet.h:64-69) or with F0 = reflectance.
+VT_D v3 fresnel(const Frame& F, v3 f0, float cos_h) {
+  const float p = vtb::vpow(1.0f - cos_h, 5.0f);
+  if (F.quirks & Q_FIXED_IOR) {
+    const float ior = 7.3f;
+    const float sr0 = (1.0f - ior) / (1.0f + ior);
+    const float r0 = sr0 * sr0;
+    const float fr = r0 + (1.0f - r0) * p;
+    return mk3(fr, fr, fr);
+  }
+  return mk3(f0.x + (1.0f - f0.x) * p, f0.y + (1.0f - f0.y) * p, f0.z + (1.0f - f0.z) * p);
+}
+// Blinn distribution D and its pdf (microfacet.h:19-37); `color` multiplies f.
+VT_D FPdf d_term(v3 color, float e, v3 wo, v3 wh) {
+  const float pc = vtb::vpow(wh.y, e);
+  const float f = ((e + 2.0f) * kINV_TWOPI) * pc;
+  const float wodh = dot(wo, wh);
+  FPdf r;
+  r.pdf = (wodh <= 0.0f) ? 0.0f : ((e + 1.0f) * pc) / ((kTWO_PI * 4.0f) * wodh);
+  r.f = color * f;
+  return r;
+}
+VT_D float blinn_exponent(const Frame& F, float roughness) {
+  if (F.quirks & Q_EXPONENT_IS_ROUGHNESS) return roughness;          // metal.h:13-14
+  const float r2 = vtb::gmax(roughness * roughness, 1e-6f);
+  return vtb::gmax(2.0f / r2 - 2.0f, 0.0f);
+}
+// evaluateMaterialBSDF (materials.h:7-19 + matte/metal/plastic).
+VT_D FPdf eval_bsdf(const Frame& F, const Mat& m, v3 wo, v3 wi) {
+  FPdf r;
+  if (m.type == 0) {                                                 // lambertian.h:23-29
+    r.pdf = wi.y / kPI;
+    r.f = m.albedo / kPI;
+    return r;
+  }
+  if (m.type == 1 || m.type == 2) {                                  // microfacet.h:73-91
+    const v3 refl = (m.type == 1) ? m.albedo : mk3(1.0f, 1.0f, 1.0f);
+    const float e = blinn_exponent(F, m.roughness);
+    const float cwi = wi.y, cwo = wo.y;
+    const v3 wh = normalize(wi + wo);
+    const float ch = dot(wi, wh);
+    const bool fixed = (F.quirks & Q_FIXED_IOR) != 0;
+    r = d_term(fixed ? refl : mk3(1.0f, 1.0f, 1.0f), e, wo, wh);
+    const float g = g_term(wo, wi, wh);
+    const v3 fr = fresnel(F, refl, ch);
+    const float den = (4.0f * cwo) * cwi;
+    r.f = mk3(r.f.x * ((g * fr.x) / den), r.f.y * ((g * fr.y) / den), r.f.z * ((g * fr.z) / den));
+    return r;
+  }
+  r.f = mk3(0.f, 0.f, 0.f); r.pdf = 0.0f;
+  return r;
+}
+// sampleMaterialBSDF (materials.h:30-43): consumes one rand() block; returns
+// the local direction, f and pdf, and the block's z for Russian roulette.
+template <bool kCount>
+VT_D v3 sample_bsdf(const Frame& F, const JobDev& J, const Mat& m, v3 wo, Rng& rng, FPdf& out, float& u_rr) {
+  const float4 u = rng_next(F, J, rng);
+  u_rr = u.z;
+  if (m.type == 0) {                                                 // lambertian.h:10-19
+    const float4 s = cosine_hemisphere(u.x, u.y);
+    out.f = m.albedo / kPI;
+    out.pdf = s.w;
+    return mk3(s.x, s.y, s.z);
+  }
+  // microfacet.h:41-61 and 102-123
+  const v3 refl = (m.type == 1) ? m.albedo : mk3(1.0f, 1.0f, 1.0f);
+  const float e = blinn_exponent(F, m.roughness);
+  const float ct = vtb::vpow(u.x, 1.0f / (e + 1.0f));
+  const float st = sqrtf(vtb::gmax(0.0f, 1.0f - ct * ct));
+  const float phi = (u.y * 2.0f) * kPI;
+  const v3 wh = mk3(st * vtb::vcos(phi), ct, st * vtb::vsin(phi));
+  const v3 wi = (-wo) + (2.0f * dot(wo, wh)) * wh;
+  const bool fixed = (F.quirks & Q_FIXED_IOR) != 0;
+  FPdf d = d_term(fixed ? refl : mk3(1.0f, 1.0f, 1.0f), e, wo, wh);
+  const float cwi = wi.y, cwo = wo.y;
+  const v3 wh2 = normalize(wi + wo);
+  const float ch = dot(wi, wh2);
+  const float g = g_term(wo, wi, wh2);
+  const v3 fr = fresnel(F, refl, ch);
+  const float den = (4.0f * cwo) * cwi;
+  v3 f = d.f;
+  if (F.quirks & Q_DOUBLE_REFLECTANCE) f = refl * f;
+  out.f = mk3(((f.x * g) * fr.x) / den, ((f.y * g) * fr.y) / den, ((f.z * g) * fr.z) / den);
+  out.pdf = d.pdf;
+  return wi;
+}
+
+// --------------------------------------------------------------- env light
+// uvCoordFromVector / directionFromUVCoord (coordinates.h:97-116).
+VT_D float2 uv_from_dir(v3 v, float rot) {
+  const float theta = vtb::vacos(v.y);
+  const float phi = (vtb::vatan2(v.z, v.x) + kPI) + rot;
+  const float x = phi / kTWO_PI;
+  const float u = x - 1.0f * floorf(x / 1.0f);
+  return make_float2(u, theta / kPI);
+}
+VT_D v3 dir_from_uv(float u, float v, float rot) {
+  const float phi = ((u * kTWO_PI) - kPI) - rot;
+  const float theta = v * kPI;
+  const float st = vtb::vsin(theta);
+  return mk3(st * vtb::vcos(phi), vtb::vcos(theta), st * vtb::vsin(phi));
+}
+VT_D v3 texel(const JobDev& J, int w, int i, int j) {
+  const uint2 q = __ldg(&J.env_texels[(size_t)j * w + i]);
+  return mk3(hf((unsigned short)(q.x & 0xffffu)), hf((unsigned short)(q.x >> 16)),
+             hf((unsigned short)(q.y & 0xffffu)));
+}
+// texture(backgroundTexture, uv) with GL_LINEAR filtering and clamp to edge.
+template <bool kCount>
+VT_D v3 env_lookup(const Frame& F, const JobDev& J, float u, float v, Cnt<kCount>& cnt) {
+  cnt.add(C_ENV_EVALS, 1);
+  const int w = F.env_w, h = F.env_h;
+  const float x = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+  const float x0 = floorf(x), y0 = floorf(y);
+  const float fx = x - x0, fy = y - y0;
+  int i0 = (int)x0, j0 = (int)y0;
+  int i1 = i0 + 1, j1 = j0 + 1;
+  i0 = min(max(i0, 0), w - 1); i1 = min(max(i1, 0), w - 1);
+  j0 = min(max(j0, 0), h - 1); j1 = min(max(j1, 0), h - 1);
+  const v3 t00 = texel(J, w, i0, j0), t10 = texel(J, w, i1, j0);
+  const v3 t01 = texel(J, w, i0, j1), t11 = texel(J, w, i1, j1);
+  const float gx = 1.0f - fx, gy = 1.0f - fy;
+  const v3 a = t00 * gx + t10 * fx;
+  const v3 b = t01 * gx + t11 * fx;
+  return a * gy + b * fy;
+}
+// getBackgroundColor (lights.h:4-17).
+template <bool kCount>
+VT_D v3 background(const Frame& F, const JobDev& J, v3 d, Cnt<kCount>& cnt) {
+  if (F.use_image) {
+    const float2 uv = uv_from_dir(d, F.bg_rot);
+    return env_lookup(F, J, uv.x, uv.y, cnt);
+  }
+  const float bias = vtb::gmax(0.0f, d.y);
+  return ld3(F.bg_bottom) * (1.0f - bias) + ld3(F.bg_top) * bias;
+}
+// evaluateEnvironmentRadiance (lights.h:20-33).
+template <bool kCount>
+VT_D v3 eval_env(const Frame& F, const JobDev& J, v3 d, float& pdf, Cnt<kCount>& cnt) {
+  const v3 L = background(F, J, d, cnt);
+  if (F.use_image) pdf = luminance(L) / F.env_integral;
+  else pdf = (F.quirks & Q_GRADIENT_PDF_MISMATCH) ? 1.0f / (4.0f * kPI) : 1.0f / (2.0f * kPI);
+  return L;
+}
+// binarySearchCDFV / binarySearchCDFU (envMapSample.h:70-123).
+template <bool kCount>
+VT_D int search_cdf(const float* cdf, int high, float u, Cnt<kCount>& cnt) {
+  int low = 0;
+  while (low != high - 1) {
+    const int mid = (low + high) / 2;
+    cnt.add(C_CDF_PROBES, 1);
+    if (u < __ldg(&cdf[mid])) high = mid; else low = mid;
+  }
+  return low;
+}
+// sampleEnvironmentRadiance (lights.h:36-55, envMapSample.h:23-65).
+template <bool kCount>
+VT_D v3 sample_env(const Frame& F, const JobDev& J, const Basis& b, float u0, float u1,
+                   v3& dir, float& pdf, Cnt<kCount>& cnt) {
+  if (F.use_image) {
+    const int su = F.env_w + 1, sv = F.env_h + 1;
+    const int row = search_cdf(J.cdf_v, sv - 1, u1, cnt);
+    const float* cu = J.cdf_u + (size_t)row * su;
+    const int col = search_cdf(cu, su - 1, u0, cnt);
+    cnt.add(C_CDF_PROBES, 4);
+    const float lu = __ldg(&cu[col]), hu = __ldg(&cu[col + 1]);
+    const float du = (u0 - lu) / (hu - lu);
+    const float lv = __ldg(&J.cdf_v[row]), hv = __ldg(&J.cdf_v[row + 1]);
+    const float dv = (u1 - lv) / (hv - lv);
+    const float u = ((float)col + du) / (float)(su - 1);
+    const float v = ((float)row + dv) / (float)(sv - 1);
+    dir = dir_from_uv(u, v, F.bg_rot);
+    const v3 L = env_lookup(F, J, u, v, cnt);
+    pdf = luminance(L) / F.env_integral;
+    return L;
+  }
+  const float4 s = uniform_hemisphere(u0, u1);
+  dir = local_to_world(mk3(s.x, s.y, s.z), b);
+  pdf = s.w;
+  return background(F, J, dir, cnt);
+}
+
+// ------------------------------------------------------------------ camera
+// screenToEyeSpacePerspective / Orthographic (coordinates.h:1-27) with
+// gl_DepthRange = [0, 1].
+VT_D float4 screen_to_eye_persp(const Frame& F, v3 w) {
+  v3 ndc;
+  ndc.x = ((2.0f * w.x) - (2.0f * F.viewport[0])) / F.viewport[2] - 1.0f;
+  ndc.y = ((2.0f * w.y) - (2.0f * F.viewport[1])) / F.viewport[3] - 1.0f;
+  ndc.z = ((2.0f * w.z - 0.0f) - 1.0f) / (1.0f - 0.0f);
+  const float cw = F.proj[11] / (ndc.z - (F.proj[10] / F.proj[14]));
+  return mul4(F.inv_proj, make_float4(ndc.x * cw, ndc.y * cw, ndc.z * cw, cw));
+}
+VT_D float4 screen_to_eye_ortho(const Frame& F, v3 w) {
+  v3 ndc;
+  ndc.x = (w.x / F.viewport[2]) * 2.0f - 1.0f;
+  ndc.y = (w.y / F.viewport[3]) * 2.0f - 1.0f;
+  ndc.z = ((2.0f * w.z - 0.0f) - 1.0f) / (1.0f - 0.0f);
+  return mul4(F.inv_proj, make_float4(ndc.x, ndc.y, ndc.z, 1.0f));
+}
+VT_D v3 xyz(float4 v) { return mk3(v.x, v.y, v.z); }
+
+// generateRay (generateRay.h:1-123).  frag = gl_FragCoord.xyz.
+VT_D void generate_ray(const Frame& F, const JobDev& J, v3 frag, Rng& rng, v3& o, v3& d) {
+  const float* M = F.inv_mv;
+  if (F.lens_model == 0) {                                         // pinhole :10-26
+    const float4 u = rng_next(F, J, rng);
+    const v3 jit = mk3(u.x - 0.5f, u.y - 0.5f, 0.0f);
+    const float4 es = screen_to_eye_persp(F, frag + jit);
+    o = xyz(mul4(M, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));
+    const v3 n = normalize(mk3(es.x, es.y, es.z));
+    const float4 w = mul4(M, make_float4(n.x, n.y, n.z, 0.0f));
+    const float l = sqrtf(((w.x * w.x + w.y * w.y) + w.z * w.z) + w.w * w.w);
+    d = mk3(w.x / l, w.y / l, w.z / l);
+  } else if (F.lens_model == 1) {                                  // thin lens :30-101
+    const float4 u = rng_next(F, J, rng);
+    const float2 disk = sample_disk(u.x, u.y);
+    const v3 lens = mk3(disk.x * F.lens_radius, disk.y * F.lens_radius, 0.0f);
+    v3 fp = frag;
+    if (!(F.quirks & Q_THINLENS_NO_JITTER)) fp = frag + mk3(u.z - 0.5f, u.w - 0.5f, 0.0f);
+    const v3 eo = xyz(screen_to_eye_persp(F, fp));
+    const v3 ed = normalize(eo);
+    const float t = F.focal_distance / -(ed.z);
+    const v3 ef = eo + ed * t;
+    const v3 wf = xyz(mul4(M, make_float4(ef.x, ef.y, ef.z, 1.0f)));
+    o = xyz(mul4(M, make_float4(lens.x, lens.y, lens.z, 1.0f)));
+    d = normalize(wf - o);
+  } else {                                                         // orthographic :1-7
+    o = xyz(mul4(M, screen_to_eye_ortho(F, frag)));
+    d = xyz(mul4(M, make_float4(0.0f, 0.0f, -1.0f, 0.0f)));
+  }
+}
+
+// ------------------------------------------------------------ path state
+enum { PH_EXT = 0, PH_SHADOW = 1, PH_DONE = 2 };
+
+struct Path {
+  Rng rng;
+  v3 L;          // radiance
+  v3 T;          // throughput
+  v3 ro, rd;     // current ray: origin used for the exact hit, direction
+  v3 cont_d;     // continuation direction, traced after the shadow ray
+  v3 nee_T;      // throughput at the vertex of the pending light sample
+  v3 nee_C;      // directLighting value if the light is visible
+  int32_t light; // emissive voxel index of the light sample, -1 = environment
+  float bsdf_pdf;
+  int32_t bounces;
+  int32_t phase;
+  int32_t primary;
+  int32_t has_cont;
+};
+
+// Per-sample output: pow(L*exposure, 1/gamma) when the gamma quirk is on
+// (pathTracer.fs:294-295), linear radiance otherwise; alpha = 1.
+VT_D float4 path_output(const Frame& F, const Path& p) {
+  if (F.quirks & Q_GAMMA_BEFORE_AVERAGE) {
+    return make_float4(vtb::vpow(p.L.x * F.exposure, F.inv_gamma), vtb::vpow(p.L.y * F.exposure, F.inv_gamma),
+                       vtb::vpow(p.L.z * F.exposure, F.inv_gamma), 1.0f);
+  }
+  return make_float4(p.L.x, p.L.y, p.L.z, 1.0f);
+}
+
+
+// main() up to the primary traversal (pathTracer.fs:172-208).  Leaves the
+// path in PH_EXT with the primary DDA set up, or PH_DONE on a miss.
+template <bool kCount>
+VT_D void path_start(const Frame& F, const JobDev& J, Path& p, Dda& s, int px, int py, int sample,
+                     Cnt<kCount>& cnt) {
+  rng_init(F, p.rng, px, py, sample);
+  cnt.add(C_PATHS, 1);
+  p.L = mk3(0.0f, 0.0f, 0.0f);
+  p.T = mk3(1.0f, 1.0f, 1.0f);
+  p.bounces = 0;
+  p.primary = 1;
+  p.has_cont = 0;
+  p.light = -1;
+  p.bsdf_pdf = 0.0f;
+  v3 o, d;
+  generate_ray(F, J, mk3((float)px + 0.5f, (float)py + 0.5f, F.frag_z), p.rng, o, d);
+  p.ro = o;
+  p.rd = d;
+  const float t = ray_aabb(o, d, ld3(F.bmin), ld3(F.bmax));
+  if (t < 0.0f) {
+    p.L = background(F, J, d, cnt);
+    p.phase = PH_DONE;
+    return;
+  }
+  cnt.add(C_SEGMENTS, 1);
+  dda_begin(F, s, o + t * d, d);
+  p.phase = PH_EXT;
+}
+
+// directLighting (pathTracer.fs:64-170) up to the shadow ray: picks a light,
+// evaluates the BSDF and MIS weight for it and leaves the shadow segment set
+// up.  The BSDF evaluation does not depend on visibility, so it is done
+// before the shadow ray; the contribution is added only if the segment
+// confirms visibility (see path_event).
+template <bool kCount>
+VT_D void light_sample(const Frame& F, const JobDev& J, Path& p, const Basis& b, const Mat& m, v3 wo,
+                       Dda& s, Cnt<kCount>& cnt) {
+  const float4 u = rng_next(F, J, p.rng);
+  const int num_lights = F.n_emissive + 1;
+  const int li = (int)(u.x * (float)num_lights);
+  v3 dir, Ll;
+  float pdf;
+  if (li < num_lights - 1) {
+    cnt.add(C_EMISSIVE_READS, 1);
+    const int idx = __ldg(&J.emissive[li]);
+    const int dz = F.res[0] * F.res[1], dy = F.res[0];
+    const int ez = idx / dz;
+    const int r1 = idx - ez * dz;
+    const int ey = r1 / dy;
+    const int ex = r1 - ey * dy;
+    const Mat lm = voxel_mat(F, J, ex, ey, ez, cnt);
+    Ll = mk3(F.nee_scale, F.nee_scale, F.nee_scale) * lm.emission;
+    const v3 res = mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
+    v3 wp = (mk3((float)ex, (float)ey, (float)ez) / res) * (ld3(F.bmax) - ld3(F.bmin)) + ld3(F.bmin);
+    wp = wp + mk3(u.y, u.z, u.w) * ld3(F.vsize);
+    const v3 to_light = wp - b.position;
+    const float r = length(to_light);
+    dir = to_light / r;
+    const Basis lb = voxel_basis(F, ex, ey, ez, b.position, dir);
+    const float area = (6.0f * F.vsize[0]) * F.vsize[1];
+    const float jac = (r * r) / fabsf(dot(-dir, lb.normal));
+    pdf = jac / area;
+    p.light = idx;
+  } else {
+    Ll = sample_env(F, J, b, u.y, u.z, dir, pdf, cnt);
+    p.light = -1;
+  }
+  pdf = pdf / (float)num_lights;
+  const v3 lwo = world_to_local(wo, b);
+  const v3 lwi = world_to_local(dir, b);
+  const FPdf bf = eval_bsdf(F, m, lwo, lwi);
+  const float mis = power_heuristic(pdf, bf.pdf);
+  p.nee_C = (((bf.f * Ll) * fabsf(dot(dir, b.normal))) * mis) / pdf;
+  // Without the unguarded-samples quirk a light sample with a zero, negative
+  // or infinite pdf contributes nothing instead of dividing by it.
+  if (!(F.quirks & Q_UNGUARDED) && !(pdf > 0.0f && pdf < __int_as_float(0x7f800000)))
+    p.nee_C = mk3(0.0f, 0.0f, 0.0f);
+  p.nee_T = p.T;
+  cnt.add(C_SEGMENTS, 1);
+  dda_begin(F, s, b.position, dir);
+}
+
+// Segment-end event: the body of the bounce loop (pathTracer.fs:214-292) cut
+// at its two traversals.  After an extension segment: miss -> environment
+// (with MIS unless primary), hit -> shade the vertex and start the shadow
+// segment.  After a shadow segment: add the light sample if visible, then
+// start the continuation segment.
+template <bool kCount>
+VT_D void path_event(const Frame& F, const JobDev& J, Path& p, Dda& s, Cnt<kCount>& cnt) {
+  const bool hit = dda_hit(F, s);
+  if (p.phase == PH_SHADOW) {
+    bool visible;
+    if (p.light >= 0) {
+      const int dz = F.res[0] * F.res[1], dy = F.res[0];
+      const int ez = p.light / dz;
+      const int r1 = p.light - ez * dz;
+      const int ey = r1 / dy;
+      const int ex = r1 - ey * dy;
+      visible = hit && s.x == ex && s.y == ey && s.z == ez;
+    } else {
+      visible = !hit;
+    }
+    const v3 c = visible ? p.nee_C : mk3(0.0f, 0.0f, 0.0f);
+    p.L = p.L + p.nee_T * c;
+    if (!p.has_cont) { p.phase = PH_DONE; return; }
+    p.rd = p.cont_d;
+    p.primary = 0;
+    p.phase = PH_EXT;
+    cnt.add(C_SEGMENTS, 1);
+    dda_begin(F, s, p.ro, p.rd);
+    return;
+  }
+  // extension segment ended
+  if (!hit) {
+    if (p.primary) {
+      p.L = background(F, J, p.rd, cnt);                          // :202-208
+    } else {
+      float lpdf;
+      const v3 Le = eval_env(F, J, p.rd, lpdf, cnt);              // :282-289
+      const float mis = power_heuristic(p.bsdf_pdf, lpdf);
+      p.L = p.L + (p.T * Le) * mis;
+    }
+    p.phase = PH_DONE;
+    return;
+  }
+  if (!p.primary) p.bounces += 1;                                 // :291
+  if (p.bounces >= F.max_bounces) { p.phase = PH_DONE; return; }  // :214
+  const Basis b = voxel_basis(F, s.x, s.y, s.z, p.ro, p.rd);      // :220-223
+  const Mat m = voxel_mat(F, J, s.x, s.y, s.z, cnt);              // :225-226
+  if (F.sel_enabled && s.x == F.sel[0] && s.y == F.sel[1] && s.z == F.sel[2]) {
+    p.L = p.L + mk3(1.0f, 0.0f, 0.0f);                            // :228-233
+    p.phase = PH_DONE;
+    return;
+  }
+  const v3 wo = -p.rd;
+  const v3 lwo = world_to_local(wo, b);
+  if (p.bounces == 0) p.L = p.L + p.T * m.emission;               // :241-245
+  const int hx = s.x, hy = s.y, hz = s.z;
+  light_sample(F, J, p, b, m, wo, s, cnt);                        // :248-251
+  FPdf bs;
+  float u_rr;
+  v3 lwi = sample_bsdf<kCount>(F, J, m, lwo, p.rng, bs, u_rr);    // :254-258
+  if (F.wire_opacity > 0.0f) {                                    // :260-270
+    const v3 res = mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
+    const v3 vc = ((b.position - ld3(F.bmin)) / (ld3(F.bmax) - ld3(F.bmin))) * res;
+    const v3 uvw = mk3((float)hx, (float)hy, (float)hz) - vc;
+    const v3 nyzx = mk3(b.normal.y, b.normal.z, b.normal.x);
+    const v3 nzxy = mk3(b.normal.z, b.normal.x, b.normal.y);
+    const float ux = fabsf(dot(nyzx, uvw)), uy = fabsf(dot(nzxy, uvw));
+    const float th = F.wire_thickness;
+    float wire = (vtb::gstep(th, ux) ? 1.0f : 0.0f) * (vtb::gstep(ux, 1.0f - th) ? 1.0f : 0.0f);
+    wire = wire * (vtb::gstep(th, uy) ? 1.0f : 0.0f);
+    wire = wire * (vtb::gstep(uy, 1.0f - th) ? 1.0f : 0.0f);
+    wire = (1.0f - F.wire_opacity) + F.wire_opacity * wire;
+    bs.f = bs.f * mk3(wire, wire, wire);
+  }
+  const v3 wwi = local_to_world(lwi, b);                          // :273
+  const bool guard = !(F.quirks & Q_UNGUARDED);
+  p.has_cont = 1;
+  // Without the unguarded-samples quirk a BSDF sample with zero pdf or below
+  // the surface ends the path (the reference divides by the pdf regardless).
+  if (guard && (!(bs.pdf > 0.0f) || !(lwi.y > 0.0f))) p.has_cont = 0;
+  if (p.has_cont) {
+    p.T = p.T * ((bs.f * fabsf(dot(wwi, b.normal))) / bs.pdf);    // :276
+    if (guard && !(finite3(p.T))) p.has_cont = 0;
+  }
+  if (p.has_cont && F.rr_start >= 0 && p.bounces >= F.rr_start) {  // Russian roulette
+    const float q = vtb::gmin(1.0f, vtb::gmax(p.T.x, vtb::gmax(p.T.y, p.T.z)));
+    if (!(u_rr < q)) p.has_cont = 0;
+    else p.T = p.T / q;
+  }
+  p.ro = b.position;                                              // :278-279
+  p.cont_d = wwi;
+  p.bsdf_pdf = bs.pdf;
+  p.phase = PH_SHADOW;
+}
+
+// One complete sample, run to the end by a single lane.
+template <bool kCount>
+VT_D float4 trace_sample(const Frame& F, const JobDev& J, int px, int py, int sample, Cnt<kCount>& cnt,
+                         HitRecord* first_hit) {
+  Path p;
+  Dda s;
+  path_start(F, J, p, s, px, py, sample, cnt);
+  bool first = true;
+  if (first_hit) { first_hit->x = -1; first_hit->y = -1; first_hit->z = -1; first_hit->flags = 0; }
+  while (p.phase != PH_DONE) {
+    if (s.state == DDA_RUNNING) dda_advance(F, J, s, 0x7fffffff, cnt);
+    if (first && first_hit) {
+      first = false;
+      const bool h = dda_hit(F, s);
+      first_hit->x = s.x; first_hit->y = s.y; first_hit->z = s.z;
+      int flags = (h ? 1 : 0) << 8 | ((h && s.state != DDA_HIT) ? 1 : 0) << 9;
+      if (h) {
+        const Basis b = voxel_basis(F, s.x, s.y, s.z, p.ro, p.rd);
+        flags |= ((int)b.normal.x + 1) | (((int)b.normal.y + 1) << 2) | (((int)b.normal.z + 1) << 4);
+      }
+      first_hit->flags = flags;
+    }
+    path_event(F, J, p, s, cnt);
+  }
+  return path_output(F, p);
+}
+
+// Kahan-compensated accumulation of one sample into a pixel.
+VT_D void kahan_add(float4& sum, float4& comp, float4 v) {
+  float y, t;
+  y = v.x - comp.x; t = sum.x + y; comp.x = (t - sum.x) - y; sum.x = t;
+  y = v.y - comp.y; t = sum.y + y; comp.y = (t - sum.y) - y; sum.y = t;
+  y = v.z - comp.z; t = sum.z + y; comp.z = (t - sum.z) - y; sum.z = t;
+  y = v.w - comp.w; t = sum.w + y; comp.w = (t - sum.w) - y; sum.w = t;
+}
+
+}  // namespace vt
