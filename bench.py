@@ -139,20 +139,25 @@ def cpu_sample_rate(cfg, seconds: float, threads: int = 0) -> dict:
     from oracle import binding as orc
     osc = orc.Scene(cfg.voxels, cfg.palette, cfg._emissive)
     oenv = orc.Env(cfg.env_rgb) if cfg.env_rgb is not None else orc.Env()
-    rows = 8
+    rows = 16
+    r0 = (cfg.height - rows) // 2
     t0 = time.perf_counter()
-    orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 1, 32, threads, rows=(0, rows))
+    orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 1, 32, threads, rows=(r0, r0 + rows))
     dt = time.perf_counter() - t0
     rate = rows * cfg.width / max(dt, 1e-9)
-    band = int(min(cfg.height, max(rows, rate * seconds / cfg.width)))
+    # full frame rows, then as many samples per pixel as fit the time budget
+    want = rate * seconds
+    band = int(min(cfg.height, max(rows, want / cfg.width)))
+    spp = int(max(1, min(cfg.spp, want / (band * cfg.width))))
     r0 = (cfg.height - band) // 2
     t0 = time.perf_counter()
-    orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 1, 32, threads, rows=(r0, r0 + band))
+    orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, spp, 32, threads,
+                       rows=(r0, r0 + band))
     dt = time.perf_counter() - t0
-    paths = band * cfg.width
+    paths = band * cfg.width * spp
     return {"value": paths / dt / 1e6, "seconds": dt, "paths": paths,
-            "sample": f"{band} centre rows x {cfg.width} px x 1 spp of the {cfg.width}x{cfg.height} frame "
-                      f"({paths} paths, FP32 oracle)"}
+            "sample": f"{band} centre rows x {cfg.width} px x {spp} spp of the {cfg.width}x{cfg.height} frame "
+                      f"({paths} paths, {dt:.1f} s, FP32 oracle, {threads or os.cpu_count()} threads)"}
 
 
 def emissive_for_oracle(cfg):
@@ -217,6 +222,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 persistent")
+    ap.add_argument("--profile", action="store_true",
+                    help="only warm-up and timed renders of the resident frame (for ncu captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
     world, rank, local = dist_setup()
@@ -239,6 +246,16 @@ def main():
     env = Env(ctx, cfg.env_rgb)
     job = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
     paths = cfg.width * cfg.height * cfg.spp
+    if args.profile:
+        for k in range(args.warmup + args.steps):
+            job.reset()
+            t0 = time.perf_counter()
+            job.render(cfg.spp)
+            job.synchronize()
+            if k >= args.warmup:
+                print(json.dumps({"profile_step_ms": 1e3 * (time.perf_counter() - t0), "paths": paths}), flush=True)
+        job.close(); env.close(); scene.close(); ctx.close()
+        return 0
 
     # event counts of one full frame: the algorithmic bytes of a launch
     cnt = job.render_counted(cfg.spp).astype(np.float64)
@@ -263,9 +280,11 @@ def main():
     barrier(world)
     torch.cuda.synchronize()
     times = []
+    launches0 = ctx.launch_count()
     with ClockSampler(local) as clk:
         for _ in range(args.steps):
             times.append(one_step())
+    launches = ctx.launch_count() - launches0
     torch.cuda.synchronize()
     barrier(world)
     ms = all_max(world, float(np.mean(times)))
@@ -316,10 +335,10 @@ def main():
         "config": config_dict(args, cfg),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "ms_per_step": e2e_s * 1e3},
-        "gpu_launches": args.steps * (1 if args.kernel == 2 else cfg.spp),
+        "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-                     "peak_source": pk["source"], "kernel": "k_persistent",
+                     "peak_source": pk["source"], "kernel": "k_wf_trace + k_wf_shade (one frame)",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "bytes_model": "1 B/DDA cell + 16 B/palette record + 8 B/env texel eval + 4 B/CDF probe + "
                                     "4 B/emissive read + 64 B/path framebuffer"},

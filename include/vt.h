@@ -341,10 +341,10 @@ VT_API int vt_job_destroy(vt_job* job);
  * (counter-based random streams, per-pixel sample order).  opts may be NULL
  * (autotuned defaults). */
 typedef struct vt_batch_opts {
-  int32_t tile_pixels;     /* pixels per work item (multiple of 32), 0 = auto   */
+  int32_t path_slots;      /* paths in flight per launch, 0 = auto (1M)          */
   int32_t blocks_per_sm;   /* resident blocks per SM, 0 = auto                  */
   int32_t threads_per_block; /* 0 = auto                                        */
-  int32_t kernel;          /* 0 = auto, 1 = plain per-pixel, 2 = persistent     */
+  int32_t kernel;          /* 0 = auto, 1 = plain per-pixel, 2 = wavefront      */
 } vt_batch_opts;
 VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
                            int32_t passes, const vt_batch_opts* opts,
@@ -355,7 +355,7 @@ typedef struct vt_server_opts {
   uint64_t hbm_budget_bytes;   /* admission budget for job buffers + scenes    */
   int32_t max_active_jobs;     /* slots traced concurrently                     */
   int32_t passes_per_round;    /* samples per pixel each active job gets per round */
-  int32_t tile_pixels;         /* 0 = auto                                      */
+  int32_t path_slots;          /* paths in flight per round, 0 = auto            */
 } vt_server_opts;
 
 enum {

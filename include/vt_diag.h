@@ -60,6 +60,10 @@ VT_API int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int32_t
                                      int32_t height, float* cdf_u, float* cdf_v,
                                      float* integral);
 
+/* Number of rendering kernels (plain, wavefront shade/trace/accumulate) the
+ * context has launched so far. */
+VT_API int vt_diag_launch_count(const vt_context* ctx, uint64_t* launches);
+
 /* The cudaStream_t on which the context issues its work (for timing with
  * CUDA events recorded on that stream). */
 VT_API int vt_diag_stream(vt_context* ctx, void** stream);

@@ -213,8 +213,8 @@ def test_batch_equals_alone(ctx):
             j.render(4)
             alone.append(j.readback().copy())
             j.reset()
-        ctx.render_batch([j for _s, _e, j in made], 2, tile_pixels=64)
-        ctx.render_batch([j for _s, _e, j in made], 2, tile_pixels=96)
+        ctx.render_batch([j for _s, _e, j in made], 2, path_slots=64)
+        ctx.render_batch([j for _s, _e, j in made], 2, path_slots=96)
         for (_s, _e, j), want in zip(made, alone):
             np.testing.assert_array_equal(j.readback().view(np.uint32), want.view(np.uint32))
     finally:

@@ -76,13 +76,13 @@ class RenderSettings(C.Structure):
 
 
 class BatchOpts(C.Structure):
-    _fields_ = [("tile_pixels", C.c_int32), ("blocks_per_sm", C.c_int32), ("threads_per_block", C.c_int32),
+    _fields_ = [("path_slots", C.c_int32), ("blocks_per_sm", C.c_int32), ("threads_per_block", C.c_int32),
                 ("kernel", C.c_int32)]
 
 
 class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_int32), ("passes_per_round", C.c_int32),
-                ("tile_pixels", C.c_int32)]
+                ("path_slots", C.c_int32)]
 
 
 class ServerStats(C.Structure):
@@ -158,6 +158,7 @@ SIGNATURES = {
     "vt_diag_cdf_from_function": [P, P, C.c_int32, C.c_int32, P, P, fp],
     "vt_diag_env_texels": [P, P, C.c_size_t],
     "vt_diag_stream": [P, PP],
+    "vt_diag_launch_count": [P, C.POINTER(C.c_uint64)],
     "vt_diag_set_noise_table": [P, P, C.c_size_t],
     "vt_diag_get_noise_table": [P, P, C.c_size_t],
 }

@@ -148,6 +148,11 @@ extern "C" int vt_destroy(vt_context* ctx) {
   ctx->release(ctx->d_queue);
   ctx->release(ctx->d_error);
   ctx->release(ctx->d_jobs);
+  ctx->release(ctx->d_grids);
+  ctx->release(ctx->wf_mem);
+  ctx->release(ctx->sbuf);
+  ctx->release(ctx->wf_ctl);
+  if (ctx->h_live) cudaFreeHost(ctx->h_live);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -1042,7 +1047,7 @@ extern "C" int vt_job_reset(vt_job* j) {
 
 // Launch `passes` samples per pixel for a set of jobs with the selected kernel.
 int vt::render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int kernel,
-                    int tile_pixels, int blocks_per_sm, bool count) {
+                    int path_slots, int blocks_per_sm, bool count) {
   cudaSetDevice(ctx->device);
   if (count) VT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * C_NUM, ctx->stream), "counters");
   if (kernel == 1) {
@@ -1051,53 +1056,167 @@ int vt::render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32
       for (int k = 0; k < passes[i]; ++k)
         VT_CUDA(launch_plain(j->frame, j->dev, j->samples + k, 1, count ? ctx->d_counters : nullptr, ctx->stream),
                 "plain render");
+      ctx->launches += (uint64_t)passes[i];
     }
     return VT_OK;
   }
-  if (tile_pixels <= 0) tile_pixels = 64;
-  tile_pixels = std::max(32, tile_pixels / 32 * 32);
-  std::vector<JobEntry> entries;
-  entries.reserve(n);
-  int64_t tiles = 0;
-  for (int i = 0; i < n; ++i) {
-    if (passes[i] <= 0) continue;
-    JobEntry e;
-    memset(&e, 0, sizeof(e));
-    e.F = jobs[i]->frame;
-    e.J = jobs[i]->dev;
-    e.sample_base = jobs[i]->samples;
-    e.passes = passes[i];
-    e.tile_begin = tiles;
-    e.n_pixels = (int64_t)jobs[i]->w * jobs[i]->h;
-    tiles += (e.n_pixels + tile_pixels - 1) / tile_pixels;
-    entries.push_back(e);
+  return render_wavefront(ctx, jobs, n, passes, path_slots, blocks_per_sm, count);
+}
+
+// Device buffers of the wavefront for `slots` path slots and `items` samples.
+static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
+  if (ctx->wf_slots < slots) {
+    ctx->release(ctx->wf_mem);
+    ctx->wf_mem = nullptr;
+    ctx->wf_slots = 0;
+    const size_t bytes = (size_t)slots * (7 * sizeof(float4) + sizeof(uint32_t) + 2 * sizeof(int4) + 4 * sizeof(uint32_t));
+    int rc = ctx->alloc(&ctx->wf_mem, bytes);
+    if (rc != VT_OK) return rc;
+    ctx->wf_slots = slots;
   }
-  if (entries.empty()) return VT_OK;
-  const size_t bytes = sizeof(JobEntry) * entries.size();
-  if (ctx->d_jobs_bytes < bytes) {
+  if (ctx->sbuf_items < items) {
+    ctx->release(ctx->sbuf);
+    ctx->sbuf = nullptr;
+    ctx->sbuf_items = 0;
+    int rc = ctx->alloc((void**)&ctx->sbuf, sizeof(float4) * (size_t)items);
+    if (rc != VT_OK) return rc;
+    ctx->sbuf_items = items;
+  }
+  if (!ctx->wf_ctl) {
+    int rc = ctx->alloc((void**)&ctx->wf_ctl, 64);
+    if (rc != VT_OK) return rc;
+  }
+  if (!ctx->h_live) {
+    cudaError_t e = cudaHostAlloc((void**)&ctx->h_live, 64, cudaHostAllocDefault);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc");
+  }
+  return VT_OK;
+}
+
+static WfSlots wf_slots_view(vt_context* ctx) {
+  const size_t S = (size_t)ctx->wf_slots;
+  char* b = (char*)ctx->wf_mem;
+  WfSlots st;
+  float4* f = (float4*)b;
+  st.a0 = f; st.a1 = f + S; st.a2 = f + 2 * S; st.a3 = f + 3 * S; st.a4 = f + 4 * S; st.a5 = f + 5 * S;
+  st.a6 = f + 6 * S;
+  st.hits = (int4*)(f + 7 * S);
+  st.flags = (uint32_t*)(st.hits + 2 * S);
+  return st;
+}
+
+// One wavefront launch over `entries` (tile_begin = first item of each job).
+static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std::vector<Grid>& grids,
+                     int64_t items, int64_t slots_cap, int blocks_per_sm, bool count) {
+  const int64_t slots = std::max<int64_t>(32, std::min<int64_t>(items, slots_cap));
+  int rc = wf_reserve(ctx, slots, items);
+  if (rc != VT_OK) return rc;
+  const size_t jbytes = sizeof(JobEntry) * entries.size();
+  if (ctx->d_jobs_bytes < jbytes) {
     ctx->release(ctx->d_jobs);
     ctx->d_jobs = nullptr;
     ctx->d_jobs_bytes = 0;
-    int rc = ctx->alloc((void**)&ctx->d_jobs, bytes);
+    rc = ctx->alloc((void**)&ctx->d_jobs, jbytes);
     if (rc != VT_OK) return rc;
-    ctx->d_jobs_bytes = bytes;
+    ctx->d_jobs_bytes = jbytes;
   }
-  VT_CUDA(cudaMemcpyAsync(ctx->d_jobs, entries.data(), bytes, cudaMemcpyHostToDevice, ctx->stream), "job table");
-  VT_CUDA(cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned long long), ctx->stream), "queue reset");
-  PersistentParams P;
+  const size_t gbytes = sizeof(Grid) * grids.size();
+  if (ctx->d_grids_bytes < gbytes) {
+    ctx->release(ctx->d_grids);
+    ctx->d_grids = nullptr;
+    ctx->d_grids_bytes = 0;
+    rc = ctx->alloc((void**)&ctx->d_grids, gbytes);
+    if (rc != VT_OK) return rc;
+    ctx->d_grids_bytes = gbytes;
+  }
+  cudaStream_t st = ctx->stream;
+  VT_CUDA(cudaMemcpyAsync(ctx->d_jobs, entries.data(), jbytes, cudaMemcpyHostToDevice, st), "job table");
+  VT_CUDA(cudaMemcpyAsync(ctx->d_grids, grids.data(), gbytes, cudaMemcpyHostToDevice, st), "grid table");
+  WfParams P;
+  memset(&P, 0, sizeof(P));
   P.jobs = ctx->d_jobs;
   P.n_jobs = (int32_t)entries.size();
-  P.n_tiles = tiles;
-  P.tile_pixels = tile_pixels;
-  P.queue = ctx->d_queue;
+  P.grids = ctx->d_grids;
+  P.st = wf_slots_view(ctx);
+  P.n_slots = (int32_t)slots;
+  uint32_t* qmem = (uint32_t*)(P.st.flags + ctx->wf_slots);
+  P.queue[0] = qmem;
+  P.queue[1] = qmem + 2 * ctx->wf_slots;
+  P.ctl = ctx->wf_ctl;
+  P.next_item = (unsigned long long*)(ctx->wf_ctl + 8);
+  P.n_items = (unsigned long long)items;
+  P.sbuf = ctx->sbuf;
   P.counters = count ? ctx->d_counters : nullptr;
-  P.error = ctx->d_error;
-  if (blocks_per_sm <= 0) blocks_per_sm = std::max(1, persistent_max_blocks_per_sm(128));
-  int64_t blocks = (int64_t)ctx->sm_count * blocks_per_sm;
-  const int64_t warps_needed = tiles;
-  blocks = std::min<int64_t>(blocks, (warps_needed + 3) / 4);
-  blocks = std::max<int64_t>(blocks, 1);
-  VT_CUDA(launch_persistent(P, (int)blocks, 128, count, ctx->stream), "persistent render");
+  VT_CUDA(cudaMemsetAsync(P.st.flags, 0, sizeof(uint32_t) * (size_t)slots, st), "slot flags");
+  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, 64, st), "wavefront control");
+  if (ctx->trace_blocks_per_sm <= 0) ctx->trace_blocks_per_sm = std::max(1, wf_trace_blocks_per_sm());
+  const int bps = blocks_per_sm > 0 ? blocks_per_sm : ctx->trace_blocks_per_sm;
+  const int trace_blocks = ctx->sm_count * bps;
+  for (int64_t iter = 0;; ++iter) {
+    const int par = (int)(iter & 1);
+    VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + 4 * par, 0, 3 * sizeof(uint32_t), st), "round counters");
+    VT_CUDA(launch_wf_shade(P, par, count, st), "wavefront shade");
+    VT_CUDA(launch_wf_trace(P, par, trace_blocks, count, st), "wavefront trace");
+    ctx->launches += 2;
+    if ((iter & 7) == 7) {
+      VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + 4 * par + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+              "live count");
+      VT_CUDA(cudaStreamSynchronize(st), "wavefront round");
+      if (*(volatile uint32_t*)ctx->h_live == 0) break;
+    }
+  }
+  long long max_pixels = 0;
+  for (const JobEntry& e : entries) max_pixels = std::max<long long>(max_pixels, e.n_pixels);
+  VT_CUDA(launch_wf_accumulate(ctx->d_jobs, (int)entries.size(), max_pixels, ctx->sbuf, st), "accumulate");
+  ctx->launches += 1;
+  return VT_OK;
+}
+
+// Wavefront rendering of passes[i] samples per pixel for each job, split in
+// launches whose sample buffers stay within ctx->max_items.
+int vt::render_wavefront(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int slots,
+                         int blocks_per_sm, bool count) {
+  std::vector<int32_t> done(n, 0);
+  const int64_t slots_cap = slots > 0 ? slots : ctx->max_slots;
+  for (;;) {
+    int64_t pix_left = 0;
+    for (int i = 0; i < n; ++i)
+      if (done[i] < passes[i]) pix_left += (int64_t)jobs[i]->w * jobs[i]->h;
+    if (pix_left == 0) break;
+    const int32_t q = (int32_t)std::max<int64_t>(1, ctx->max_items / pix_left);
+    std::vector<JobEntry> entries;
+    std::vector<Grid> grids;
+    int64_t items = 0;
+    for (int i = 0; i < n; ++i) {
+      const int32_t p = std::min(q, passes[i] - done[i]);
+      if (p <= 0) continue;
+      JobEntry e;
+      memset(&e, 0, sizeof(e));
+      e.F = jobs[i]->frame;
+      e.J = jobs[i]->dev;
+      e.sample_base = jobs[i]->samples + done[i];
+      e.passes = p;
+      e.tile_begin = items;
+      e.n_pixels = (int64_t)jobs[i]->w * jobs[i]->h;
+      items += e.n_pixels * p;
+      entries.push_back(e);
+      Grid g;
+      memset(&g, 0, sizeof(g));
+      const Frame& F = jobs[i]->frame;
+      g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
+      g.bx = F.bdim[0]; g.bxy = F.bdim[0] * F.bdim[1];
+      g.max_steps = F.max_steps;
+      g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
+      g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
+      g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
+      g.bricks = jobs[i]->dev.bricks;
+      grids.push_back(g);
+      done[i] += p;
+    }
+    if (items >= ((int64_t)1 << 32)) return fail(VT_EINVAL, "more than 2^32 samples in one launch");
+    int rc = wf_launch(ctx, entries, grids, items, slots_cap, blocks_per_sm, count);
+    if (rc != VT_OK) return rc;
+  }
   return VT_OK;
 }
 
@@ -1186,7 +1305,7 @@ extern "C" int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_j
     np[i] = job_passes(jobs[i], passes);
   }
   const int kernel = (opts && opts->kernel) ? opts->kernel : ctx->kernel;
-  int rc = render_jobs(ctx, jobs, n_jobs, np.data(), kernel, opts ? opts->tile_pixels : 0,
+  int rc = render_jobs(ctx, jobs, n_jobs, np.data(), kernel, opts ? opts->path_slots : 0,
                        opts ? opts->blocks_per_sm : 0, false);
   if (rc != VT_OK) return rc;
   for (int i = 0; i < n_jobs; ++i) {
@@ -1297,6 +1416,12 @@ extern "C" int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int
   VT_CUDA(cudaMemcpyAsync(&iv, d_int, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "cdf");
   VT_CUDA(cudaStreamSynchronize(ctx->stream), "cdf");
   if (integral) *integral = iv;
+  return VT_OK;
+}
+
+extern "C" int vt_diag_launch_count(const vt_context* ctx, uint64_t* launches) {
+  VT_CHECK_ARG(ctx && launches, "null argument");
+  *launches = ctx->launches;
   return VT_OK;
 }
 

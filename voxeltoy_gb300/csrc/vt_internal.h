@@ -69,6 +69,18 @@ struct Frame {
   int32_t height;
 };
 
+// What the DDA needs of a volume: extents, bounds, brick layout, step cap.
+struct Grid {
+  int32_t rx, ry, rz;
+  int32_t bx, bxy;           // brick-grid row and slice strides
+  int32_t max_steps;         // int(2*ceil(length(vec3(res)))), dda.h:98
+  float bminx, bminy, bminz;
+  float vextx, vexty, vextz; // 1/(bmax-bmin), dda.h:16
+  float bmaxx, bmaxy, bmaxz;
+  int32_t pad;
+  const unsigned long long* bricks;
+};
+
 // Device pointers of everything one job reads and writes.
 struct JobDev {
   const uint8_t* grid;

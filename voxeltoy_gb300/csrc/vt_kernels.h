@@ -15,7 +15,7 @@ struct JobEntry {
   JobDev J;
   int32_t sample_base;    // first sample index of this launch
   int32_t passes;         // samples per pixel in this launch
-  int64_t tile_begin;     // first global tile index of this job
+  int64_t tile_begin;     // first global work item (sample) of this job
   int64_t n_pixels;
 };
 
@@ -24,18 +24,38 @@ cudaError_t launch_plain(const Frame& F, const JobDev& J, int sample_base, int p
                          unsigned long long* counters, cudaStream_t st);
 cudaError_t launch_diag(const Frame& F, const JobDev& J, int sample, float4* out, HitRecord* hits,
                         unsigned long long* counters, cudaStream_t st);
-struct PersistentParams {
-  const JobEntry* jobs;          // device array
-  int32_t n_jobs;
-  int64_t n_tiles;               // total tiles over all jobs
-  int32_t tile_pixels;           // multiple of 32
-  unsigned long long* queue;     // device work counter, zeroed before launch
-  unsigned long long* counters;  // nullable
-  int32_t* error;                // device error word
+// Wavefront path state, structure of arrays over the path slots.
+struct WfSlots {
+  float4* a0;      // ro.xyz, bsdf_pdf
+  float4* a1;      // rd.xyz, light (int bits)
+  float4* a2;      // sd.xyz, rng state (uint bits)
+  float4* a3;      // L.xyz, sample (uint bits)
+  float4* a4;      // T.xyz, pixel (uint bits)
+  float4* a5;      // nee_T.xyz, job (uint bits)
+  float4* a6;      // nee_C.xyz, item (uint bits)
+  uint32_t* flags; // bounces | primary | has_cont | ext | shadow | active | dead
+  int4* hits;      // [2][n_slots] segment ends: extension, shadow
 };
-cudaError_t launch_persistent(const PersistentParams& P, int blocks, int threads, bool count,
-                              cudaStream_t st);
-int persistent_max_blocks_per_sm(int threads);
+struct WfParams {
+  const JobEntry* jobs;            // device array, tile_begin = first item of the job
+  int32_t n_jobs;
+  const Grid* grids;               // device array, DDA view of each job's volume
+  WfSlots st;
+  int32_t n_slots;
+  uint32_t* queue[2];              // segment entries: slot << 2 | primary << 1 | kind
+  uint32_t* ctl;                   // per parity i: ctl[4i] entries appended to queue[i],
+                                   // ctl[4i+1] entries taken by the tracer,
+                                   // ctl[4i+2] active slots after the shade
+  unsigned long long* next_item;
+  unsigned long long n_items;
+  float4* sbuf;                    // per-item sample outputs
+  unsigned long long* counters;    // nullable
+};
+cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st);
+cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, bool count, cudaStream_t st);
+cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max_pixels, const float4* sbuf,
+                                 cudaStream_t st);
+int wf_trace_blocks_per_sm();
 cudaError_t launch_trace_rays(const Frame& F, const JobDev& J, const float* origins, const float* dirs,
                               int64_t n, int32_t* out, cudaStream_t st);
 cudaError_t launch_pick(const Frame& F, const JobDev& J, float x, float y, float* out_dist,

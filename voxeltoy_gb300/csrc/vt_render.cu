@@ -2,13 +2,13 @@
 //
 //   k_plain       one thread per pixel, `passes` samples per launch; the
 //                 reference's one-pass-per-draw structure (renderer.cpp:584-611)
-//   k_persistent  one launch for many jobs and passes: warps pull
-//                 (job, 32-pixel tile) work items from a device counter, and
-//                 every lane regenerates paths for its pixel until the tile's
-//                 samples are done.  Lanes whose segment ended wait until at
-//                 least half the warp needs an event, so shading runs with
-//                 most of the warp active while the DDA loop keeps running
-//                 for the rest.
+//   wavefront     many jobs and passes per launch, in rounds of two kernels:
+//                 k_wf_shade (one thread per path slot: segment results ->
+//                 shading -> new segments appended to a queue by warp
+//                 ballot, new items started as paths finish) and k_wf_trace
+//                 (DDA of every queued segment with per-warp refill from the
+//                 queue); per-sample outputs land in a sample buffer that
+//                 k_wf_accumulate reduces in sample order.
 //   k_diag        per-sample output and first-hit record (parity tests)
 //   k_trace_rays  DDA of caller-supplied rays (parity tests)
 //   k_pick        focal-distance pick of one pixel (focalDistance.vs:45-81)
@@ -86,106 +86,276 @@ cudaError_t launch_diag(const Frame& F, const JobDev& J, int sample, float4* out
   return cudaGetLastError();
 }
 
-// ------------------------------------------------------------- persistent
-constexpr int kPersistThreads = 128;
-constexpr int kWarpsPerBlock = kPersistThreads / 32;
+// -------------------------------------------------------------- wavefront
+// Slot flags.
+enum : uint32_t {
+  SL_BOUNCES = 0xffu,
+  SL_PRIMARY = 1u << 8,
+  SL_HAS_CONT = 1u << 9,
+  SL_EXT = 1u << 10,      // an extension segment was traced for this slot
+  SL_SHADOW = 1u << 11,   // a shadow segment was traced for this slot
+  SL_ACTIVE = 1u << 12,
+  SL_DEAD = 1u << 13,     // no work left for this slot in this launch
+};
 
+__device__ __forceinline__ v3 xyz4(float4 v) { return mk3(v.x, v.y, v.z); }
+__device__ __forceinline__ float4 pack4(v3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
+
+// Job of a global item index (binary search over item_begin).
+__device__ __forceinline__ int job_of(const JobEntry* jobs, int n_jobs, unsigned long long item) {
+  int lo = 0, hi = n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((unsigned long long)__ldg(&jobs[mid].tile_begin) <= item) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void load_path(const WfSlots& st, int slot, uint32_t fl, const Frame& F, Path& p) {
+  const float4 a0 = st.a0[slot], a1 = st.a1[slot], a2 = st.a2[slot];
+  const float4 a3 = st.a3[slot], a4 = st.a4[slot], a5 = st.a5[slot], a6 = st.a6[slot];
+  p.ro = xyz4(a0); p.bsdf_pdf = a0.w;
+  p.rd = xyz4(a1); p.light = __float_as_int(a1.w);
+  p.sd = xyz4(a2);
+  p.L = xyz4(a3);
+  p.T = xyz4(a4);
+  p.nee_T = xyz4(a5);
+  p.nee_C = xyz4(a6);
+  p.bounces = (int)(fl & SL_BOUNCES);
+  p.primary = (fl & SL_PRIMARY) ? 1 : 0;
+  p.has_cont = (fl & SL_HAS_CONT) ? 1 : 0;
+  const uint32_t rng = __float_as_uint(a2.w);
+  p.rng.pixel = __float_as_uint(a4.w);
+  p.rng.sample = __float_as_uint(a3.w);
+  if (F.rng_mode == 1) { p.rng.ox = (int32_t)(rng & 0xffffu); p.rng.oy = (int32_t)(rng >> 16); p.rng.call = 0; }
+  else { p.rng.call = rng; p.rng.ox = p.rng.oy = 0; }
+}
+
+__device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Frame& F, const Path& p, uint32_t job,
+                                           uint32_t item) {
+  const uint32_t rng = (F.rng_mode == 1) ? ((uint32_t)p.rng.ox | ((uint32_t)p.rng.oy << 16)) : p.rng.call;
+  st.a0[slot] = pack4(p.ro, p.bsdf_pdf);
+  st.a1[slot] = pack4(p.rd, __int_as_float(p.light));
+  st.a2[slot] = pack4(p.sd, __uint_as_float(rng));
+  st.a3[slot] = pack4(p.L, __uint_as_float(p.rng.sample));
+  st.a4[slot] = pack4(p.T, __uint_as_float(p.rng.pixel));
+  st.a5[slot] = pack4(p.nee_T, __uint_as_float(job));
+  st.a6[slot] = pack4(p.nee_C, __uint_as_float(item));
+}
+
+// One round of shading: consume the segment results of the previous trace,
+// retire finished paths into the sample buffer, start new items, and append
+// the next segments to queue[par] (warp-aggregated).
 template <bool kCount>
-__global__ void __launch_bounds__(kPersistThreads) k_persistent(const PersistentParams P) {
-  __shared__ JobEntry s_job[kWarpsPerBlock];
+__global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
-  JobEntry& E = s_job[wid];
-  const Frame& F = E.F;
-  const JobDev& J = E.J;
+  const unsigned lt = (1u << lane) - 1u;
+  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool in_range = slot < P.n_slots;
   Cnt<kCount> cnt;
 #pragma unroll
   for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
-  int cur_job = -1;
-  const int tiles_per_item = P.tile_pixels >> 5;   // lane owns tiles_per_item pixels, one after another
-
+  uint32_t fl = in_range ? P.st.flags[slot] : SL_DEAD;
+  bool active = (fl & SL_ACTIVE) != 0;
+  bool need_new = !active && !(fl & SL_DEAD);
+  Path p;
+  uint32_t job = 0, item = 0;
+  uint32_t emit = 0;   // 1: extension, 2: shadow
+  if (active) {
+    const float4 a5 = P.st.a5[slot], a6 = P.st.a6[slot];
+    job = __float_as_uint(a5.w);
+    item = __float_as_uint(a6.w);
+    const JobEntry& E = P.jobs[job];
+    load_path(P.st, slot, fl, E.F, p);
+    if (fl & SL_SHADOW) {
+      const int4 h = P.st.hits[(size_t)P.n_slots + slot];
+      SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
+      shadow_end(E.F, p, e);
+    }
+    bool alive = false;
+    if (fl & SL_EXT) {
+      const int4 h = P.st.hits[slot];
+      SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
+      alive = ext_end(E.F, E.J, p, e, cnt);
+    }
+    if (alive) {
+      emit = 2u | (p.has_cont ? 1u : 0u);
+    } else {
+      P.sbuf[item] = path_output(E.F, p);
+      active = false;
+      need_new = true;
+    }
+  }
+  // start new items, warp-aggregated; a path that misses the volume is
+  // finished at once and its lane asks again
+  bool dead = (fl & SL_DEAD) != 0;
   for (;;) {
-    unsigned long long item = 0;
-    if (lane == 0) item = atomicAdd(P.queue, 1ull);
-    item = __shfl_sync(0xffffffffu, item, 0);
-    if ((long long)item >= P.n_tiles) break;
-    // locate the job of this tile: binary search over tile_begin
-    int lo = 0, hi = P.n_jobs - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if ((long long)__ldg(&P.jobs[mid].tile_begin) <= (long long)item) lo = mid; else hi = mid - 1;
-    }
-    if (lo != cur_job) {
-      __syncwarp();
-      const int words = (int)(sizeof(JobEntry) / 4);
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(&P.jobs[lo]);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(&E);
-      for (int w = lane; w < words; w += 32) dst[w] = __ldg(&src[w]);
-      __syncwarp();
-      cur_job = lo;
-    }
-    const long long tile = (long long)item - E.tile_begin;
-    const int passes = E.passes;
-    const int base = E.sample_base;
-    // lane-local work: pixels tile*tile_pixels + lane + 32*k, k < tiles_per_item
-    int k_pix = 0;
-    long long pix = tile * P.tile_pixels + lane;
-    bool active = pix < E.n_pixels;
-    int sample = 0;
-    Path p;
-    Dda s;
-    float4 sum = make_float4(0.f, 0.f, 0.f, 0.f), comp = sum;
-    if (active) {
-      sum = J.sum[pix]; comp = J.comp[pix];
-      path_start(F, J, p, s, (int)(pix % F.width), (int)(pix / F.width), base, cnt);
-    }
-    for (;;) {
-      // traversal: keep stepping while more than half of the live lanes are mid-segment
-      for (;;) {
-        const bool run = active && p.phase != PH_DONE && s.state == DDA_RUNNING;
-        const unsigned live = __ballot_sync(0xffffffffu, active);
-        const unsigned running = __ballot_sync(0xffffffffu, run);
-        if (live == 0u || running == 0u || 2 * __popc(running) < __popc(live)) break;
-        if (run) dda_advance(F, J, s, 8, cnt);
-      }
-      if (active) {
-        if (p.phase != PH_DONE && s.state != DDA_RUNNING) path_event(F, J, p, s, cnt);
-        if (p.phase == PH_DONE) {
-          kahan_add(sum, comp, path_output(F, p));
-          ++sample;
-          if (sample < passes) {
-            path_start(F, J, p, s, (int)(pix % F.width), (int)(pix / F.width), base + sample, cnt);
-          } else {
-            J.sum[pix] = sum; J.comp[pix] = comp;
-            ++k_pix;
-            pix += 32;
-            active = (k_pix < tiles_per_item) && pix < E.n_pixels;
-            sample = 0;
-            if (active) {
-              sum = J.sum[pix]; comp = J.comp[pix];
-              path_start(F, J, p, s, (int)(pix % F.width), (int)(pix / F.width), base, cnt);
-            }
-          }
+    const unsigned want = __ballot_sync(FULL, need_new);
+    if (!want) break;
+    const int leader = __ffs(want) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(P.next_item, (unsigned long long)__popc(want));
+    base = __shfl_sync(FULL, base, leader);
+    if (need_new) {
+      const unsigned long long my = base + __popc(want & lt);
+      if (my >= P.n_items) {
+        need_new = false;
+        dead = true;
+      } else {
+        item = (uint32_t)my;
+        job = (uint32_t)job_of(P.jobs, P.n_jobs, my);
+        const JobEntry& E = P.jobs[job];
+        const long long r = (long long)my - (long long)E.tile_begin;
+        const int pass = (int)(r / E.n_pixels);
+        const int pixel = (int)(r - (long long)pass * E.n_pixels);
+        const int px = pixel % E.F.width, py = pixel / E.F.width;
+        if (path_start(E.F, E.J, p, px, py, E.sample_base + pass, cnt)) {
+          active = true;
+          need_new = false;
+          emit = 1u;
+        } else {
+          P.sbuf[item] = path_output(E.F, p);
         }
       }
-      if (__ballot_sync(0xffffffffu, active) == 0u) break;
+    }
+  }
+  // append the next segments: entry = slot << 2 | primary << 1 | kind
+  const uint32_t n1 = (emit & 1u) ? 1u : 0u, n2 = (emit & 2u) ? 1u : 0u;
+  const unsigned b1 = __ballot_sync(FULL, n1), b2 = __ballot_sync(FULL, n2);
+  const uint32_t tot = __popc(b1) + __popc(b2);
+  if (tot) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(&P.ctl[4 * par], tot);
+    base = __shfl_sync(FULL, base, 0);
+    // the warp's extension entries first, then its shadow entries
+    uint32_t* q = P.queue[par];
+    if (n1) q[base + __popc(b1 & lt)] = ((uint32_t)slot << 2) | (p.primary ? 2u : 0u);
+    if (n2) q[base + __popc(b1) + __popc(b2 & lt)] = ((uint32_t)slot << 2) | 1u;
+  }
+  if (in_range) {
+    uint32_t nf;
+    if (active) {
+      const JobEntry& E = P.jobs[job];
+      store_path(P.st, slot, E.F, p, job, item);
+      nf = SL_ACTIVE | (uint32_t)(p.bounces & 0xff) | (p.primary ? SL_PRIMARY : 0u) |
+           (p.has_cont ? SL_HAS_CONT : 0u) | ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u);
+    } else {
+      nf = dead ? SL_DEAD : 0u;
+    }
+    P.st.flags[slot] = nf;
+  }
+  const unsigned live = __ballot_sync(FULL, active);
+  if (lane == 0 && live) atomicAdd(&P.ctl[4 * par + 2], (uint32_t)__popc(live));
+  flush_counters(cnt, P.counters);
+}
+
+// One round of tracing: every queued segment runs its DDA to the end.  Each
+// warp takes chunks of queue entries with one atomic and hands them to its
+// lanes as they finish their previous segment, so lanes stay busy until the
+// queue is drained.
+constexpr uint32_t kTraceChunk = 128;
+constexpr int kTraceSteps = 8;
+
+template <bool kCount>
+__global__ void __launch_bounds__(256) k_wf_trace(const WfParams P, int par) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const uint32_t n = *(volatile uint32_t*)&P.ctl[4 * par];
+  if (n == 0) return;
+  const uint32_t* q = P.queue[par];
+  Cnt<kCount> cnt;
+#pragma unroll
+  for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
+  uint32_t pool = 0, pool_end = 0;
+  bool exhausted = false, have = false;
+  Grid g;
+  Dda s;
+  uint32_t entry = 0;
+  for (;;) {
+    unsigned need = __ballot_sync(FULL, !have);
+    while (need && !exhausted) {
+      if (pool >= pool_end) {
+        uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(&P.ctl[4 * par + 1], kTraceChunk);
+        c = __shfl_sync(FULL, c, 0);
+        if (c >= n) { exhausted = true; break; }
+        pool = c;
+        pool_end = min(c + kTraceChunk, n);
+      }
+      const uint32_t avail = pool_end - pool;
+      const uint32_t r = __popc(need & lt);
+      if (!have && r < avail) {
+        entry = __ldg(&q[pool + r]);
+        const int slot = (int)(entry >> 2);
+        const uint32_t job = __float_as_uint(__ldg(&P.st.a5[slot].w));
+        g = P.grids[job];
+        const float4 a0 = __ldg(&P.st.a0[slot]);
+        const float4 ad = (entry & 1u) ? __ldg(&P.st.a2[slot]) : __ldg(&P.st.a1[slot]);
+        v3 o = xyz4(a0);
+        const v3 d = xyz4(ad);
+        if (entry & 2u) o = primary_origin(o, d, mk3(g.bminx, g.bminy, g.bminz), mk3(g.bmaxx, g.bmaxy, g.bmaxz));
+        dda_begin(g, s, o, d);
+        if (s.state == DDA_RUNNING) {
+          have = true;
+        } else {
+          P.st.hits[(size_t)(entry & 1u) * P.n_slots + slot] = make_int4(s.x, s.y, s.z, s.state);
+        }
+      }
+      pool += min(avail, (uint32_t)__popc(need));
+      need = __ballot_sync(FULL, !have);
+    }
+    if (__ballot_sync(FULL, have) == 0u) break;
+    if (have) {
+      dda_advance(g, s, kTraceSteps, cnt);
+      if (s.state != DDA_RUNNING) {
+        const int slot = (int)(entry >> 2);
+        P.st.hits[(size_t)(entry & 1u) * P.n_slots + slot] = make_int4(s.x, s.y, s.z, s.state);
+        have = false;
+      }
     }
   }
   flush_counters(cnt, P.counters);
 }
 
-int persistent_max_blocks_per_sm(int threads) {
-  int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_persistent<false>, threads, 0);
-  return n;
+// Ordered reduction of the per-sample outputs into each pixel's Kahan sums:
+// sample order within a pixel is the same as one sample per launch.
+__global__ void k_wf_accumulate(const JobEntry* jobs, const float4* sbuf) {
+  const JobEntry& E = jobs[blockIdx.y];
+  const long long px = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (px >= E.n_pixels || E.passes <= 0) return;
+  float4 sum = E.J.sum[px], comp = E.J.comp[px];
+  for (int k = 0; k < E.passes; ++k) kahan_add(sum, comp, sbuf[E.tile_begin + (long long)k * E.n_pixels + px]);
+  E.J.sum[px] = sum;
+  E.J.comp[px] = comp;
 }
 
-cudaError_t launch_persistent(const PersistentParams& P, int blocks, int threads, bool count,
-                              cudaStream_t st) {
-  (void)threads;
-  if (count) k_persistent<true><<<blocks, kPersistThreads, 0, st>>>(P);
-  else k_persistent<false><<<blocks, kPersistThreads, 0, st>>>(P);
+cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st) {
+  const int blocks = (P.n_slots + 127) / 128;
+  if (count) k_wf_shade<true><<<blocks, 128, 0, st>>>(P, par);
+  else k_wf_shade<false><<<blocks, 128, 0, st>>>(P, par);
   return cudaGetLastError();
+}
+
+cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, bool count, cudaStream_t st) {
+  if (count) k_wf_trace<true><<<blocks, 256, 0, st>>>(P, par);
+  else k_wf_trace<false><<<blocks, 256, 0, st>>>(P, par);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max_pixels, const float4* sbuf,
+                                 cudaStream_t st) {
+  if (n_jobs <= 0 || max_pixels <= 0) return cudaSuccess;
+  dim3 grid((unsigned)((max_pixels + 255) / 256), (unsigned)n_jobs);
+  k_wf_accumulate<<<grid, 256, 0, st>>>(jobs, sbuf);
+  return cudaGetLastError();
+}
+
+int wf_trace_blocks_per_sm() {
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false>, 256, 0);
+  return n;
 }
 
 // ------------------------------------------------------------- trace rays
@@ -198,8 +368,9 @@ __global__ void k_trace_rays(const Frame F, const JobDev J, const float* origins
   const v3 o = mk3(origins[3 * i], origins[3 * i + 1], origins[3 * i + 2]);
   const v3 d = mk3(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]);
   Dda s;
-  dda_begin(F, s, o, d);
-  if (s.state == DDA_RUNNING) dda_advance(F, J, s, 0x7fffffff, cnt);
+  const Grid g = grid_of(F, J);
+  dda_begin(g, s, o, d);
+  if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
   const bool h = dda_hit(F, s);
   int flags = (h ? 1 : 0) << 8 | ((h && s.state != DDA_HIT) ? 1 : 0) << 9 | (s.steps << 10);
   if (h) {
@@ -232,8 +403,9 @@ __global__ void k_pick(const Frame F, const JobDev J, float x, float y, float* o
   const float t = ray_aabb(o, d, ld3(F.bmin), ld3(F.bmax));
   if (t < 0.0f) return;
   Dda s;
-  dda_begin(F, s, o + t * d, d);
-  if (s.state == DDA_RUNNING) dda_advance(F, J, s, 0x7fffffff, cnt);
+  const Grid g = grid_of(F, J);
+  dda_begin(g, s, o + t * d, d);
+  if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
   if (!dda_hit(F, s)) return;
   const v3 vs = ld3(F.vsize);
   const v3 vmin = mk3((float)s.x, (float)s.y, (float)s.z) * vs + ld3(F.bmin);

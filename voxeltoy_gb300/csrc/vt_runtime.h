@@ -27,6 +27,19 @@ struct vt_context {
   size_t scratch_bytes = 0;
   vt::JobEntry* d_jobs = nullptr;
   size_t d_jobs_bytes = 0;
+  // wavefront buffers (grown on demand)
+  vt::Grid* d_grids = nullptr;
+  size_t d_grids_bytes = 0;
+  void* wf_mem = nullptr;        // slot state, flags, hits, queues
+  int64_t wf_slots = 0;
+  float4* sbuf = nullptr;        // per-sample outputs of one launch
+  int64_t sbuf_items = 0;
+  uint32_t* wf_ctl = nullptr;    // [2][4] qcount, qhead, live, pad + next_item
+  uint32_t* h_live = nullptr;    // pinned host copy of a live counter
+  int64_t max_slots = 1 << 20;   // path slots per launch
+  int64_t max_items = 1 << 28;   // samples per launch (sample buffer entries)
+  int trace_blocks_per_sm = 0;   // 0 = occupancy limit
+  uint64_t launches = 0;         // render kernels launched by this context
   unsigned long long* d_counters = nullptr;
   unsigned long long* d_queue = nullptr;
   int32_t* d_error = nullptr;
@@ -87,4 +100,7 @@ int build_frame(vt_job* j);
 // passes[i] samples per pixel for jobs[i]; kernel 1 = plain, 2 = persistent.
 int render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int kernel,
                 int tile_pixels, int blocks_per_sm, bool count);
+// Wavefront form; `slots` path slots per launch (0 = context default).
+int render_wavefront(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int slots,
+                     int blocks_per_sm, bool count);
 }  // namespace vt

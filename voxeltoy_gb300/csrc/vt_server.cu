@@ -164,7 +164,7 @@ void vt_server::run() {
       passes.push_back(p);
       paths += (uint64_t)r->w * r->h * (uint64_t)p;
     }
-    int rc = render_jobs(&lane, jobs.data(), (int32_t)jobs.size(), passes.data(), 2, opts.tile_pixels, 0, false);
+    int rc = render_jobs(&lane, jobs.data(), (int32_t)jobs.size(), passes.data(), 2, opts.path_slots, 0, false);
     if (rc == VT_OK && cudaStreamSynchronize(lane.stream) != cudaSuccess) rc = VT_EDEVICE;
     std::unique_lock<std::mutex> g(mu);
     stats.rounds++;

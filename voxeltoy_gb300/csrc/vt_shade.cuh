@@ -208,6 +208,18 @@ VT_D v3 world_to_local(v3 w, const Basis& b) {
 }
 
 // -------------------------------------------------------------------- dda
+VT_D Grid grid_of(const Frame& F, const JobDev& J) {
+  Grid g;
+  g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
+  g.bx = F.bdim[0]; g.bxy = F.bdim[0] * F.bdim[1];
+  g.max_steps = F.max_steps;
+  g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
+  g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
+  g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
+  g.bricks = J.bricks;
+  return g;
+}
+
 struct Dda {
   int32_t x, y, z;
   float dx, dy, dz;    // distances to the next face crossing (dda.h:34)
@@ -223,17 +235,17 @@ enum { DDA_RUNNING = 0, DDA_HIT = 1, DDA_MISS = 2 };
 // raymarch set-up (dda.h:15-34).  An origin outside the grid ends the
 // segment at once with the out-of-grid voxel as position (the reference
 // leaves the out parameter unwritten there).
-VT_D void dda_begin(const Frame& F, Dda& s, v3 o, v3 d) {
-  const v3 bmin = ld3(F.bmin);
+VT_D void dda_begin(const Grid& g, Dda& s, v3 o, v3 d) {
+  const v3 bmin = mk3(g.bminx, g.bminy, g.bminz);
   o = o + mk3(vtb::gsign(d.x), vtb::gsign(d.y), vtb::gsign(d.z)) * 0.001f;
-  const v3 vo = ((o - bmin) * ld3(F.vext)) * mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
+  const v3 vo = ((o - bmin) * mk3(g.vextx, g.vexty, g.vextz)) * mk3((float)g.rx, (float)g.ry, (float)g.rz);
   const v3 vp = mk3(floorf(vo.x), floorf(vo.y), floorf(vo.z));
   s.x = (int32_t)vp.x; s.y = (int32_t)vp.y; s.z = (int32_t)vp.z;
   s.steps = 0;
   s.cb = -1;
   s.bits = 0ull;
-  if (vp.x < 0.0f || vp.y < 0.0f || vp.z < 0.0f || vp.x >= (float)F.res[0] ||
-      vp.y >= (float)F.res[1] || vp.z >= (float)F.res[2]) {
+  if (vp.x < 0.0f || vp.y < 0.0f || vp.z < 0.0f || vp.x >= (float)g.rx || vp.y >= (float)g.ry ||
+      vp.z >= (float)g.rz) {
     s.state = DDA_MISS;
     return;
   }
@@ -252,22 +264,19 @@ VT_D void dda_begin(const Frame& F, Dda& s, v3 o, v3 d) {
 // DDA loop (dda.h:38-57): at most `budget` iterations of
 // bounds test -> occupancy test -> advance every minimal axis.
 template <bool kCount>
-VT_D void dda_advance(const Frame& F, const JobDev& J, Dda& s, int budget, Cnt<kCount>& cnt) {
-  const int rx = F.res[0], ry = F.res[1], rz = F.res[2];
-  const int bx = F.bdim[0], bxy = F.bdim[0] * F.bdim[1];
+VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt) {
   int x = s.x, y = s.y, z = s.z, steps = s.steps, cb = s.cb;
   float dx = s.dx, dy = s.dy, dz = s.dz;
   unsigned long long bits = s.bits;
   int state = DDA_RUNNING;
-  const int max_steps = F.max_steps;
   while (budget-- > 0) {
-    if (steps >= max_steps) { state = DDA_MISS; break; }
-    if ((unsigned)x >= (unsigned)rx || (unsigned)y >= (unsigned)ry || (unsigned)z >= (unsigned)rz) {
+    if (steps >= g.max_steps) { state = DDA_MISS; break; }
+    if ((unsigned)x >= (unsigned)g.rx || (unsigned)y >= (unsigned)g.ry || (unsigned)z >= (unsigned)g.rz) {
       state = DDA_MISS; break;
     }
     cnt.add(C_DDA_CELLS, 1);
-    const int b = (x >> 2) + bx * (y >> 2) + bxy * (z >> 2);
-    if (b != cb) { bits = __ldg(&J.bricks[b]); cb = b; }
+    const int b = (x >> 2) + g.bx * (y >> 2) + g.bxy * (z >> 2);
+    if (b != cb) { bits = __ldg(&g.bricks[b]); cb = b; }
     if ((bits >> ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4))) & 1ull) { state = DDA_HIT; break; }
     const bool mx = (dy >= dx) && (dz >= dx);
     const bool my = (dx >= dy) && (dz >= dy);
@@ -283,10 +292,15 @@ VT_D void dda_advance(const Frame& F, const JobDev& J, Dda& s, int budget, Cnt<k
 }
 
 // traverse (dda.h:63-79): voxel hit, or with the ground quirk an exit below y = 0.
-VT_D bool dda_hit(const Frame& F, const Dda& s) {
-  if (s.state == DDA_HIT) return true;
-  return (F.quirks & Q_GROUND) && s.y < 0;
+VT_D bool seg_hit(uint32_t quirks, int state, int y) {
+  if (state == DDA_HIT) return true;
+  return (quirks & Q_GROUND) && y < 0;
 }
+VT_D bool dda_hit(const Frame& F, const Dda& s) { return seg_hit(F.quirks, s.state, s.y); }
+
+// End of one DDA segment as the shading code sees it.
+struct SegEnd { int32_t x, y, z, state; };
+VT_D SegEnd seg_end(const Dda& s) { SegEnd e; e.x = s.x; e.y = s.y; e.z = s.z; e.state = s.state; return e; }
 
 // --------------------------------------------------------------- sampling
 // sampling.h:2-43
@@ -552,20 +566,29 @@ VT_D void generate_ray(const Frame& F, const JobDev& J, v3 frag, Rng& rng, v3& o
 }
 
 // ------------------------------------------------------------ path state
-enum { PH_EXT = 0, PH_SHADOW = 1, PH_DONE = 2 };
-
+// A path alternates between DDA segments and shading events:
+//   path_start   raygen and volume clip; leaves an extension segment (the
+//                primary ray, traced from the volume entry point) or ends
+//   ext_end      end of an extension segment: miss -> environment, hit ->
+//                shade the vertex, which leaves a shadow segment (ro, sd)
+//                and, unless the path ends there, a continuation (ro, rd)
+//   shadow_end   end of a shadow segment: add the light sample if visible
+// The megakernel runs these one segment at a time; the wavefront traces the
+// shadow and continuation segments of a vertex in the same round and runs
+// shadow_end before ext_end, which performs the same operations in the same
+// order as the reference loop.
 struct Path {
   Rng rng;
   v3 L;          // radiance
   v3 T;          // throughput
-  v3 ro, rd;     // current ray: origin used for the exact hit, direction
-  v3 cont_d;     // continuation direction, traced after the shadow ray
+  v3 ro;         // origin of the current extension ray (camera or last vertex)
+  v3 rd;         // direction of the current extension ray
+  v3 sd;         // direction of the pending shadow ray (origin ro)
   v3 nee_T;      // throughput at the vertex of the pending light sample
   v3 nee_C;      // directLighting value if the light is visible
   int32_t light; // emissive voxel index of the light sample, -1 = environment
   float bsdf_pdf;
   int32_t bounces;
-  int32_t phase;
   int32_t primary;
   int32_t has_cont;
 };
@@ -580,12 +603,11 @@ VT_D float4 path_output(const Frame& F, const Path& p) {
   return make_float4(p.L.x, p.L.y, p.L.z, 1.0f);
 }
 
-
-// main() up to the primary traversal (pathTracer.fs:172-208).  Leaves the
-// path in PH_EXT with the primary DDA set up, or PH_DONE on a miss.
+// main() up to the primary traversal (pathTracer.fs:172-196).  Returns true
+// if the primary ray enters the volume; its segment then starts at
+// ro + t*rd with t = ray_aabb(ro, rd, bounds) (see primary_origin).
 template <bool kCount>
-VT_D void path_start(const Frame& F, const JobDev& J, Path& p, Dda& s, int px, int py, int sample,
-                     Cnt<kCount>& cnt) {
+VT_D bool path_start(const Frame& F, const JobDev& J, Path& p, int px, int py, int sample, Cnt<kCount>& cnt) {
   rng_init(F, p.rng, px, py, sample);
   cnt.add(C_PATHS, 1);
   p.L = mk3(0.0f, 0.0f, 0.0f);
@@ -595,29 +617,35 @@ VT_D void path_start(const Frame& F, const JobDev& J, Path& p, Dda& s, int px, i
   p.has_cont = 0;
   p.light = -1;
   p.bsdf_pdf = 0.0f;
+  p.nee_T = mk3(0.0f, 0.0f, 0.0f);
+  p.nee_C = mk3(0.0f, 0.0f, 0.0f);
   v3 o, d;
   generate_ray(F, J, mk3((float)px + 0.5f, (float)py + 0.5f, F.frag_z), p.rng, o, d);
   p.ro = o;
   p.rd = d;
+  p.sd = d;
   const float t = ray_aabb(o, d, ld3(F.bmin), ld3(F.bmax));
   if (t < 0.0f) {
     p.L = background(F, J, d, cnt);
-    p.phase = PH_DONE;
-    return;
+    return false;
   }
   cnt.add(C_SEGMENTS, 1);
-  dda_begin(F, s, o + t * d, d);
-  p.phase = PH_EXT;
+  return true;
+}
+// Volume entry point of the primary ray (pathTracer.fs:196).
+VT_D v3 primary_origin(v3 o, v3 d, v3 bmin, v3 bmax) {
+  const float t = ray_aabb(o, d, bmin, bmax);
+  return o + t * d;
 }
 
 // directLighting (pathTracer.fs:64-170) up to the shadow ray: picks a light,
-// evaluates the BSDF and MIS weight for it and leaves the shadow segment set
-// up.  The BSDF evaluation does not depend on visibility, so it is done
+// evaluates the BSDF and MIS weight for it and leaves the shadow direction in
+// p.sd.  The BSDF evaluation does not depend on visibility, so it is done
 // before the shadow ray; the contribution is added only if the segment
-// confirms visibility (see path_event).
+// confirms visibility (shadow_end).
 template <bool kCount>
 VT_D void light_sample(const Frame& F, const JobDev& J, Path& p, const Basis& b, const Mat& m, v3 wo,
-                       Dda& s, Cnt<kCount>& cnt) {
+                       Cnt<kCount>& cnt) {
   const float4 u = rng_next(F, J, p.rng);
   const int num_lights = F.n_emissive + 1;
   const int li = (int)(u.x * (float)num_lights);
@@ -659,41 +687,35 @@ VT_D void light_sample(const Frame& F, const JobDev& J, Path& p, const Basis& b,
   if (!(F.quirks & Q_UNGUARDED) && !(pdf > 0.0f && pdf < __int_as_float(0x7f800000)))
     p.nee_C = mk3(0.0f, 0.0f, 0.0f);
   p.nee_T = p.T;
+  p.sd = dir;
   cnt.add(C_SEGMENTS, 1);
-  dda_begin(F, s, b.position, dir);
 }
 
-// Segment-end event: the body of the bounce loop (pathTracer.fs:214-292) cut
-// at its two traversals.  After an extension segment: miss -> environment
-// (with MIS unless primary), hit -> shade the vertex and start the shadow
-// segment.  After a shadow segment: add the light sample if visible, then
-// start the continuation segment.
-template <bool kCount>
-VT_D void path_event(const Frame& F, const JobDev& J, Path& p, Dda& s, Cnt<kCount>& cnt) {
-  const bool hit = dda_hit(F, s);
-  if (p.phase == PH_SHADOW) {
-    bool visible;
-    if (p.light >= 0) {
-      const int dz = F.res[0] * F.res[1], dy = F.res[0];
-      const int ez = p.light / dz;
-      const int r1 = p.light - ez * dz;
-      const int ey = r1 / dy;
-      const int ex = r1 - ey * dy;
-      visible = hit && s.x == ex && s.y == ey && s.z == ez;
-    } else {
-      visible = !hit;
-    }
-    const v3 c = visible ? p.nee_C : mk3(0.0f, 0.0f, 0.0f);
-    p.L = p.L + p.nee_T * c;
-    if (!p.has_cont) { p.phase = PH_DONE; return; }
-    p.rd = p.cont_d;
-    p.primary = 0;
-    p.phase = PH_EXT;
-    cnt.add(C_SEGMENTS, 1);
-    dda_begin(F, s, p.ro, p.rd);
-    return;
+// End of a shadow segment (pathTracer.fs:133-153, 248-251).
+VT_D void shadow_end(const Frame& F, Path& p, SegEnd e) {
+  const bool hit = seg_hit(F.quirks, e.state, e.y);
+  bool visible;
+  if (p.light >= 0) {
+    const int dz = F.res[0] * F.res[1], dy = F.res[0];
+    const int ez = p.light / dz;
+    const int r1 = p.light - ez * dz;
+    const int ey = r1 / dy;
+    const int ex = r1 - ey * dy;
+    visible = hit && e.x == ex && e.y == ey && e.z == ez;
+  } else {
+    visible = !hit;
   }
-  // extension segment ended
+  const v3 c = visible ? p.nee_C : mk3(0.0f, 0.0f, 0.0f);
+  p.L = p.L + p.nee_T * c;
+}
+
+// End of an extension segment: the body of the bounce loop
+// (pathTracer.fs:202-292).  Returns false when the path ends here; true when
+// it leaves a shadow segment (ro, sd) and, if p.has_cont, a continuation
+// segment (ro, rd).
+template <bool kCount>
+VT_D bool ext_end(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount>& cnt) {
+  const bool hit = seg_hit(F.quirks, e.state, e.y);
   if (!hit) {
     if (p.primary) {
       p.L = background(F, J, p.rd, cnt);                          // :202-208
@@ -703,30 +725,27 @@ VT_D void path_event(const Frame& F, const JobDev& J, Path& p, Dda& s, Cnt<kCoun
       const float mis = power_heuristic(p.bsdf_pdf, lpdf);
       p.L = p.L + (p.T * Le) * mis;
     }
-    p.phase = PH_DONE;
-    return;
+    return false;
   }
   if (!p.primary) p.bounces += 1;                                 // :291
-  if (p.bounces >= F.max_bounces) { p.phase = PH_DONE; return; }  // :214
-  const Basis b = voxel_basis(F, s.x, s.y, s.z, p.ro, p.rd);      // :220-223
-  const Mat m = voxel_mat(F, J, s.x, s.y, s.z, cnt);              // :225-226
-  if (F.sel_enabled && s.x == F.sel[0] && s.y == F.sel[1] && s.z == F.sel[2]) {
+  if (p.bounces >= F.max_bounces) return false;                   // :214
+  const Basis b = voxel_basis(F, e.x, e.y, e.z, p.ro, p.rd);      // :220-223
+  const Mat m = voxel_mat(F, J, e.x, e.y, e.z, cnt);              // :225-226
+  if (F.sel_enabled && e.x == F.sel[0] && e.y == F.sel[1] && e.z == F.sel[2]) {
     p.L = p.L + mk3(1.0f, 0.0f, 0.0f);                            // :228-233
-    p.phase = PH_DONE;
-    return;
+    return false;
   }
   const v3 wo = -p.rd;
   const v3 lwo = world_to_local(wo, b);
   if (p.bounces == 0) p.L = p.L + p.T * m.emission;               // :241-245
-  const int hx = s.x, hy = s.y, hz = s.z;
-  light_sample(F, J, p, b, m, wo, s, cnt);                        // :248-251
+  light_sample(F, J, p, b, m, wo, cnt);                           // :248-251
   FPdf bs;
   float u_rr;
   v3 lwi = sample_bsdf<kCount>(F, J, m, lwo, p.rng, bs, u_rr);    // :254-258
   if (F.wire_opacity > 0.0f) {                                    // :260-270
     const v3 res = mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
     const v3 vc = ((b.position - ld3(F.bmin)) / (ld3(F.bmax) - ld3(F.bmin))) * res;
-    const v3 uvw = mk3((float)hx, (float)hy, (float)hz) - vc;
+    const v3 uvw = mk3((float)e.x, (float)e.y, (float)e.z) - vc;
     const v3 nyzx = mk3(b.normal.y, b.normal.z, b.normal.x);
     const v3 nzxy = mk3(b.normal.z, b.normal.x, b.normal.y);
     const float ux = fabsf(dot(nyzx, uvw)), uy = fabsf(dot(nzxy, uvw));
@@ -752,35 +771,42 @@ VT_D void path_event(const Frame& F, const JobDev& J, Path& p, Dda& s, Cnt<kCoun
     if (!(u_rr < q)) p.has_cont = 0;
     else p.T = p.T / q;
   }
+  if (p.has_cont) cnt.add(C_SEGMENTS, 1);
   p.ro = b.position;                                              // :278-279
-  p.cont_d = wwi;
+  p.rd = wwi;
   p.bsdf_pdf = bs.pdf;
-  p.phase = PH_SHADOW;
+  p.primary = 0;
+  return true;
 }
 
-// One complete sample, run to the end by a single lane.
+// One complete sample, run to the end by a single lane (megakernel form).
 template <bool kCount>
 VT_D float4 trace_sample(const Frame& F, const JobDev& J, int px, int py, int sample, Cnt<kCount>& cnt,
                          HitRecord* first_hit) {
+  const Grid g = grid_of(F, J);
   Path p;
   Dda s;
-  path_start(F, J, p, s, px, py, sample, cnt);
-  bool first = true;
   if (first_hit) { first_hit->x = -1; first_hit->y = -1; first_hit->z = -1; first_hit->flags = 0; }
-  while (p.phase != PH_DONE) {
-    if (s.state == DDA_RUNNING) dda_advance(F, J, s, 0x7fffffff, cnt);
-    if (first && first_hit) {
-      first = false;
-      const bool h = dda_hit(F, s);
-      first_hit->x = s.x; first_hit->y = s.y; first_hit->z = s.z;
-      int flags = (h ? 1 : 0) << 8 | ((h && s.state != DDA_HIT) ? 1 : 0) << 9;
-      if (h) {
-        const Basis b = voxel_basis(F, s.x, s.y, s.z, p.ro, p.rd);
-        flags |= ((int)b.normal.x + 1) | (((int)b.normal.y + 1) << 2) | (((int)b.normal.z + 1) << 4);
-      }
-      first_hit->flags = flags;
+  if (!path_start(F, J, p, px, py, sample, cnt)) return path_output(F, p);
+  dda_begin(g, s, primary_origin(p.ro, p.rd, ld3(F.bmin), ld3(F.bmax)), p.rd);
+  if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
+  if (first_hit) {
+    const bool h = dda_hit(F, s);
+    first_hit->x = s.x; first_hit->y = s.y; first_hit->z = s.z;
+    int flags = (h ? 1 : 0) << 8 | ((h && s.state != DDA_HIT) ? 1 : 0) << 9;
+    if (h) {
+      const Basis b = voxel_basis(F, s.x, s.y, s.z, p.ro, p.rd);
+      flags |= ((int)b.normal.x + 1) | (((int)b.normal.y + 1) << 2) | (((int)b.normal.z + 1) << 4);
     }
-    path_event(F, J, p, s, cnt);
+    first_hit->flags = flags;
+  }
+  while (ext_end(F, J, p, seg_end(s), cnt)) {
+    dda_begin(g, s, p.ro, p.sd);
+    if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
+    shadow_end(F, p, seg_end(s));
+    if (!p.has_cont) break;
+    dda_begin(g, s, p.ro, p.rd);
+    if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
   }
   return path_output(F, p);
 }

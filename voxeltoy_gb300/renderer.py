@@ -73,6 +73,11 @@ class Context:
         L.call("vt_diag_stream", self.h, C.byref(st))
         return st.value or 0
 
+    def launch_count(self) -> int:
+        n = C.c_uint64()
+        L.call("vt_diag_launch_count", self.h, C.byref(n))
+        return n.value
+
     def set_kernel(self, kernel: int):
         L.call("vt_diag_set_kernel", self.h, kernel)
 
@@ -97,11 +102,11 @@ class Context:
         L.call("vt_diag_get_noise_table", self.h, L.ptr(out), out.nbytes)
         return out
 
-    def render_batch(self, jobs: Sequence["Job"], passes: int, tile_pixels: int = 0, kernel: int = 0,
+    def render_batch(self, jobs: Sequence["Job"], passes: int, path_slots: int = 0, kernel: int = 0,
                      blocks_per_sm: int = 0) -> list[int]:
         arr = (C.c_void_p * max(1, len(jobs)))(*[j.h.value for j in jobs])
         res = (C.c_int32 * max(1, len(jobs)))()
-        opts = L.BatchOpts(tile_pixels, blocks_per_sm, 0, kernel)
+        opts = L.BatchOpts(path_slots, blocks_per_sm, 0, kernel)
         L.call("vt_render_batch", self.h, arr, len(jobs), passes, C.byref(opts), res)
         return list(res)[: len(jobs)]
 
@@ -277,8 +282,8 @@ class Job:
 
 class Server:
     def __init__(self, ctx: Context, hbm_budget_bytes: int = 0, max_active_jobs: int = 64,
-                 passes_per_round: int = 4, tile_pixels: int = 0):
-        opts = L.ServerOpts(hbm_budget_bytes, max_active_jobs, passes_per_round, tile_pixels)
+                 passes_per_round: int = 4, path_slots: int = 0):
+        opts = L.ServerOpts(hbm_budget_bytes, max_active_jobs, passes_per_round, path_slots)
         h = C.c_void_p()
         L.call("vt_server_create", ctx.h, C.byref(opts), C.byref(h))
         self.h = h
