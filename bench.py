@@ -222,6 +222,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 persistent")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up and timed renders of the resident frame (for ncu captures)")
     args = ap.parse_args()
@@ -246,6 +247,13 @@ def main():
     env = Env(ctx, cfg.env_rgb)
     job = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
     paths = cfg.width * cfg.height * cfg.spp
+    tuning = {"path_slots": "default"}
+    if not args.no_tune and args.kernel == 2:
+        from voxeltoy_gb300 import autotune
+        best = autotune.tune(ctx, [job], passes=min(16, cfg.spp), use_cache=False)
+        tuning = {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps")}
+        for r in best.get("sweep", [])[:12]:
+            print("tune", json.dumps(r), file=sys.stderr)
     if args.profile:
         for k in range(args.warmup + args.steps):
             job.reset()
@@ -348,6 +356,7 @@ def main():
         "time_to_spp_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99))},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
+        "tuning": tuning,
     }
     job.close(); env.close(); scene.close(); ctx.close()
     if rank == 0:

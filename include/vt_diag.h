@@ -60,6 +60,15 @@ VT_API int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int32_t
                                      int32_t height, float* cdf_u, float* cdf_v,
                                      float* integral);
 
+/* Tuning of the wavefront form (path_slots, trace_steps and max_items <= 0
+ * and trace_blocks_per_sm < 0 keep their value):
+ * path_slots paths in flight per launch (default 2M), trace_blocks_per_sm
+ * resident blocks of the DDA kernel (0: occupancy limit, the default),
+ * trace_steps DDA steps between ray-pool refills (8, 16 or 32; default 16),
+ * max_items samples per launch (sample-buffer entries, default 2^28). */
+VT_API int vt_diag_set_tuning(vt_context* ctx, int64_t path_slots, int32_t trace_blocks_per_sm,
+                              int32_t trace_steps, int64_t max_items);
+
 /* Number of rendering kernels (plain, wavefront shade/trace/accumulate) the
  * context has launched so far. */
 VT_API int vt_diag_launch_count(const vt_context* ctx, uint64_t* launches);

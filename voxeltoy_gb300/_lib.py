@@ -159,6 +159,7 @@ SIGNATURES = {
     "vt_diag_env_texels": [P, P, C.c_size_t],
     "vt_diag_stream": [P, PP],
     "vt_diag_launch_count": [P, C.POINTER(C.c_uint64)],
+    "vt_diag_set_tuning": [P, C.c_int64, C.c_int32, C.c_int32, C.c_int64],
     "vt_diag_set_noise_table": [P, P, C.c_size_t],
     "vt_diag_get_noise_table": [P, P, C.c_size_t],
 }

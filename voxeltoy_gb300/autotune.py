@@ -1,0 +1,97 @@
+"""Autotuner of the wavefront renderer's launch parameters.
+
+Times short renders of the caller's own jobs over a grid of
+  path_slots            paths in flight per launch (state + queues per slot)
+  trace_blocks_per_sm   resident blocks of the DDA kernel
+  trace_steps           DDA steps between ray-pool refills
+and applies the fastest setting to the context.  Results are cached in a JSON
+file keyed by a workload class (log2 of the largest grid edge, log2 of the
+pixels per pass, number of jobs) so later runs with a similar workload skip
+the sweep.
+"""
+from __future__ import annotations
+
+import itertools
+import json
+import math
+import os
+import time
+from pathlib import Path
+
+DEFAULT_GRID = {
+    "path_slots": [1 << 20, 1 << 21, 1 << 22],
+    "trace_blocks_per_sm": [0, 3],
+    "trace_steps": [8, 16, 32],
+}
+
+
+def cache_path() -> Path:
+    base = os.environ.get("VOXELTOY_TUNE_CACHE")
+    if base:
+        return Path(base)
+    return Path.home() / ".cache" / "voxeltoy_gb300" / "tune.json"
+
+
+def workload_key(jobs) -> str:
+    edge = max(max(j.scene.info().resolution) for j in jobs)
+    pixels = sum(j.width * j.height for j in jobs)
+    return f"edge{int(round(math.log2(max(edge, 1))))}_px{int(round(math.log2(max(pixels, 1))))}_jobs{len(jobs)}"
+
+
+def _time_render(ctx, jobs, passes: int, repeats: int) -> float:
+    best = float("inf")
+    for _ in range(repeats):
+        for j in jobs:
+            j.reset()
+        for j in jobs:
+            j.synchronize()
+        t0 = time.perf_counter()
+        if len(jobs) == 1:
+            jobs[0].render(passes)
+        else:
+            ctx.render_batch(jobs, passes)
+        for j in jobs:
+            j.synchronize()
+        best = min(best, time.perf_counter() - t0)
+    return best
+
+
+def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None, use_cache: bool = True) -> dict:
+    """Sweep the grid on `passes` samples per pixel of `jobs`, apply and return
+    the best setting ({"path_slots", "trace_blocks_per_sm", "trace_steps",
+    "seconds", "key", "cached"})."""
+    key = workload_key(jobs)
+    path = cache_path()
+    cache = {}
+    if use_cache and path.exists():
+        try:
+            cache = json.loads(path.read_text())
+        except (OSError, ValueError):
+            cache = {}
+    if use_cache and key in cache:
+        best = dict(cache[key])
+        ctx.set_tuning(best["path_slots"], best["trace_blocks_per_sm"], best["trace_steps"])
+        best.update(key=key, cached=True)
+        return best
+    grid = grid or DEFAULT_GRID
+    results = []
+    for slots, bps, steps in itertools.product(grid["path_slots"], grid["trace_blocks_per_sm"], grid["trace_steps"]):
+        ctx.set_tuning(slots, bps, steps)
+        t = _time_render(ctx, jobs, passes, repeats)
+        results.append((t, slots, bps, steps))
+    results.sort()
+    t, slots, bps, steps = results[0]
+    ctx.set_tuning(slots, bps, steps)
+    best = {"path_slots": slots, "trace_blocks_per_sm": bps, "trace_steps": steps, "seconds": t}
+    for j in jobs:
+        j.reset()
+    if use_cache:
+        cache[key] = best
+        try:
+            path.parent.mkdir(parents=True, exist_ok=True)
+            path.write_text(json.dumps(cache, indent=1))
+        except OSError:
+            pass
+    best.update(key=key, cached=False, sweep=[{"seconds": r[0], "path_slots": r[1], "trace_blocks_per_sm": r[2],
+                                               "trace_steps": r[3]} for r in results])
+    return best

@@ -263,7 +263,7 @@ static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette
   VT_CUDA(cudaMemcpyAsync(s->palette, pal.data(), sizeof(uint4) * pal.size(), cudaMemcpyHostToDevice, ctx->stream),
           "palette upload");
   // bit-bricks
-  const int64_t nb = (int64_t)s->bdim[0] * s->bdim[1] * s->bdim[2];
+  const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
   rc = ctx->alloc((void**)&s->bricks, sizeof(unsigned long long) * nb);
   if (rc != VT_OK) return rc;
   VT_CUDA(launch_build_bricks(s->grid, s->res[0], s->res[1], s->res[2], s->bricks, s->bdim[0], s->bdim[1],
@@ -1069,7 +1069,7 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     ctx->release(ctx->wf_mem);
     ctx->wf_mem = nullptr;
     ctx->wf_slots = 0;
-    const size_t bytes = (size_t)slots * (7 * sizeof(float4) + sizeof(uint32_t) + 2 * sizeof(int4) + 4 * sizeof(uint32_t));
+    const size_t bytes = (size_t)slots * (6 * sizeof(float4) + sizeof(uint32_t) + 2 * sizeof(int4) + 4 * sizeof(uint32_t));
     int rc = ctx->alloc(&ctx->wf_mem, bytes);
     if (rc != VT_OK) return rc;
     ctx->wf_slots = slots;
@@ -1099,8 +1099,7 @@ static WfSlots wf_slots_view(vt_context* ctx) {
   WfSlots st;
   float4* f = (float4*)b;
   st.a0 = f; st.a1 = f + S; st.a2 = f + 2 * S; st.a3 = f + 3 * S; st.a4 = f + 4 * S; st.a5 = f + 5 * S;
-  st.a6 = f + 6 * S;
-  st.hits = (int4*)(f + 7 * S);
+  st.hits = (int4*)(f + 6 * S);
   st.flags = (uint32_t*)(st.hits + 2 * S);
   return st;
 }
@@ -1149,14 +1148,15 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   P.counters = count ? ctx->d_counters : nullptr;
   VT_CUDA(cudaMemsetAsync(P.st.flags, 0, sizeof(uint32_t) * (size_t)slots, st), "slot flags");
   VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, 64, st), "wavefront control");
-  if (ctx->trace_blocks_per_sm <= 0) ctx->trace_blocks_per_sm = std::max(1, wf_trace_blocks_per_sm());
-  const int bps = blocks_per_sm > 0 ? blocks_per_sm : ctx->trace_blocks_per_sm;
+  if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
+  const int bps = blocks_per_sm > 0 ? blocks_per_sm
+                                    : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
   const int trace_blocks = ctx->sm_count * bps;
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
     VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + 4 * par, 0, 3 * sizeof(uint32_t), st), "round counters");
     VT_CUDA(launch_wf_shade(P, par, count, st), "wavefront shade");
-    VT_CUDA(launch_wf_trace(P, par, trace_blocks, count, st), "wavefront trace");
+    VT_CUDA(launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st), "wavefront trace");
     ctx->launches += 2;
     if ((iter & 7) == 7) {
       VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + 4 * par + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
@@ -1204,12 +1204,12 @@ int vt::render_wavefront(vt_context* ctx, vt_job* const* jobs, int32_t n, const 
       memset(&g, 0, sizeof(g));
       const Frame& F = jobs[i]->frame;
       g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
-      g.bx = F.bdim[0]; g.bxy = F.bdim[0] * F.bdim[1];
+      g.bx = F.bdim[0] + 2; g.bxy = (F.bdim[0] + 2) * (F.bdim[1] + 2);
       g.max_steps = F.max_steps;
       g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
       g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
       g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
-      g.bricks = jobs[i]->dev.bricks;
+      g.bricks = jobs[i]->dev.bricks + 1 + g.bx + g.bxy;
       grids.push_back(g);
       done[i] += p;
     }
@@ -1416,6 +1416,16 @@ extern "C" int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int
   VT_CUDA(cudaMemcpyAsync(&iv, d_int, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "cdf");
   VT_CUDA(cudaStreamSynchronize(ctx->stream), "cdf");
   if (integral) *integral = iv;
+  return VT_OK;
+}
+
+extern "C" int vt_diag_set_tuning(vt_context* ctx, int64_t slots, int32_t blocks_per_sm, int32_t steps,
+                                  int64_t max_items) {
+  VT_CHECK_ARG(ctx, "context is null");
+  if (slots > 0) ctx->max_slots = std::max<int64_t>(32, std::min<int64_t>(slots, (int64_t)1 << 26));
+  if (blocks_per_sm >= 0) ctx->trace_blocks_per_sm = blocks_per_sm;
+  if (steps > 0) ctx->trace_steps = steps <= 8 ? 8 : (steps <= 16 ? 16 : 32);
+  if (max_items > 0) ctx->max_items = std::max<int64_t>(1024, max_items);
   return VT_OK;
 }
 

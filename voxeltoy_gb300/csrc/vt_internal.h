@@ -3,9 +3,12 @@
 // Device-memory layout of one scene (all resident in HBM):
 //   grid     uint8[rx*ry*rz]        palette entry + 1 per voxel, 0 = empty,
 //                                   linear index x + y*rx + z*rx*ry
-//   bricks   uint64[bx*by*bz]       occupancy bit-bricks: one 64-bit word per
-//                                   4x4x4 voxel block, bit (x&3)|(y&3)<<2|(z&3)<<4,
-//                                   brick index (x>>2) + bx*((y>>2) + by*(z>>2))
+//   bricks   uint64[(bx+2)*(by+2)*(bz+2)]  occupancy bit-bricks: one 64-bit word
+//                                   per 4x4x4 voxel block, bit (x&3)|(y&3)<<2|(z&3)<<4,
+//                                   bx = ceil(rx/4) ...; a border of one brick on
+//                                   every side has all bits set, as do voxels of
+//                                   the last bricks beyond the volume, so that a
+//                                   ray leaving the volume stops on a set bit
 //   palette  uint4[n_palette]       one 16-byte record per material: eight IEEE
 //                                   halves {type, emission rgb, albedo rgb, roughness}
 //   emissive int32[n_emissive]      linear voxel indices sampled by NEE
@@ -72,13 +75,13 @@ struct Frame {
 // What the DDA needs of a volume: extents, bounds, brick layout, step cap.
 struct Grid {
   int32_t rx, ry, rz;
-  int32_t bx, bxy;           // brick-grid row and slice strides
+  int32_t bx, bxy;           // padded brick-grid row and slice strides
   int32_t max_steps;         // int(2*ceil(length(vec3(res)))), dda.h:98
   float bminx, bminy, bminz;
   float vextx, vexty, vextz; // 1/(bmax-bmin), dda.h:16
   float bmaxx, bmaxy, bmaxz;
   int32_t pad;
-  const unsigned long long* bricks;
+  const unsigned long long* bricks;   // brick (0,0,0) of the padded array
 };
 
 // Device pointers of everything one job reads and writes.

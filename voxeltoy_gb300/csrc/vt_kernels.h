@@ -26,13 +26,12 @@ cudaError_t launch_diag(const Frame& F, const JobDev& J, int sample, float4* out
                         unsigned long long* counters, cudaStream_t st);
 // Wavefront path state, structure of arrays over the path slots.
 struct WfSlots {
-  float4* a0;      // ro.xyz, bsdf_pdf
-  float4* a1;      // rd.xyz, light (int bits)
-  float4* a2;      // sd.xyz, rng state (uint bits)
-  float4* a3;      // L.xyz, sample (uint bits)
-  float4* a4;      // T.xyz, pixel (uint bits)
-  float4* a5;      // nee_T.xyz, job (uint bits)
-  float4* a6;      // nee_C.xyz, item (uint bits)
+  float4* a0;      // ro.xyz, job (uint bits)
+  float4* a1;      // rd.xyz, item (uint bits)
+  float4* a2;      // sd.xyz, light (int bits)
+  float4* a3;      // L.xyz, rng state (uint bits)
+  float4* a4;      // T.xyz, bsdf_pdf
+  float4* a5;      // nee_P.xyz, unused
   uint32_t* flags; // bounces | primary | has_cont | ext | shadow | active | dead
   int4* hits;      // [2][n_slots] segment ends: extension, shadow
 };
@@ -52,7 +51,7 @@ struct WfParams {
   unsigned long long* counters;    // nullable
 };
 cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st);
-cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, bool count, cudaStream_t st);
+cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st);
 cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max_pixels, const float4* sbuf,
                                  cudaStream_t st);
 int wf_trace_blocks_per_sm();

@@ -96,6 +96,7 @@ enum : uint32_t {
   SL_SHADOW = 1u << 11,   // a shadow segment was traced for this slot
   SL_ACTIVE = 1u << 12,
   SL_DEAD = 1u << 13,     // no work left for this slot in this launch
+  // bits 14..16: non-finite throughput components of the pending light sample
 };
 
 __device__ __forceinline__ v3 xyz4(float4 v) { return mk3(v.x, v.y, v.z); }
@@ -111,36 +112,41 @@ __device__ __forceinline__ int job_of(const JobEntry* jobs, int n_jobs, unsigned
   return lo;
 }
 
-__device__ __forceinline__ void load_path(const WfSlots& st, int slot, uint32_t fl, const Frame& F, Path& p) {
+// Slot state layout: a0 = (ro, job), a1 = (rd, item), a2 = (sd, light),
+// a3 = (L, rng), a4 = (T, bsdf_pdf), a5 = (nee_P, -); pixel and sample are
+// derived from the item; bounces and flag bits live in `flags`.
+__device__ __forceinline__ void load_path(const WfSlots& st, int slot, uint32_t fl, const JobEntry& E, uint32_t item,
+                                          Path& p) {
   const float4 a0 = st.a0[slot], a1 = st.a1[slot], a2 = st.a2[slot];
-  const float4 a3 = st.a3[slot], a4 = st.a4[slot], a5 = st.a5[slot], a6 = st.a6[slot];
-  p.ro = xyz4(a0); p.bsdf_pdf = a0.w;
-  p.rd = xyz4(a1); p.light = __float_as_int(a1.w);
-  p.sd = xyz4(a2);
+  const float4 a3 = st.a3[slot], a4 = st.a4[slot], a5 = st.a5[slot];
+  p.ro = xyz4(a0);
+  p.rd = xyz4(a1);
+  p.sd = xyz4(a2); p.light = __float_as_int(a2.w);
   p.L = xyz4(a3);
-  p.T = xyz4(a4);
-  p.nee_T = xyz4(a5);
-  p.nee_C = xyz4(a6);
+  p.T = xyz4(a4); p.bsdf_pdf = a4.w;
+  p.nee_P = xyz4(a5);
   p.bounces = (int)(fl & SL_BOUNCES);
   p.primary = (fl & SL_PRIMARY) ? 1 : 0;
   p.has_cont = (fl & SL_HAS_CONT) ? 1 : 0;
-  const uint32_t rng = __float_as_uint(a2.w);
-  p.rng.pixel = __float_as_uint(a4.w);
-  p.rng.sample = __float_as_uint(a3.w);
-  if (F.rng_mode == 1) { p.rng.ox = (int32_t)(rng & 0xffffu); p.rng.oy = (int32_t)(rng >> 16); p.rng.call = 0; }
+  p.nee_nf = (int)((fl >> 14) & 7u);
+  const long long r = (long long)item - E.tile_begin;
+  const long long pass = r / E.n_pixels;
+  const uint32_t rng = __float_as_uint(a3.w);
+  p.rng.pixel = (uint32_t)(r - pass * E.n_pixels);
+  p.rng.sample = (uint32_t)(E.sample_base + pass);
+  if (E.F.rng_mode == 1) { p.rng.ox = (int32_t)(rng & 0xffffu); p.rng.oy = (int32_t)(rng >> 16); p.rng.call = 0; }
   else { p.rng.call = rng; p.rng.ox = p.rng.oy = 0; }
 }
 
 __device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Frame& F, const Path& p, uint32_t job,
                                            uint32_t item) {
   const uint32_t rng = (F.rng_mode == 1) ? ((uint32_t)p.rng.ox | ((uint32_t)p.rng.oy << 16)) : p.rng.call;
-  st.a0[slot] = pack4(p.ro, p.bsdf_pdf);
-  st.a1[slot] = pack4(p.rd, __int_as_float(p.light));
-  st.a2[slot] = pack4(p.sd, __uint_as_float(rng));
-  st.a3[slot] = pack4(p.L, __uint_as_float(p.rng.sample));
-  st.a4[slot] = pack4(p.T, __uint_as_float(p.rng.pixel));
-  st.a5[slot] = pack4(p.nee_T, __uint_as_float(job));
-  st.a6[slot] = pack4(p.nee_C, __uint_as_float(item));
+  st.a0[slot] = pack4(p.ro, __uint_as_float(job));
+  st.a1[slot] = pack4(p.rd, __uint_as_float(item));
+  st.a2[slot] = pack4(p.sd, __int_as_float(p.light));
+  st.a3[slot] = pack4(p.L, __uint_as_float(rng));
+  st.a4[slot] = pack4(p.T, p.bsdf_pdf);
+  st.a5[slot] = pack4(p.nee_P, 0.0f);
 }
 
 // One round of shading: consume the segment results of the previous trace,
@@ -163,11 +169,10 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
   uint32_t job = 0, item = 0;
   uint32_t emit = 0;   // 1: extension, 2: shadow
   if (active) {
-    const float4 a5 = P.st.a5[slot], a6 = P.st.a6[slot];
-    job = __float_as_uint(a5.w);
-    item = __float_as_uint(a6.w);
+    job = __float_as_uint(P.st.a0[slot].w);
+    item = __float_as_uint(P.st.a1[slot].w);
     const JobEntry& E = P.jobs[job];
-    load_path(P.st, slot, fl, E.F, p);
+    load_path(P.st, slot, fl, E, item, p);
     if (fl & SL_SHADOW) {
       const int4 h = P.st.hits[(size_t)P.n_slots + slot];
       SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
@@ -239,7 +244,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
       const JobEntry& E = P.jobs[job];
       store_path(P.st, slot, E.F, p, job, item);
       nf = SL_ACTIVE | (uint32_t)(p.bounces & 0xff) | (p.primary ? SL_PRIMARY : 0u) |
-           (p.has_cont ? SL_HAS_CONT : 0u) | ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u);
+           (p.has_cont ? SL_HAS_CONT : 0u) | ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u) |
+           ((uint32_t)(p.nee_nf & 7) << 14);
     } else {
       nf = dead ? SL_DEAD : 0u;
     }
@@ -255,9 +261,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
 // lanes as they finish their previous segment, so lanes stay busy until the
 // queue is drained.
 constexpr uint32_t kTraceChunk = 128;
-constexpr int kTraceSteps = 8;
 
-template <bool kCount>
+template <bool kCount, int kTraceSteps>
 __global__ void __launch_bounds__(256) k_wf_trace(const WfParams P, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -289,9 +294,8 @@ __global__ void __launch_bounds__(256) k_wf_trace(const WfParams P, int par) {
       if (!have && r < avail) {
         entry = __ldg(&q[pool + r]);
         const int slot = (int)(entry >> 2);
-        const uint32_t job = __float_as_uint(__ldg(&P.st.a5[slot].w));
-        g = P.grids[job];
         const float4 a0 = __ldg(&P.st.a0[slot]);
+        g = P.grids[__float_as_uint(a0.w)];
         const float4 ad = (entry & 1u) ? __ldg(&P.st.a2[slot]) : __ldg(&P.st.a1[slot]);
         v3 o = xyz4(a0);
         const v3 d = xyz4(ad);
@@ -338,9 +342,11 @@ cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, bool count, cudaStream_t st) {
-  if (count) k_wf_trace<true><<<blocks, 256, 0, st>>>(P, par);
-  else k_wf_trace<false><<<blocks, 256, 0, st>>>(P, par);
+cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st) {
+  if (count) k_wf_trace<true, 16><<<blocks, 256, 0, st>>>(P, par);
+  else if (steps <= 8) k_wf_trace<false, 8><<<blocks, 256, 0, st>>>(P, par);
+  else if (steps <= 16) k_wf_trace<false, 16><<<blocks, 256, 0, st>>>(P, par);
+  else k_wf_trace<false, 32><<<blocks, 256, 0, st>>>(P, par);
   return cudaGetLastError();
 }
 
@@ -354,7 +360,7 @@ cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max
 
 int wf_trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8>, 256, 0);
   return n;
 }
 

@@ -36,9 +36,11 @@ struct vt_context {
   int64_t sbuf_items = 0;
   uint32_t* wf_ctl = nullptr;    // [2][4] qcount, qhead, live, pad + next_item
   uint32_t* h_live = nullptr;    // pinned host copy of a live counter
-  int64_t max_slots = 1 << 20;   // path slots per launch
+  int64_t max_slots = 1 << 21;   // path slots per launch
   int64_t max_items = 1 << 28;   // samples per launch (sample buffer entries)
   int trace_blocks_per_sm = 0;   // 0 = occupancy limit
+  int trace_occupancy = 0;       // occupancy limit of the DDA kernel (cached)
+  int trace_steps = 16;          // DDA steps between refills of the trace kernel
   uint64_t launches = 0;         // render kernels launched by this context
   unsigned long long* d_counters = nullptr;
   unsigned long long* d_queue = nullptr;

@@ -9,27 +9,27 @@
 namespace vt {
 
 // ------------------------------------------------------------- bit-bricks
-// One thread per 4x4x4 brick gathers its 64 voxels into one word.
+// One thread per brick of the padded brick grid (one border brick on every
+// side).  Voxels outside the volume read as occupied, so the DDA stops on
+// the first voxel beyond the volume without a separate bounds test.
 __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int32_t ry, int32_t rz,
                                unsigned long long* __restrict__ bricks, int32_t bx, int32_t by, int32_t bz) {
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t nb = (int64_t)bx * by * bz;
-  if (b >= nb) return;
-  const int x0 = (int)(b % bx) * 4;
-  const int y0 = (int)((b / bx) % by) * 4;
-  const int z0 = (int)(b / ((int64_t)bx * by)) * 4;
+  const int64_t px = bx + 2, py = by + 2, pz = bz + 2;
+  if (b >= px * py * pz) return;
+  const int x0 = ((int)(b % px) - 1) * 4;
+  const int y0 = ((int)((b / px) % py) - 1) * 4;
+  const int z0 = ((int)(b / (px * py)) - 1) * 4;
   unsigned long long w = 0ull;
   for (int dz = 0; dz < 4; ++dz) {
     const int z = z0 + dz;
-    if (z >= rz) break;
     for (int dy = 0; dy < 4; ++dy) {
       const int y = y0 + dy;
-      if (y >= ry) break;
-      const size_t row = (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z);
       for (int dx = 0; dx < 4; ++dx) {
         const int x = x0 + dx;
-        if (x >= rx) break;
-        if (grid[row + x] != 0) w |= 1ull << (dx | (dy << 2) | (dz << 4));
+        const bool outside = x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz;
+        const bool set = outside || grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)] != 0;
+        if (set) w |= 1ull << (dx | (dy << 2) | (dz << 4));
       }
     }
   }
@@ -39,8 +39,7 @@ __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int
 cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
                                 unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
                                 cudaStream_t st) {
-  const int64_t nb = (int64_t)bx * by * bz;
-  if (nb <= 0) return cudaSuccess;
+  const int64_t nb = (int64_t)(bx + 2) * (by + 2) * (bz + 2);
   k_build_bricks<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(grid, rx, ry, rz, bricks, bx, by, bz);
   return cudaGetLastError();
 }

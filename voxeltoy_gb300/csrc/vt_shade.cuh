@@ -211,12 +211,12 @@ VT_D v3 world_to_local(v3 w, const Basis& b) {
 VT_D Grid grid_of(const Frame& F, const JobDev& J) {
   Grid g;
   g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
-  g.bx = F.bdim[0]; g.bxy = F.bdim[0] * F.bdim[1];
+  g.bx = F.bdim[0] + 2; g.bxy = (F.bdim[0] + 2) * (F.bdim[1] + 2);
   g.max_steps = F.max_steps;
   g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
   g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
   g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
-  g.bricks = J.bricks;
+  g.bricks = J.bricks + 1 + g.bx + g.bxy;   // brick (0,0,0) inside the border
   return g;
 }
 
@@ -263,29 +263,39 @@ VT_D void dda_begin(const Grid& g, Dda& s, v3 o, v3 d) {
 
 // DDA loop (dda.h:38-57): at most `budget` iterations of
 // bounds test -> occupancy test -> advance every minimal axis.
+// The brick grid carries a one-brick border whose voxels are all set, so the
+// bounds test folds into the occupancy test: a set bit outside [0, res) is
+// the exit the reference detects at the top of its loop, with the same
+// voxel position.  `bricks` points at brick (0, 0, 0) of the padded array.
 template <bool kCount>
 VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt) {
   int x = s.x, y = s.y, z = s.z, steps = s.steps, cb = s.cb;
   float dx = s.dx, dy = s.dy, dz = s.dz;
   unsigned long long bits = s.bits;
   int state = DDA_RUNNING;
-  while (budget-- > 0) {
-    if (steps >= g.max_steps) { state = DDA_MISS; break; }
-    if ((unsigned)x >= (unsigned)g.rx || (unsigned)y >= (unsigned)g.ry || (unsigned)z >= (unsigned)g.rz) {
-      state = DDA_MISS; break;
-    }
-    cnt.add(C_DDA_CELLS, 1);
+  const int left = g.max_steps - steps;
+  if (budget > left) budget = left;
+  int k = 0;
+  for (; k < budget; ++k) {
     const int b = (x >> 2) + g.bx * (y >> 2) + g.bxy * (z >> 2);
     if (b != cb) { bits = __ldg(&g.bricks[b]); cb = b; }
-    if ((bits >> ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4))) & 1ull) { state = DDA_HIT; break; }
-    const bool mx = (dy >= dx) && (dz >= dx);
-    const bool my = (dx >= dy) && (dz >= dy);
-    const bool mz = (dy >= dz) && (dx >= dz);
+    if ((bits >> ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4))) & 1ull) {
+      const bool inside = (unsigned)x < (unsigned)g.rx && (unsigned)y < (unsigned)g.ry && (unsigned)z < (unsigned)g.rz;
+      if (inside) cnt.add(C_DDA_CELLS, 1);
+      state = inside ? DDA_HIT : DDA_MISS;
+      break;
+    }
+    cnt.add(C_DDA_CELLS, 1);
+    // step(dis.xyz, dis.yxy) * step(dis.xyz, dis.zzx): every axis whose
+    // distance equals the minimum (distances are never NaN)
+    const float m = fminf(dx, fminf(dy, dz));
+    const bool mx = dx == m, my = dy == m, mz = dz == m;
     if (mx) { dx = dx + s.ax; x += s.sx; }
     if (my) { dy = dy + s.ay; y += s.sy; }
     if (mz) { dz = dz + s.az; z += s.sz; }
-    ++steps;
   }
+  steps += k;
+  if (state == DDA_RUNNING && steps >= g.max_steps) state = DDA_MISS;   // step cap
   s.x = x; s.y = y; s.z = z; s.steps = steps; s.cb = cb; s.bits = bits;
   s.dx = dx; s.dy = dy; s.dz = dz;
   s.state = state;
@@ -584,8 +594,9 @@ struct Path {
   v3 ro;         // origin of the current extension ray (camera or last vertex)
   v3 rd;         // direction of the current extension ray
   v3 sd;         // direction of the pending shadow ray (origin ro)
-  v3 nee_T;      // throughput at the vertex of the pending light sample
-  v3 nee_C;      // directLighting value if the light is visible
+  v3 nee_P;      // throughput * directLighting value, added if the light is visible
+  int32_t nee_nf;// bit c set: throughput component c was not finite (then an
+                 // occluded light sample still turns L.c into NaN, as T * 0 does)
   int32_t light; // emissive voxel index of the light sample, -1 = environment
   float bsdf_pdf;
   int32_t bounces;
@@ -617,8 +628,8 @@ VT_D bool path_start(const Frame& F, const JobDev& J, Path& p, int px, int py, i
   p.has_cont = 0;
   p.light = -1;
   p.bsdf_pdf = 0.0f;
-  p.nee_T = mk3(0.0f, 0.0f, 0.0f);
-  p.nee_C = mk3(0.0f, 0.0f, 0.0f);
+  p.nee_P = mk3(0.0f, 0.0f, 0.0f);
+  p.nee_nf = 0;
   v3 o, d;
   generate_ray(F, J, mk3((float)px + 0.5f, (float)py + 0.5f, F.frag_z), p.rng, o, d);
   p.ro = o;
@@ -681,12 +692,14 @@ VT_D void light_sample(const Frame& F, const JobDev& J, Path& p, const Basis& b,
   const v3 lwi = world_to_local(dir, b);
   const FPdf bf = eval_bsdf(F, m, lwo, lwi);
   const float mis = power_heuristic(pdf, bf.pdf);
-  p.nee_C = (((bf.f * Ll) * fabsf(dot(dir, b.normal))) * mis) / pdf;
+  v3 C = (((bf.f * Ll) * fabsf(dot(dir, b.normal))) * mis) / pdf;
   // Without the unguarded-samples quirk a light sample with a zero, negative
   // or infinite pdf contributes nothing instead of dividing by it.
   if (!(F.quirks & Q_UNGUARDED) && !(pdf > 0.0f && pdf < __int_as_float(0x7f800000)))
-    p.nee_C = mk3(0.0f, 0.0f, 0.0f);
-  p.nee_T = p.T;
+    C = mk3(0.0f, 0.0f, 0.0f);
+  p.nee_P = p.T * C;
+  const float inf = __int_as_float(0x7f800000);
+  p.nee_nf = (fabsf(p.T.x) < inf ? 0 : 1) | (fabsf(p.T.y) < inf ? 0 : 2) | (fabsf(p.T.z) < inf ? 0 : 4);
   p.sd = dir;
   cnt.add(C_SEGMENTS, 1);
 }
@@ -705,8 +718,17 @@ VT_D void shadow_end(const Frame& F, Path& p, SegEnd e) {
   } else {
     visible = !hit;
   }
-  const v3 c = visible ? p.nee_C : mk3(0.0f, 0.0f, 0.0f);
-  p.L = p.L + p.nee_T * c;
+  // radiance += throughput * directLighting: the product was formed at the
+  // vertex; an occluded sample adds T * 0, which changes L only where T is
+  // not finite (L is never -0, so adding +-0 is exact otherwise)
+  if (visible) {
+    p.L = p.L + p.nee_P;
+  } else if (p.nee_nf) {
+    const float nan = __int_as_float(0x7fffffff);
+    if (p.nee_nf & 1) p.L.x = p.L.x + nan;
+    if (p.nee_nf & 2) p.L.y = p.L.y + nan;
+    if (p.nee_nf & 4) p.L.z = p.L.z + nan;
+  }
 }
 
 // End of an extension segment: the body of the bounce loop

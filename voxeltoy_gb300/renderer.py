@@ -73,6 +73,11 @@ class Context:
         L.call("vt_diag_stream", self.h, C.byref(st))
         return st.value or 0
 
+    def set_tuning(self, path_slots: int = 0, trace_blocks_per_sm: int = -1, trace_steps: int = 0,
+                   max_items: int = 0):
+        """Wavefront launch parameters; 0 (or -1 for trace_blocks_per_sm) keeps a value."""
+        L.call("vt_diag_set_tuning", self.h, path_slots, trace_blocks_per_sm, trace_steps, max_items)
+
     def launch_count(self) -> int:
         n = C.c_uint64()
         L.call("vt_diag_launch_count", self.h, C.byref(n))
