@@ -1,0 +1,202 @@
+"""C ABI behaviour on the GPU: budgets, validation, readback flags, the
+reference's offset/table upload, the Renderer mirror, server admission,
+cancellation and timeouts.  Failures are provoked on the host side (bad
+arguments, a small budget, a cancelled request); nothing faults the GPU."""
+import ctypes as C
+import math
+import os
+
+import numpy as np
+import pytest
+
+from helpers import close_all, gpu_setup, small_config1, small_config2
+from voxeltoy_gb300 import Context, Env, Job, Renderer, Scene, Server
+from voxeltoy_gb300 import _lib as L
+from voxeltoy_gb300 import scenes as S
+
+pytestmark = pytest.mark.gpu
+
+
+def test_budget_is_enforced_and_released():
+    with Context(0, hbm_budget_bytes=32 << 20) as ctx:
+        base = ctx.memory()
+        with pytest.raises(L.VtError) as e:
+            Scene.dense(ctx, np.zeros((320, 320, 320), np.uint8), [S.lambert(0.5)])
+        assert e.value.code == L.VT_EBUDGET
+        assert ctx.memory() == base
+        sc = Scene.dense(ctx, np.ones((64, 64, 64), np.uint8), [S.lambert(0.5)])
+        assert ctx.memory() > base
+        sc.close()
+        assert ctx.memory() == base
+
+
+def test_input_validation(ctx):
+    g = np.ones((8, 8, 8), np.uint8)
+    with pytest.raises(L.VtError) as e:
+        Scene.dense(ctx, g * 3, [S.lambert(0.5)])                       # entry 3 of a 1-entry palette
+    assert e.value.code == L.VT_EINVAL
+    with pytest.raises(L.VtError):
+        Scene.dense(ctx, g, [(5, (0, 0, 0), (1, 1, 1), 0.0)])            # unknown material type
+    with pytest.raises(L.VtError):
+        Scene.dense(ctx, g, [S.lambert(0.5)], emissive=np.array([512], np.int32))
+    bad = np.ones((4, 8, 3), np.float32)
+    bad[1, 2, 0] = np.nan
+    with pytest.raises(L.VtError):
+        Env(ctx, bad)
+    sc = Scene.dense(ctx, g, [S.lambert(0.5)])
+    try:
+        s = S.physical_settings(2)
+        s.ground_material = 4
+        with pytest.raises(L.VtError):
+            Job(ctx, sc, None, S.orbit_camera(), s, 8, 8)
+        s.ground_material = 0
+        s.max_bounces = -1
+        with pytest.raises(L.VtError):
+            Job(ctx, sc, None, S.orbit_camera(), s, 8, 8)
+    finally:
+        sc.close()
+    assert b"" != L.load().vt_last_error()
+
+
+def test_offsets_upload_matches_palette_upload(ctx):
+    """createVoxelDataTexture's layout: int32 record offsets and a float table."""
+    cfg = small_config1(edge=32, w=24, h=24)
+    # two records: Lambert at offset 0 (7 floats), metal at offset 7 (8 floats)
+    table = np.array([0, 0, 0, 0, 0.7, 0.6, 0.5,
+                      1, 0, 0, 0, 0.9, 0.8, 0.4, 0.3], np.float32)
+    rng = np.random.default_rng(1)
+    occ = cfg.voxels > 0
+    which = rng.integers(0, 2, size=cfg.voxels.shape)
+    offsets = np.where(occ, np.where(which == 0, 0, 7), -1).astype(np.int32)
+    dense = np.where(occ, which + 1, 0).astype(np.uint8)
+    palette = [S.lambert((0.7, 0.6, 0.5)), S.metal((0.9, 0.8, 0.4), 0.3)]
+    a = Scene.from_offsets(ctx, offsets, table)
+    b = Scene.dense(ctx, dense, palette)
+    try:
+        np.testing.assert_array_equal(a.voxels(), b.voxels())
+        ja = Job(ctx, a, None, cfg.camera, cfg.settings, 24, 24)
+        jb = Job(ctx, b, None, cfg.camera, cfg.settings, 24, 24)
+        ja.render(3); jb.render(3)
+        np.testing.assert_array_equal(ja.readback().view(np.uint32), jb.readback().view(np.uint32))
+        ja.close(); jb.close()
+    finally:
+        a.close(); b.close()
+    with pytest.raises(L.VtError):
+        Scene.from_offsets(ctx, np.where(occ, 100, -1).astype(np.int32), table)   # offset beyond the table
+    with pytest.raises(L.VtError):
+        Scene.from_offsets(ctx, np.where(occ, 11, -1).astype(np.int32), table)    # record cut off by the end
+
+
+def test_readback_flags(ctx, orc):
+    cfg = small_config1(edge=32, w=20, h=12)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        job.render(2)
+        lin = job.readback()
+        flip = job.readback(L.VT_READBACK_FLIP_Y)
+        np.testing.assert_array_equal(flip, lin[::-1])
+        tm = job.readback(L.VT_READBACK_TONEMAP)
+        want = orc.builtins(2, np.ascontiguousarray(lin[..., :3] * np.float32(1.0)),
+                            np.full(lin[..., :3].shape, np.float32(1.0) / np.float32(2.2), np.float32))
+        np.testing.assert_array_equal(tm[..., :3], want)
+        assert job.samples() == 2
+        job.reset()
+        assert job.samples() == 0
+    finally:
+        close_all(job, scene, env)
+
+
+def test_max_samples_finishes(ctx):
+    cfg = small_config1(edge=24, w=8, h=8)
+    cfg.settings.max_samples = 5
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        assert job.render(3) == L.VT_SAMPLES_PENDING
+        assert job.render(3) == L.VT_FINISHED_RENDERING
+        assert job.samples() == 5
+        assert job.render(1) == L.VT_FINISHED_RENDERING and job.samples() == 5
+    finally:
+        close_all(job, scene, env)
+
+
+def test_renderer_mirror(tmp_path):
+    r = Renderer()
+    r.initialize()
+    try:
+        cfg = S.config1(edge=32, width=32, height=24)
+        r.resize_frame(32, 24)
+        r.load_volume(cfg.voxels, cfg.palette)
+        cam = r.camera()
+        for f, _t in L.Camera._fields_:
+            v = getattr(cfg.camera, f)
+            if hasattr(v, "__len__"):
+                getattr(cam, f)[:] = list(v)
+            else:
+                setattr(cam, f, v)
+        r.update_camera()
+        r.render_settings().max_samples = 4
+        r.render_settings().max_bounces = 3
+        r.update_render_settings()
+        n = 0
+        while r.render() == 0:
+            n += 1
+        assert n == 3 and r.job.samples() == 4
+        img = r.image()
+        assert img.shape == (24, 32, 4) and np.isfinite(img).all()
+        out = tmp_path / "frame.pfm"
+        r.save_image(str(out))
+        data = out.read_bytes()
+        assert data.startswith(b"PF\n32 24\n-1.0\n") and len(data) == len(b"PF\n32 24\n-1.0\n") + 32 * 24 * 12
+        d, vox = r.pick_focal_distance(16.0, 12.0)
+        assert r.job.samples() == 0
+        assert (d < 99999999.0) == (vox[0] >= 0)
+        r.resize_frame(16, 16)
+        assert r.image().shape == (16, 16, 4)
+    finally:
+        r.close()
+
+
+def test_server_budget_cancel_and_timeout(ctx):
+    cfg = small_config1(edge=32, w=64, h=64)
+    scene = Scene.dense(ctx, cfg.voxels, cfg.palette)
+    srv = Server(ctx, hbm_budget_bytes=1 << 20, max_active_jobs=1, passes_per_round=1)
+    try:
+        big = srv.submit(scene, None, cfg.camera, cfg.settings, 1024, 1024, 4)   # 48 MiB of buffers > 1 MiB
+        assert srv.wait(big, 30.0) == L.VT_EBUDGET
+        assert srv.poll(big)[0] == L.VT_REQ_FAILED
+        long = srv.submit(scene, None, cfg.camera, cfg.settings, 64, 64, 1 << 20)
+        queued = srv.submit(scene, None, cfg.camera, cfg.settings, 64, 64, 4)
+        assert srv.wait(long, 0.05) == L.VT_ETIMEOUT
+        srv.cancel(queued)
+        srv.cancel(long)
+        assert srv.wait(queued, 30.0) == L.VT_ECANCELLED
+        assert srv.wait(long, 30.0) == L.VT_ECANCELLED
+        ok = srv.submit(scene, None, cfg.camera, cfg.settings, 16, 16, 3)
+        assert srv.wait(ok, 30.0) == L.VT_OK
+        img, secs = srv.result(ok, 16, 16)
+        assert np.isfinite(img).all() and secs > 0
+        st = srv.stats()
+        assert st.failed == 1 and st.cancelled == 2 and st.completed == 1
+    finally:
+        srv.close()
+        scene.close()
+
+
+def test_emissive_scene_renders_light(ctx):
+    """A single emissive voxel lights its neighbourhood only through NEE."""
+    g = np.zeros((16, 16, 16), np.uint8)
+    g[:2, :, :] = 1
+    g[5, 8, 8] = 2
+    pal = [S.lambert(0.8), S.lambert(0.5, emission=(20, 20, 20))]
+    sc = Scene.dense(ctx, g, pal, flags=L.VT_SCENE_AUTO_EMISSIVE | L.VT_SCENE_PRUNE_EMISSIVE)
+    try:
+        assert sc.emissive().tolist() == [8 + 16 * (8 + 16 * 5)]
+        s = S.physical_settings(2, top=(0, 0, 0), bottom=(0, 0, 0))
+        cam = S.orbit_camera(distance=1500, theta_deg=150, phi_deg=20)
+        job = Job(ctx, sc, None, cam, s, 32, 32)
+        job.render(32)
+        img = job.readback()
+        assert img[..., :3].max() > 1.0 and img[..., :3].min() == 0.0
+        job.close()
+    finally:
+        sc.close()
