@@ -1069,7 +1069,8 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     ctx->release(ctx->wf_mem);
     ctx->wf_mem = nullptr;
     ctx->wf_slots = 0;
-    const size_t bytes = (size_t)slots * (6 * sizeof(float4) + sizeof(uint32_t) + 2 * sizeof(int4) + 4 * sizeof(uint32_t));
+    // six float4 of state, two int4 segment ends, two queues of 2 records x 32 B, flags
+    const size_t bytes = (size_t)slots * (6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + sizeof(uint32_t));
     int rc = ctx->alloc(&ctx->wf_mem, bytes);
     if (rc != VT_OK) return rc;
     ctx->wf_slots = slots;
@@ -1100,7 +1101,7 @@ static WfSlots wf_slots_view(vt_context* ctx) {
   float4* f = (float4*)b;
   st.a0 = f; st.a1 = f + S; st.a2 = f + 2 * S; st.a3 = f + 3 * S; st.a4 = f + 4 * S; st.a5 = f + 5 * S;
   st.hits = (int4*)(f + 6 * S);
-  st.flags = (uint32_t*)(st.hits + 2 * S);
+  st.flags = (uint32_t*)((float4*)(st.hits + 2 * S) + 8 * S);   // after the two queues
   return st;
 }
 
@@ -1138,9 +1139,9 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   P.grids = ctx->d_grids;
   P.st = wf_slots_view(ctx);
   P.n_slots = (int32_t)slots;
-  uint32_t* qmem = (uint32_t*)(P.st.flags + ctx->wf_slots);
+  float4* qmem = (float4*)(P.st.hits + 2 * ctx->wf_slots);
   P.queue[0] = qmem;
-  P.queue[1] = qmem + 2 * ctx->wf_slots;
+  P.queue[1] = qmem + 4 * ctx->wf_slots;
   P.ctl = ctx->wf_ctl;
   P.next_item = (unsigned long long*)(ctx->wf_ctl + 8);
   P.n_items = (unsigned long long)items;

@@ -41,7 +41,8 @@ struct WfParams {
   const Grid* grids;               // device array, DDA view of each job's volume
   WfSlots st;
   int32_t n_slots;
-  uint32_t* queue[2];              // segment entries: slot << 2 | primary << 1 | kind
+  float4* queue[2];                // segment records, two float4 each:
+                                   // {origin.xyz, dir.x} {dir.yz, slot << 1 | kind, job}
   uint32_t* ctl;                   // per parity i: ctl[4i] entries appended to queue[i],
                                    // ctl[4i+1] entries taken by the tracer,
                                    // ctl[4i+2] active slots after the shade

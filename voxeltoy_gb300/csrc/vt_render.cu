@@ -225,7 +225,9 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
       }
     }
   }
-  // append the next segments: entry = slot << 2 | primary << 1 | kind
+  // append the next segments as 32-byte ray records {o.xyz, d.x} {d.yz,
+  // slot << 1 | kind, job}: the warp's extension records first, then its
+  // shadow records; a primary ray starts at its volume entry point
   const uint32_t n1 = (emit & 1u) ? 1u : 0u, n2 = (emit & 2u) ? 1u : 0u;
   const unsigned b1 = __ballot_sync(FULL, n1), b2 = __ballot_sync(FULL, n2);
   const uint32_t tot = __popc(b1) + __popc(b2);
@@ -233,10 +235,22 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(&P.ctl[4 * par], tot);
     base = __shfl_sync(FULL, base, 0);
-    // the warp's extension entries first, then its shadow entries
-    uint32_t* q = P.queue[par];
-    if (n1) q[base + __popc(b1 & lt)] = ((uint32_t)slot << 2) | (p.primary ? 2u : 0u);
-    if (n2) q[base + __popc(b1) + __popc(b2 & lt)] = ((uint32_t)slot << 2) | 1u;
+    float4* q = P.queue[par];
+    if (n1) {
+      v3 o = p.ro;
+      if (p.primary) {
+        const Frame& F = P.jobs[job].F;
+        o = primary_origin(p.ro, p.rd, ld3(F.bmin), ld3(F.bmax));
+      }
+      const size_t at = 2 * (size_t)(base + __popc(b1 & lt));
+      q[at] = make_float4(o.x, o.y, o.z, p.rd.x);
+      q[at + 1] = make_float4(p.rd.y, p.rd.z, __uint_as_float((uint32_t)slot << 1), __uint_as_float(job));
+    }
+    if (n2) {
+      const size_t at = 2 * (size_t)(base + __popc(b1) + __popc(b2 & lt));
+      q[at] = make_float4(p.ro.x, p.ro.y, p.ro.z, p.sd.x);
+      q[at + 1] = make_float4(p.sd.y, p.sd.z, __uint_as_float(((uint32_t)slot << 1) | 1u), __uint_as_float(job));
+    }
   }
   if (in_range) {
     uint32_t nf;
@@ -257,9 +271,10 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
 }
 
 // One round of tracing: every queued segment runs its DDA to the end.  Each
-// warp takes chunks of queue entries with one atomic and hands them to its
-// lanes as they finish their previous segment, so lanes stay busy until the
-// queue is drained.
+// warp takes chunks of queue records with one atomic and hands them to its
+// lanes; every lane keeps the record of its next segment loaded while it
+// steps the current one, so starting a segment never waits on memory, and
+// lanes pick up a new segment every kTraceSteps steps as theirs finish.
 constexpr uint32_t kTraceChunk = 128;
 
 template <bool kCount, int kTraceSteps>
@@ -269,18 +284,27 @@ __global__ void __launch_bounds__(256) k_wf_trace(const WfParams P, int par) {
   const unsigned lt = (1u << lane) - 1u;
   const uint32_t n = *(volatile uint32_t*)&P.ctl[4 * par];
   if (n == 0) return;
-  const uint32_t* q = P.queue[par];
+  const float4* q = P.queue[par];
   Cnt<kCount> cnt;
 #pragma unroll
   for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
   uint32_t pool = 0, pool_end = 0;
-  bool exhausted = false, have = false;
+  bool exhausted = false, have = false, have_next = false;
+  float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
   Grid g;
   Dda s;
-  uint32_t entry = 0;
+  uint32_t tag = 0;   // slot << 1 | kind of the current segment
   for (;;) {
-    unsigned need = __ballot_sync(FULL, !have);
-    while (need && !exhausted) {
+    if (!have && have_next) {            // start the prefetched segment
+      have_next = false;
+      tag = __float_as_uint(nb.z);
+      g = P.grids[__float_as_uint(nb.w)];
+      dda_begin(g, s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
+      if (s.state == DDA_RUNNING) have = true;
+      else P.st.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
+    }
+    unsigned need = __ballot_sync(FULL, !have_next);
+    while (need && !exhausted) {          // prefetch next records
       if (pool >= pool_end) {
         uint32_t c = 0;
         if (lane == 0) c = atomicAdd(&P.ctl[4 * par + 1], kTraceChunk);
@@ -291,31 +315,19 @@ __global__ void __launch_bounds__(256) k_wf_trace(const WfParams P, int par) {
       }
       const uint32_t avail = pool_end - pool;
       const uint32_t r = __popc(need & lt);
-      if (!have && r < avail) {
-        entry = __ldg(&q[pool + r]);
-        const int slot = (int)(entry >> 2);
-        const float4 a0 = __ldg(&P.st.a0[slot]);
-        g = P.grids[__float_as_uint(a0.w)];
-        const float4 ad = (entry & 1u) ? __ldg(&P.st.a2[slot]) : __ldg(&P.st.a1[slot]);
-        v3 o = xyz4(a0);
-        const v3 d = xyz4(ad);
-        if (entry & 2u) o = primary_origin(o, d, mk3(g.bminx, g.bminy, g.bminz), mk3(g.bmaxx, g.bmaxy, g.bmaxz));
-        dda_begin(g, s, o, d);
-        if (s.state == DDA_RUNNING) {
-          have = true;
-        } else {
-          P.st.hits[(size_t)(entry & 1u) * P.n_slots + slot] = make_int4(s.x, s.y, s.z, s.state);
-        }
+      if (!have_next && r < avail) {
+        na = __ldg(&q[2 * (size_t)(pool + r)]);
+        nb = __ldg(&q[2 * (size_t)(pool + r) + 1]);
+        have_next = true;
       }
       pool += min(avail, (uint32_t)__popc(need));
-      need = __ballot_sync(FULL, !have);
+      need = __ballot_sync(FULL, !have_next);
     }
-    if (__ballot_sync(FULL, have) == 0u) break;
+    if (__ballot_sync(FULL, have || have_next) == 0u) break;
     if (have) {
       dda_advance(g, s, kTraceSteps, cnt);
       if (s.state != DDA_RUNNING) {
-        const int slot = (int)(entry >> 2);
-        P.st.hits[(size_t)(entry & 1u) * P.n_slots + slot] = make_int4(s.x, s.y, s.z, s.state);
+        P.st.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
         have = false;
       }
     }
