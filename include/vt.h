@@ -350,6 +350,48 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
                            int32_t passes, const vt_batch_opts* opts,
                            int32_t* results);
 
+/* ------------------------------------------------ fixed-memory batching -- */
+/* No counterpart in the reference: its renderer draws one GL pass per frame
+ * and has no working memory of its own to speak of.
+ *
+ * vt_render_batch_fixed renders like vt_render_batch with the wavefront
+ * kernels, with bit-identical results, but allocates nothing.  The normal
+ * path grows per-context working buffers (path state, segment queues, the
+ * sample buffer, job tables) with cudaMalloc the first time a batch needs
+ * more.  That fails for a caller whose HBM budget (vt_create) is already
+ * spent on scenes and images, and it stalls a caller that must keep steady
+ * frame times, such as an interactive viewer, because cudaMalloc and
+ * cudaFree can synchronise the whole device.  Instead, this call takes all
+ * of its working memory from one array compiled into the library
+ * (VT_FIXED_SCRATCH_BYTES, about 34 MB, not counted against any budget),
+ * reserved on a device when the CUDA runtime loads the library's code for
+ * that device.
+ *
+ * Limits, each rejected with VT_EINVAL and a message naming the limit:
+ *   n_jobs        <= VT_FIXED_MAX_JOBS
+ *   path_slots    <= VT_FIXED_MAX_PATH_SLOTS (0 = that maximum)
+ *   width*height  <= VT_FIXED_MAX_SAMPLES for every job; a call traces at
+ *                    most that many samples per launch and splits the rest
+ *                    into further launches.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) once, with that device current; make that first
+ * call before any stream capture begins on the device.  Each launch clears
+ * the words that must start at zero (queue counters, the item counter, the
+ * path-slot flags); everything else in the array is written before it is
+ * read.  There is one array per device, shared by every call on every
+ * context of that device: two calls whose device work overlaps (two host
+ * threads, or two contexts driven at the same time) race on it and both
+ * results are wrong.  A call returns only after its device work has
+ * finished, so calls made one after another are safe. */
+#define VT_FIXED_MAX_JOBS 16
+#define VT_FIXED_MAX_PATH_SLOTS 65536
+#define VT_FIXED_MAX_SAMPLES (1 << 20)
+#define VT_FIXED_SCRATCH_BYTES 33826560
+VT_API int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs,
+                                 int32_t n_jobs, int32_t passes,
+                                 int32_t path_slots, int32_t* results);
+
 /* -------------------------------------------------------------- serving -- */
 typedef struct vt_server_opts {
   uint64_t hbm_budget_bytes;   /* admission budget for job buffers + scenes    */

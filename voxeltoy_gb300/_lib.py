@@ -141,6 +141,7 @@ SIGNATURES = {
     "vt_job_pick": [P, C.c_float, C.c_float, fp, C.POINTER(C.c_int32)],
     "vt_job_destroy": [P],
     "vt_render_batch": [P, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(BatchOpts), C.POINTER(C.c_int32)],
+    "vt_render_batch_fixed": [P, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)],
     "vt_server_create": [P, C.POINTER(ServerOpts), PP],
     "vt_server_submit": [P, P, P, C.POINTER(Camera), C.POINTER(RenderSettings), C.c_int32, C.c_int32, C.c_int32,
                          C.POINTER(C.c_uint64)],

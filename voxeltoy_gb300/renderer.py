@@ -115,6 +115,15 @@ class Context:
         L.call("vt_render_batch", self.h, arr, len(jobs), passes, C.byref(opts), res)
         return list(res)[: len(jobs)]
 
+    def render_batch_fixed(self, jobs: Sequence["Job"], passes: int, path_slots: int = 0) -> list[int]:
+        """vt_render_batch_fixed: like render_batch with the wavefront kernels,
+        with all working memory in the library's fixed device array (no
+        allocation; calls must not overlap)."""
+        arr = (C.c_void_p * max(1, len(jobs)))(*[j.h.value for j in jobs])
+        res = (C.c_int32 * max(1, len(jobs)))()
+        L.call("vt_render_batch_fixed", self.h, arr, len(jobs), passes, path_slots, res)
+        return list(res)[: len(jobs)]
+
 
 class Scene:
     def __init__(self, ctx: Context, handle: C.c_void_p):
