@@ -139,12 +139,17 @@ def cpu_sample_rate(cfg, seconds: float, threads: int = 0) -> dict:
     from oracle import binding as orc
     osc = orc.Scene(cfg.voxels, cfg.palette, cfg._emissive)
     oenv = orc.Env(cfg.env_rgb) if cfg.env_rgb is not None else orc.Env()
+    # two probes (a thin band, then about a second of work) give the path rate
     rows = 16
-    r0 = (cfg.height - rows) // 2
-    t0 = time.perf_counter()
-    orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 1, 32, threads, rows=(r0, r0 + rows))
-    dt = time.perf_counter() - t0
-    rate = rows * cfg.width / max(dt, 1e-9)
+    rate = 0.0
+    for probe_seconds in (0.0, 1.0):
+        if probe_seconds:
+            rows = int(min(cfg.height, max(16, rate * probe_seconds / cfg.width)))
+        r0 = (cfg.height - rows) // 2
+        t0 = time.perf_counter()
+        orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 1, 32, threads,
+                           rows=(r0, r0 + rows))
+        rate = rows * cfg.width / max(time.perf_counter() - t0, 1e-9)
     # full frame rows, then as many samples per pixel as fit the time budget
     want = rate * seconds
     band = int(min(cfg.height, max(rows, want / cfg.width)))
@@ -223,10 +228,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 persistent")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
+    ap.add_argument("--slots", type=int, default=0, help="path slots per launch (skips the autotuner)")
+    ap.add_argument("--trace-steps", type=int, default=0, help="DDA steps between refills (with --slots)")
+    ap.add_argument("--trace-bps", type=int, default=-1, help="trace blocks per SM, 0 = occupancy (with --slots)")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up and timed renders of the resident frame (for ncu captures)")
     args = ap.parse_args()
-    args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
+    if args.impl == "gb300" and not args.profile:
+        args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
     if args.impl == "reference":
         return run_reference(args, world, rank)
@@ -248,9 +257,13 @@ def main():
     job = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
     paths = cfg.width * cfg.height * cfg.spp
     tuning = {"path_slots": "default"}
-    if not args.no_tune and args.kernel == 2:
+    if args.slots > 0:
+        ctx.set_tuning(args.slots, args.trace_bps, args.trace_steps)
+        tuning = {"path_slots": args.slots, "trace_blocks_per_sm": args.trace_bps, "trace_steps": args.trace_steps,
+                  "source": "command line"}
+    elif not args.no_tune and args.kernel == 2:
         from voxeltoy_gb300 import autotune
-        best = autotune.tune(ctx, [job], passes=min(16, cfg.spp), use_cache=False)
+        best = autotune.tune(ctx, [job], passes=cfg.spp, repeats=1, use_cache=False)
         tuning = {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps")}
         for r in best.get("sweep", [])[:12]:
             print("tune", json.dumps(r), file=sys.stderr)
@@ -261,7 +274,8 @@ def main():
             job.render(cfg.spp)
             job.synchronize()
             if k >= args.warmup:
-                print(json.dumps({"profile_step_ms": 1e3 * (time.perf_counter() - t0), "paths": paths}), flush=True)
+                print(json.dumps({"profile_step_ms": 1e3 * (time.perf_counter() - t0), "paths": paths,
+                                  "launches": ctx.launch_count(), "tuning": tuning}), flush=True)
         job.close(); env.close(); scene.close(); ctx.close()
         return 0
 

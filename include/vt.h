@@ -341,7 +341,7 @@ VT_API int vt_job_destroy(vt_job* job);
  * (counter-based random streams, per-pixel sample order).  opts may be NULL
  * (autotuned defaults). */
 typedef struct vt_batch_opts {
-  int32_t path_slots;      /* paths in flight per launch, 0 = auto (1M)          */
+  int32_t path_slots;      /* paths in flight per launch, 0 = context default (8M) */
   int32_t blocks_per_sm;   /* resident blocks per SM, 0 = auto                  */
   int32_t threads_per_block; /* 0 = auto                                        */
   int32_t kernel;          /* 0 = auto, 1 = plain per-pixel, 2 = wavefront      */

@@ -1147,6 +1147,16 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   P.n_items = (unsigned long long)items;
   P.sbuf = ctx->sbuf;
   P.counters = count ? ctx->d_counters : nullptr;
+  WfJobTable table;
+  const WfJobTable* T = nullptr;
+  if (entries.size() <= (size_t)kWfParamJobs) {
+    memset(&table, 0, sizeof(table));
+    for (size_t i = 0; i < entries.size(); ++i) {
+      table.e[i] = entries[i];
+      table.g[i] = grids[i];
+    }
+    T = &table;
+  }
   VT_CUDA(cudaMemsetAsync(P.st.flags, 0, sizeof(uint32_t) * (size_t)slots, st), "slot flags");
   VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, 64, st), "wavefront control");
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
@@ -1156,8 +1166,8 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
     VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + 4 * par, 0, 3 * sizeof(uint32_t), st), "round counters");
-    VT_CUDA(launch_wf_shade(P, par, count, st), "wavefront shade");
-    VT_CUDA(launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st), "wavefront trace");
+    VT_CUDA(launch_wf_shade(P, par, count, st, T), "wavefront shade");
+    VT_CUDA(launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st, T), "wavefront trace");
     ctx->launches += 2;
     if ((iter & 7) == 7) {
       VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + 4 * par + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),

@@ -51,8 +51,17 @@ struct WfParams {
   float4* sbuf;                    // per-item sample outputs
   unsigned long long* counters;    // nullable
 };
-cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st);
-cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st);
+// Launches of at most kWfParamJobs jobs pass their job and grid records as a
+// kernel parameter as well, so the kernels read them through the constant
+// cache instead of global memory.
+constexpr int kWfParamJobs = 8;
+struct WfJobTable {
+  JobEntry e[kWfParamJobs];
+  Grid g[kWfParamJobs];
+};
+cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st, const WfJobTable* T = nullptr);
+cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,
+                            const WfJobTable* T = nullptr);
 cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max_pixels, const float4* sbuf,
                                  cudaStream_t st);
 int wf_trace_blocks_per_sm();

@@ -102,12 +102,31 @@ enum : uint32_t {
 __device__ __forceinline__ v3 xyz4(float4 v) { return mk3(v.x, v.y, v.z); }
 __device__ __forceinline__ float4 pack4(v3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
 
-// Job of a global item index (binary search over item_begin).
-__device__ __forceinline__ int job_of(const JobEntry* jobs, int n_jobs, unsigned long long item) {
-  int lo = 0, hi = n_jobs - 1;
+// Job and grid records: from the global tables, or (WfJobTable) from the
+// kernel's parameter block.
+struct WfNoTable {
+  int unused;
+};
+__device__ __forceinline__ const JobEntry& job_entry(const WfParams& P, const WfNoTable&, uint32_t j) {
+  return P.jobs[j];
+}
+__device__ __forceinline__ const JobEntry& job_entry(const WfParams&, const WfJobTable& T, uint32_t j) {
+  return T.e[j];
+}
+__device__ __forceinline__ const Grid& grid_entry(const WfParams& P, const WfNoTable&, uint32_t j) {
+  return P.grids[j];
+}
+__device__ __forceinline__ const Grid& grid_entry(const WfParams&, const WfJobTable& T, uint32_t j) {
+  return T.g[j];
+}
+
+// Job of a global item index (binary search over tile_begin).
+template <class Tab>
+__device__ __forceinline__ int job_of(const WfParams& P, const Tab& T, unsigned long long item) {
+  int lo = 0, hi = P.n_jobs - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
-    if ((unsigned long long)__ldg(&jobs[mid].tile_begin) <= item) lo = mid; else hi = mid - 1;
+    if ((unsigned long long)job_entry(P, T, (uint32_t)mid).tile_begin <= item) lo = mid; else hi = mid - 1;
   }
   return lo;
 }
@@ -152,8 +171,10 @@ __device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Fr
 // One round of shading: consume the segment results of the previous trace,
 // retire finished paths into the sample buffer, start new items, and append
 // the next segments to queue[par] (warp-aggregated).
-template <bool kCount>
-__global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
+// Eight resident blocks per SM (64 registers): the extra warps hide more of
+// the state-load and instruction-fetch latency than the few spills cost.
+template <bool kCount, class Tab>
+__global__ void __launch_bounds__(128, 8) k_wf_shade(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -171,7 +192,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
   if (active) {
     job = __float_as_uint(P.st.a0[slot].w);
     item = __float_as_uint(P.st.a1[slot].w);
-    const JobEntry& E = P.jobs[job];
+    const JobEntry& E = job_entry(P, T, job);
     load_path(P.st, slot, fl, E, item, p);
     if (fl & SL_SHADOW) {
       const int4 h = P.st.hits[(size_t)P.n_slots + slot];
@@ -209,8 +230,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
         dead = true;
       } else {
         item = (uint32_t)my;
-        job = (uint32_t)job_of(P.jobs, P.n_jobs, my);
-        const JobEntry& E = P.jobs[job];
+        job = (uint32_t)job_of(P, T, my);
+        const JobEntry& E = job_entry(P, T, job);
         const long long r = (long long)my - (long long)E.tile_begin;
         const int pass = (int)(r / E.n_pixels);
         const int pixel = (int)(r - (long long)pass * E.n_pixels);
@@ -239,7 +260,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
     if (n1) {
       v3 o = p.ro;
       if (p.primary) {
-        const Frame& F = P.jobs[job].F;
+        const Frame& F = job_entry(P, T, job).F;
         o = primary_origin(p.ro, p.rd, ld3(F.bmin), ld3(F.bmax));
       }
       const size_t at = 2 * (size_t)(base + __popc(b1 & lt));
@@ -255,8 +276,7 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
   if (in_range) {
     uint32_t nf;
     if (active) {
-      const JobEntry& E = P.jobs[job];
-      store_path(P.st, slot, E.F, p, job, item);
+      store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
       nf = SL_ACTIVE | (uint32_t)(p.bounces & 0xff) | (p.primary ? SL_PRIMARY : 0u) |
            (p.has_cont ? SL_HAS_CONT : 0u) | ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u) |
            ((uint32_t)(p.nee_nf & 7) << 14);
@@ -277,8 +297,8 @@ __global__ void __launch_bounds__(128) k_wf_shade(const WfParams P, int par) {
 // lanes pick up a new segment every kTraceSteps steps as theirs finish.
 constexpr uint32_t kTraceChunk = 128;
 
-template <bool kCount, int kTraceSteps>
-__global__ void __launch_bounds__(256) k_wf_trace(const WfParams P, int par) {
+template <bool kCount, int kTraceSteps, class Tab>
+__global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -298,7 +318,7 @@ __global__ void __launch_bounds__(256) k_wf_trace(const WfParams P, int par) {
     if (!have && have_next) {            // start the prefetched segment
       have_next = false;
       tag = __float_as_uint(nb.z);
-      g = P.grids[__float_as_uint(nb.w)];
+      g = grid_entry(P, T, __float_as_uint(nb.w));
       dda_begin(g, s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
       if (s.state == DDA_RUNNING) have = true;
       else P.st.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
@@ -347,18 +367,31 @@ __global__ void k_wf_accumulate(const JobEntry* jobs, const float4* sbuf) {
   E.J.comp[px] = comp;
 }
 
-cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st) {
+template <class Tab>
+static void wf_shade(const WfParams& P, const Tab& T, int par, bool count, cudaStream_t st) {
   const int blocks = (P.n_slots + 127) / 128;
-  if (count) k_wf_shade<true><<<blocks, 128, 0, st>>>(P, par);
-  else k_wf_shade<false><<<blocks, 128, 0, st>>>(P, par);
+  if (count) k_wf_shade<true, Tab><<<blocks, 128, 0, st>>>(P, T, par);
+  else k_wf_shade<false, Tab><<<blocks, 128, 0, st>>>(P, T, par);
+}
+
+cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st, const WfJobTable* T) {
+  if (T && P.n_jobs <= kWfParamJobs) wf_shade(P, *T, par, count, st);
+  else wf_shade(P, WfNoTable{0}, par, count, st);
   return cudaGetLastError();
 }
 
-cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st) {
-  if (count) k_wf_trace<true, 16><<<blocks, 256, 0, st>>>(P, par);
-  else if (steps <= 8) k_wf_trace<false, 8><<<blocks, 256, 0, st>>>(P, par);
-  else if (steps <= 16) k_wf_trace<false, 16><<<blocks, 256, 0, st>>>(P, par);
-  else k_wf_trace<false, 32><<<blocks, 256, 0, st>>>(P, par);
+template <class Tab>
+static void wf_trace(const WfParams& P, const Tab& T, int par, int blocks, int steps, bool count, cudaStream_t st) {
+  if (count) k_wf_trace<true, 16, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else if (steps <= 8) k_wf_trace<false, 8, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else if (steps <= 16) k_wf_trace<false, 16, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else k_wf_trace<false, 32, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+}
+
+cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,
+                            const WfJobTable* T) {
+  if (T && P.n_jobs <= kWfParamJobs) wf_trace(P, *T, par, blocks, steps, count, st);
+  else wf_trace(P, WfNoTable{0}, par, blocks, steps, count, st);
   return cudaGetLastError();
 }
 
@@ -372,7 +405,7 @@ cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max
 
 int wf_trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8, WfJobTable>, 256, 0);
   return n;
 }
 

@@ -36,7 +36,7 @@ struct vt_context {
   int64_t sbuf_items = 0;
   uint32_t* wf_ctl = nullptr;    // [2][4] qcount, qhead, live, pad + next_item
   uint32_t* h_live = nullptr;    // pinned host copy of a live counter
-  int64_t max_slots = 1 << 21;   // path slots per launch
+  int64_t max_slots = 1 << 23;   // path slots per launch
   int64_t max_items = 1 << 28;   // samples per launch (sample buffer entries)
   int trace_blocks_per_sm = 0;   // 0 = occupancy limit
   int trace_occupancy = 0;       // occupancy limit of the DDA kernel (cached)
