@@ -20,6 +20,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -215,6 +216,258 @@ def config_dict(args, cfg) -> dict:
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
 
 
+class EventTimer:
+    """CUDA-event time (ms) of the work enqueued on the library's stream."""
+
+    def __init__(self, ctx, device: int):
+        import torch
+        self.torch = torch
+        self.stream = torch.cuda.ExternalStream(ctx.stream(), device=f"cuda:{device}")
+
+    def __enter__(self):
+        self.e0 = self.torch.cuda.Event(enable_timing=True)
+        self.e1 = self.torch.cuda.Event(enable_timing=True)
+        self.e0.record(self.stream)
+        return self
+
+    def __exit__(self, *exc):
+        self.e1.record(self.stream)
+        self.e1.synchronize()
+        self.ms = self.e0.elapsed_time(self.e1)
+
+
+def batching_jobs(ctx, n: int):
+    """The batching configuration: scene i from the sphere-union generator
+    (seed 100 + i, edge log-uniform 32-512, occupancy U[10%, 50%]), a
+    resolution from {128, 256, 512, 1024}^2, config-1 camera and shading."""
+    from voxeltoy_gb300 import Job, Scene, scenes as S
+    made = []
+    for i in range(n):
+        vox, res, seed = S.config3_scene(i)
+        cfg = S.config1(edge=8, width=res, height=res, spp=64, seed=seed)
+        sc = Scene.dense(ctx, vox, cfg.palette)
+        made.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, res, res), vox))
+    return made
+
+
+def run_batching(args, world, rank, local):
+    import torch
+    from voxeltoy_gb300 import Context
+    spp = 64
+    ctx = Context(local)
+    made = batching_jobs(ctx, args.scenes)
+    jobs = [m[1] for m in made]
+    paths = sum(j.width * j.height for j in jobs) * spp
+    from voxeltoy_gb300 import autotune
+    best = autotune.tune(ctx, jobs, passes=16, repeats=1, use_cache=False,
+                         grid={"path_slots": [1 << 22, 1 << 23, 1 << 24], "trace_blocks_per_sm": [0],
+                               "trace_steps": [16]})
+    timer = EventTimer(ctx, local)
+
+    def reset():
+        for j in jobs:
+            j.reset()
+        torch.cuda.synchronize()
+
+    def batched():
+        ctx.render_batch(jobs, spp, kernel=2)
+
+    def plain_loop():                  # the reference's structure: one launch per scene and pass
+        ctx.render_batch(jobs, spp, kernel=1)
+
+    def per_scene():                   # one wavefront render per scene
+        for j in jobs:
+            j.render(spp)
+
+    out = {}
+    images = {}
+    for name, fn, reps in (("batched", batched, args.steps), ("per_scene_wavefront", per_scene, 1),
+                           ("plain_loop", plain_loop, 1)):
+        times = []
+        for k in range(reps + 1):
+            reset()
+            with timer:
+                fn()
+            if k:
+                times.append(timer.ms)
+        out[name] = {"ms": float(np.median(times)), "mpaths_s": paths / (np.median(times) * 1e-3) / 1e6}
+        images[name] = [j.readback() for j in jobs]
+    same = all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
+               for name in ("per_scene_wavefront", "plain_loop") for a, b in zip(images["batched"], images[name]))
+    # end to end: upload every scene from host memory, render the batch, read every image back
+    vox_h = [m[2] for m in made]
+    for sc, j, _v in made:
+        j.close(); sc.close()
+    from voxeltoy_gb300 import Job, Scene, scenes as S
+    t0 = time.perf_counter()
+    e2e_jobs = []
+    for i, vox in enumerate(vox_h):
+        _v, res, seed = vox, jobs[i].width, 100 + i
+        cfg = S.config1(edge=8, width=res, height=res, spp=spp, seed=seed)
+        sc = Scene.dense(ctx, vox, cfg.palette)
+        e2e_jobs.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, res, res)))
+    ctx.render_batch([j for _s, j in e2e_jobs], spp, kernel=2)
+    d2h = 0
+    for _s, j in e2e_jobs:
+        d2h += j.readback().nbytes
+    e2e_s = time.perf_counter() - t0
+    for sc, j in e2e_jobs:
+        j.close(); sc.close()
+    ctx.close()
+    b = out["batched"]
+    return {"metric": METRIC, "value": b["mpaths_s"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": 1, "ms_per_step": b["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded batching configuration)",
+            "config": {"workload": f"batching: {len(jobs)} sphere-union scenes (seed 100+i, edges 32-512 "
+                                   f"log-uniform, occupancy U[10%,50%]), resolutions from {{128,256,512,1024}}^2, "
+                                   f"Lambert 0.7, white sky, 4 bounces, {spp} spp, one launch",
+                       "paths_per_step": paths, "voxels": int(sum(v.size for v in vox_h))},
+            "batched": b, "per_scene_wavefront": out["per_scene_wavefront"], "plain_loop": out["plain_loop"],
+            "batched_vs_plain": out["plain_loop"]["ms"] / b["ms"],
+            "batched_vs_per_scene": out["per_scene_wavefront"]["ms"] / b["ms"],
+            "identical_images": bool(same),
+            "e2e": {"value": paths / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(sum(v.nbytes for v in vox_h)),
+                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
+            "tuning": {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps")}}
+
+
+def run_serving(args, world, rank, local):
+    """Poisson request stream through vt_server: each request is a
+    sphere-union scene (edge 64-512), a random orbit camera, a resolution
+    with edge uniform in 256-1024 and an spp target log-uniform in
+    16-1024; half of the requests reuse a resident scene.  Latency = arrival
+    to the target sample count, read from the server's own clock plus the
+    host's submission delay."""
+    from voxeltoy_gb300 import Context, Scene, Server, scenes as S
+    rng = np.random.default_rng(3)
+    n = max(1, int(rng.poisson(args.rate * args.duration)))
+    arrivals = np.sort(rng.uniform(0.0, args.duration, n))
+    pool_n = 16
+    pool = []
+    for i in range(pool_n):
+        edge = int(rng.integers(64, 513))
+        pool.append(S.sphere_union(edge, None, 300 + i, occupancy=float(rng.uniform(0.1, 0.5))))
+    ctx = Context(local)
+    srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4)
+    resident = []
+    reqs = []
+    for k in range(n):
+        res = int(rng.integers(256, 1025))
+        spp = int(round(math.exp(rng.uniform(math.log(16), math.log(1024)))))
+        reuse = bool(resident) and rng.random() < 0.5
+        pick = int(rng.integers(0, len(resident))) if reuse else int(rng.integers(0, pool_n))
+        cam = S.orbit_camera(distance=2000.0, theta_deg=float(rng.uniform(0, 360)), phi_deg=float(rng.uniform(10, 80)))
+        reqs.append((res, spp, reuse, pick, cam))
+        if not reuse:
+            resident.append(None)
+    settings = S.physical_settings(max_bounces=4, rr_start=-1, seed=0)
+    scenes = []
+    tickets = []
+    t_start = time.perf_counter()
+    for k, (res, spp, reuse, pick, cam) in enumerate(reqs):
+        wait = arrivals[k] - (time.perf_counter() - t_start)
+        if wait > 0:
+            time.sleep(wait)
+        if reuse:
+            sc = scenes[pick]
+        else:
+            sc = Scene.dense(ctx, pool[pick], [S.lambert(0.7)])
+            scenes.append(sc)
+        t_sub = time.perf_counter() - t_start
+        tickets.append((srv.submit(sc, None, cam, settings, res, res, spp), t_sub - arrivals[k], res * res * spp))
+    lat = []
+    for t, delay, _p in tickets:
+        rc = srv.wait(t, 3600.0)
+        if rc != 0:
+            raise RuntimeError(f"request {t} failed: {rc}")
+        lat.append(delay + srv_latency(srv, t))
+    t_end = time.perf_counter() - t_start
+    lat = np.array(lat)
+    stats = srv.stats()
+    paths = sum(p for _t, _d, p in tickets)
+    srv.close()
+    for sc in scenes:
+        sc.close()
+    ctx.close()
+    return {"metric": METRIC, "value": paths / t_end / 1e6, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": t_end * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded request stream)",
+            "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s ({n} requests), "
+                                   f"sphere-union scenes edge 64-512 (pool of {pool_n}), reuse 0.5, resolution "
+                                   f"256^2-1024^2, 16-1024 spp log-uniform, 4 bounces, 60 GB admission budget",
+                       "requests": n, "offered_mpaths_s": paths / args.duration / 1e6},
+            "time_to_spp_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
+                               "max": float(lat.max() * 1e3)},
+            "server": {"completed": int(stats.completed), "failed": int(stats.failed)},
+            "e2e": {"value": paths / t_end / 1e6, "unit": UNIT,
+                    "h2d_bytes_per_step": int(sum(pool[r[3]].nbytes for r in reqs if not r[2])),
+                    "d2h_bytes_per_step": 0}}
+
+
+def srv_latency(srv, ticket) -> float:
+    """Submit-to-finish seconds of a finished request (the server's clock)."""
+    import ctypes as C
+    from voxeltoy_gb300 import _lib as L
+    secs = C.c_double()
+    L.call("vt_server_result", srv.h, ticket, None, 0, C.byref(secs))
+    return secs.value
+
+
+def run_voxelize(args, world, rank, local):
+    """1.3M-triangle fBm-displaced icosphere, conservative voxelization into
+    1024^3, then a 2048^2 render with config-1 materials and sky, 8 bounces."""
+    import torch
+    from voxeltoy_gb300 import Context, Job, Scene, scenes as S
+    from voxeltoy_gb300 import _lib as L
+    v, f = S.fbm_displaced_icosphere(level=8)
+    v = np.ascontiguousarray(v, np.float32)
+    f = np.ascontiguousarray(f, np.uint32)
+    res = (1024, 1024, 1024)
+    ctx = Context(local)
+    vox_ms = []
+    for k in range(args.steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sc = Scene.voxelize(ctx, v, f, res, mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
+                            palette=[S.lambert(0.7)])
+        sc.info()
+        torch.cuda.synchronize()
+        if k:
+            vox_ms.append((time.perf_counter() - t0) * 1e3)
+        if k < args.steps:
+            sc.close()
+    check = None
+    if args.check:
+        from oracle import binding as orc
+        want = orc.voxelize(v, f, res, L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE)
+        got = sc.voxels()
+        check = {"bit_exact": bool(np.array_equal(want > 0, got > 0)), "occupied": int(np.count_nonzero(got))}
+    spp = args.spp if args.spp != 256 else 1024
+    cfg = S.config1(edge=8, width=2048, height=2048, spp=spp)
+    cfg.settings.max_bounces = 8
+    job = Job(ctx, sc, None, cfg.camera, cfg.settings, 2048, 2048)
+    timer = EventTimer(ctx, local)
+    job.render(4)
+    job.reset()
+    torch.cuda.synchronize()
+    with timer:
+        job.render(spp)
+    paths = 2048 * 2048 * spp
+    img = job.readback()
+    job.close(); sc.close(); ctx.close()
+    return {"metric": METRIC, "value": paths / (timer.ms * 1e-3) / 1e6, "unit": UNIT, "n_gpus": world, "steps": 1,
+            "warmup": 1, "ms_per_step": timer.ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded icosphere mesh)",
+            "config": {"workload": f"voxelize: fBm-displaced icosphere level 8 ({len(f)} triangles) -> 1024^3 "
+                                   f"conservative, then 2048^2 pinhole, Lambert 0.7, white sky, 8 bounces, {spp} spp",
+                       "triangles": int(len(f))},
+            "voxelize_ms": {"median": float(np.median(vox_ms)), "min": float(min(vox_ms))},
+            "voxelize_mtris_s": len(f) / (np.median(vox_ms) * 1e-3) / 1e6,
+            "occupancy_check": check, "image_finite": bool(np.isfinite(img).all()),
+            "e2e": {"value": paths / (timer.ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
+                    "d2h_bytes_per_step": int(img.nbytes)}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -231,6 +484,14 @@ def main():
     ap.add_argument("--slots", type=int, default=0, help="path slots per launch (skips the autotuner)")
     ap.add_argument("--trace-steps", type=int, default=0, help="DDA steps between refills (with --slots)")
     ap.add_argument("--trace-bps", type=int, default=-1, help="trace blocks per SM, 0 = occupancy (with --slots)")
+    ap.add_argument("--workload", default="config2", choices=["config2", "batching", "serving", "voxelize"],
+                    help="config2 (default, the headline line); batching = 64 uneven scenes in one launch vs "
+                         "a loop of plain per-scene launches; serving = Poisson request stream through the "
+                         "server; voxelize = 1.3M-triangle mesh into 1024^3, then a 2048^2 render")
+    ap.add_argument("--scenes", type=int, default=64, help="batching: number of scenes")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: requests per second")
+    ap.add_argument("--duration", type=float, default=5.0, help="serving: seconds of arrivals")
+    ap.add_argument("--check", action="store_true", help="voxelize: compare the occupancy with the oracle")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up and timed renders of the resident frame (for ncu captures)")
     args = ap.parse_args()
@@ -245,6 +506,12 @@ def main():
     from voxeltoy_gb300 import _lib as L
 
     torch.cuda.set_device(local)
+    if args.workload != "config2":
+        runner = {"batching": run_batching, "serving": run_serving, "voxelize": run_voxelize}[args.workload]
+        line = runner(args, world, rank, local)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return 0
     cfg = workload_config(args)
     pk = peaks()
     ctx = Context(local)
@@ -366,7 +633,7 @@ def main():
                                     "4 B/emissive read + 64 B/path framebuffer"},
         "counters_per_frame": {"paths": int(cnt[0]), "dda_cells": int(cnt[1]), "palette": int(cnt[2]),
                                "env_evals": int(cnt[3]), "cdf_probes": int(cnt[4]), "emissive_reads": int(cnt[5]),
-                               "segments": int(cnt[6])},
+                               "segments": int(cnt[6]), "empty_brick_cells": int(cnt[7])},
         "time_to_spp_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99))},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),

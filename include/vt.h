@@ -255,7 +255,9 @@ VT_API int vt_camera_compute_uniforms(const vt_camera* cam, int32_t width,
 #define VT_QUIRK_EXPONENT_IS_ROUGHNESS (1u << 5) /* Blinn exponent = roughness, metal.h:13-14    */
 #define VT_QUIRK_THINLENS_NO_JITTER    (1u << 6) /* no pixel jitter, generateRay.h:83            */
 #define VT_QUIRK_UNGUARDED_SAMPLES     (1u << 7) /* zero-pdf / below-surface samples propagate,  */
-                                                 /* pathTracer.fs:164,276 divide by the pdf     */
+                                                 /* pathTracer.fs:164,276 divide by the pdf;    */
+                                                 /* a hit on a voxel corner keeps the three-axis */
+                                                 /* normal whose frame is NaN, coordinates.h:79 */
 #define VT_QUIRKS_REFERENCE 0xffu
 
 /* Random-number source.  VT_RNG_NOISE_TABLE walks a 1024x1024 RGBA table

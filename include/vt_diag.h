@@ -20,7 +20,8 @@ extern "C" {
 /* Event counters (per launch, summed over paths):
  * [0] paths, [1] DDA cells tested, [2] palette records read,
  * [3] environment texel evaluations, [4] CDF entries probed,
- * [5] emissive-list reads, [6] DDA segments started, [7] unused. */
+ * [5] emissive-list reads, [6] DDA segments started, [7] DDA cells tested
+ * inside 4x4x4 bricks that hold no occupied voxel. */
 #define VT_DIAG_NUM_COUNTERS 8
 
 /* Trace caller-supplied rays through the job's scene with the DDA of

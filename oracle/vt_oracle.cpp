@@ -408,8 +408,11 @@ struct Tracer {
     return *ground;
   }
 
-  // voxelSpaceToWorldSpace (coordinates.h:59-82)
-  Basis voxel_basis(const int* p, vec3 ro, vec3 rd) const {
+  // voxelSpaceToWorldSpace (coordinates.h:59-82).  one_axis: a three-way
+  // tie (a hit exactly on a voxel corner, whose reference frame is
+  // normalize(0) = NaN) keeps only the axis of the largest |rd| component,
+  // x before y before z.
+  Basis voxel_basis(const int* p, vec3 ro, vec3 rd, bool one_axis = false) const {
     const vec3 vsP = v3<R>(R(p[0]), R(p[1]), R(p[2]));
     const vec3 wsVoxelMin = vsP * vsize + bmin;
     const vec3 wsVoxelMax = wsVoxelMin + vsize;
@@ -420,9 +423,17 @@ struct Tracer {
     const vec3 c2h = b.position - center;
     const vec3 a = vabs(c2h);
     // step(a.yxx, a.xyz) * step(a.zzy, a.xyz)
-    const R mx = (glstep(a.y, a.x) ? R(1) : R(0)) * (glstep(a.z, a.x) ? R(1) : R(0));
-    const R my = (glstep(a.x, a.y) ? R(1) : R(0)) * (glstep(a.z, a.y) ? R(1) : R(0));
-    const R mz = (glstep(a.x, a.z) ? R(1) : R(0)) * (glstep(a.y, a.z) ? R(1) : R(0));
+    R mx = (glstep(a.y, a.x) ? R(1) : R(0)) * (glstep(a.z, a.x) ? R(1) : R(0));
+    R my = (glstep(a.x, a.y) ? R(1) : R(0)) * (glstep(a.z, a.y) ? R(1) : R(0));
+    R mz = (glstep(a.x, a.z) ? R(1) : R(0)) * (glstep(a.y, a.z) ? R(1) : R(0));
+    if (one_axis && mx != R(0) && my != R(0) && mz != R(0)) {
+      const vec3 ad = vabs(rd);
+      const bool kx = ad.x >= ad.y && ad.x >= ad.z;
+      const bool ky = !kx && ad.y >= ad.z;
+      mx = kx ? R(1) : R(0);
+      my = ky ? R(1) : R(0);
+      mz = (!kx && !ky) ? R(1) : R(0);
+    }
     b.normal = v3<R>(mx, my, mz) * v3<R>(glsign(c2h.x), glsign(c2h.y), glsign(c2h.z));
     const R k = R(0.57735026919f);
     const vec3 tangent = cross(b.normal, v3<R>(k, k, k));
@@ -771,7 +782,7 @@ struct Tracer {
       vec3 throughput = v3<R>(R(1), R(1), R(1));
       int bounces = 0;
       while (bounces < S->max_bounces) {
-        const Basis b = voxel_basis(vs, o, d);
+        const Basis b = voxel_basis(vs, o, d, !(S->quirks & Q_UNGUARDED));
         const Mat m = material(vs[0], vs[1], vs[2], C);
         if (S->select_enabled && vs[0] == S->selected_voxel[0] && vs[1] == S->selected_voxel[1] &&
             vs[2] == S->selected_voxel[2]) {

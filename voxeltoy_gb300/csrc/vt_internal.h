@@ -121,6 +121,7 @@ enum Counter {
   C_CDF_PROBES = 4,
   C_EMISSIVE_READS = 5,
   C_SEGMENTS = 6,
+  C_EMPTY_CELLS = 7,   // DDA cells tested inside bricks with no occupied voxel
   C_NUM = 8
 };
 

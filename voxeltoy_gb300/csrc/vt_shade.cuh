@@ -178,8 +178,11 @@ VT_D float ray_aabb(v3 o, v3 d, v3 bmin, v3 bmax) {
 // ------------------------------------------------------------------ basis
 struct Basis { v3 position, tangent, normal, binormal; };
 
-// voxelSpaceToWorldSpace (coordinates.h:59-82).
-VT_D Basis voxel_basis(const Frame& F, int x, int y, int z, v3 ro, v3 rd) {
+// voxelSpaceToWorldSpace (coordinates.h:59-82).  A hit exactly on a voxel
+// corner ties all three axes; the reference's frame is then normalize(0),
+// NaN.  With `one_axis` such a tie keeps only the axis along which the ray
+// moves fastest (x before y before z on equal speeds).
+VT_D Basis voxel_basis(const Frame& F, int x, int y, int z, v3 ro, v3 rd, bool one_axis = false) {
   const v3 vs = ld3(F.vsize);
   const v3 vmin = mk3((float)x, (float)y, (float)z) * vs + ld3(F.bmin);
   const v3 vmax = vmin + vs;
@@ -189,9 +192,17 @@ VT_D Basis voxel_basis(const Frame& F, int x, int y, int z, v3 ro, v3 rd) {
   const v3 center = vmin + vs * 0.5f;
   const v3 c2h = b.position - center;
   const v3 a = vabs3(c2h);
-  const float mx = (vtb::gstep(a.y, a.x) && vtb::gstep(a.z, a.x)) ? 1.0f : 0.0f;
-  const float my = (vtb::gstep(a.x, a.y) && vtb::gstep(a.z, a.y)) ? 1.0f : 0.0f;
-  const float mz = (vtb::gstep(a.x, a.z) && vtb::gstep(a.y, a.z)) ? 1.0f : 0.0f;
+  float mx = (vtb::gstep(a.y, a.x) && vtb::gstep(a.z, a.x)) ? 1.0f : 0.0f;
+  float my = (vtb::gstep(a.x, a.y) && vtb::gstep(a.z, a.y)) ? 1.0f : 0.0f;
+  float mz = (vtb::gstep(a.x, a.z) && vtb::gstep(a.y, a.z)) ? 1.0f : 0.0f;
+  if (one_axis && mx != 0.0f && my != 0.0f && mz != 0.0f) {
+    const v3 ad = vabs3(rd);
+    const bool kx = ad.x >= ad.y && ad.x >= ad.z;
+    const bool ky = !kx && ad.y >= ad.z;
+    mx = kx ? 1.0f : 0.0f;
+    my = ky ? 1.0f : 0.0f;
+    mz = (!kx && !ky) ? 1.0f : 0.0f;
+  }
   b.normal = mk3(mx * vtb::gsign(c2h.x), my * vtb::gsign(c2h.y), mz * vtb::gsign(c2h.z));
   const float d3 = 0.57735026919f;
   const v3 tangent = cross(b.normal, mk3(d3, d3, d3));
@@ -286,6 +297,7 @@ VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt) {
       break;
     }
     cnt.add(C_DDA_CELLS, 1);
+    if (kCount && bits == 0ull) cnt.add(C_EMPTY_CELLS, 1);
     // step(dis.xyz, dis.yxy) * step(dis.xyz, dis.zzx): every axis whose
     // distance equals the minimum (distances are never NaN)
     const float m = fminf(dx, fminf(dy, dz));
@@ -751,7 +763,7 @@ VT_D bool ext_end(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount
   }
   if (!p.primary) p.bounces += 1;                                 // :291
   if (p.bounces >= F.max_bounces) return false;                   // :214
-  const Basis b = voxel_basis(F, e.x, e.y, e.z, p.ro, p.rd);      // :220-223
+  const Basis b = voxel_basis(F, e.x, e.y, e.z, p.ro, p.rd, !(F.quirks & Q_UNGUARDED));   // :220-223
   const Mat m = voxel_mat(F, J, e.x, e.y, e.z, cnt);              // :225-226
   if (F.sel_enabled && e.x == F.sel[0] && e.y == F.sel[1] && e.z == F.sel[2]) {
     p.L = p.L + mk3(1.0f, 0.0f, 0.0f);                            // :228-233
