@@ -7,8 +7,8 @@
 //   job table   VT_FIXED_MAX_JOBS JobEntry records
 //   grid table  VT_FIXED_MAX_JOBS Grid records
 //   path slots  VT_FIXED_MAX_PATH_SLOTS x (six float4 of state, two int4
-//               segment ends, two queues of two 32-byte records, a flag word);
-//               the flags must start at zero
+//               segment ends, two queues of two 32-byte records, a flag word,
+//               a free-list entry); the flags must start at zero
 //   samples     VT_FIXED_MAX_SAMPLES float4 per-sample outputs
 // The kernels are the ones vt_render_batch runs; only where their buffers
 // live differs, so results are bit-identical.
@@ -24,7 +24,7 @@ namespace {
 
 constexpr size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-constexpr size_t kSlotBytes = 6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + sizeof(uint32_t);
+constexpr size_t kSlotBytes = 6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 2 * sizeof(uint32_t);
 constexpr size_t kCtlOff = 0;
 constexpr size_t kJobsOff = kCtlOff + 256;
 constexpr size_t kGridsOff = kJobsOff + round256(sizeof(JobEntry) * VT_FIXED_MAX_JOBS);
@@ -93,6 +93,7 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   P.queue[0] = (float4*)(P.st.hits + 2 * S);
   P.queue[1] = P.queue[0] + 4 * S;
   P.st.flags = (uint32_t*)(P.queue[1] + 4 * S);
+  P.free_slots = P.st.flags + S;
   P.n_slots = (int32_t)slots;
   P.ctl = ctl;
   P.next_item = (unsigned long long*)(ctl + 8);
@@ -113,13 +114,13 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   const int trace_blocks = ctx->sm_count * bps;
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
-    e = cudaMemsetAsync(ctl + 4 * par, 0, 3 * sizeof(uint32_t), st);
+    e = cudaMemsetAsync(ctl + 4 * par, 0, 4 * sizeof(uint32_t), st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed round counters");
-    e = launch_wf_shade(P, par, false, st);
+    e = launch_wf_shade(P, par, ctx->sm_count * 8, false, st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed wavefront shade");
     e = launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, false, st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed wavefront trace");
-    ctx->launches += 2;
+    ctx->launches += 3;
     if ((iter & 7) == 7) {
       uint32_t live = 0;   // pageable: the copy has completed when it returns
       e = cudaMemcpyAsync(&live, ctl + 4 * par + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);

@@ -45,7 +45,9 @@ struct WfParams {
                                    // {origin.xyz, dir.x} {dir.yz, slot << 1 | kind, job}
   uint32_t* ctl;                   // per parity i: ctl[4i] entries appended to queue[i],
                                    // ctl[4i+1] entries taken by the tracer,
-                                   // ctl[4i+2] active slots after the shade
+                                   // ctl[4i+2] active slots after the shade and regen,
+                                   // ctl[4i+3] entries appended to free_slots
+  uint32_t* free_slots;            // slots that need a new path (n_slots entries)
   unsigned long long* next_item;
   unsigned long long n_items;
   float4* sbuf;                    // per-item sample outputs
@@ -59,7 +61,10 @@ struct WfJobTable {
   JobEntry e[kWfParamJobs];
   Grid g[kWfParamJobs];
 };
-cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st, const WfJobTable* T = nullptr);
+// k_wf_shade over every slot, then k_wf_regen (regen_blocks blocks of 128)
+// over the free list it leaves.
+cudaError_t launch_wf_shade(const WfParams& P, int par, int regen_blocks, bool count, cudaStream_t st,
+                            const WfJobTable* T = nullptr);
 cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,
                             const WfJobTable* T = nullptr);
 cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max_pixels, const float4* sbuf,

@@ -168,9 +168,42 @@ __device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Fr
   st.a5[slot] = pack4(p.nee_P, 0.0f);
 }
 
+// Append this warp's next segments to queue[par] as 32-byte ray records
+// {o.xyz, d.x} {d.yz, slot << 1 | kind, job}: the warp's extension records
+// first, then its shadow records.  emit: 1 extension (from `ext_o`), 2 shadow.
+__device__ __forceinline__ void append_segments(const WfParams& P, int par, uint32_t emit, int slot, uint32_t job,
+                                                v3 ext_o, const Path& p) {
+  const unsigned FULL = 0xffffffffu;
+  const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
+  const uint32_t n1 = (emit & 1u) ? 1u : 0u, n2 = (emit & 2u) ? 1u : 0u;
+  const unsigned b1 = __ballot_sync(FULL, n1), b2 = __ballot_sync(FULL, n2);
+  const uint32_t tot = __popc(b1) + __popc(b2);
+  if (tot == 0) return;
+  uint32_t base = 0;
+  if ((threadIdx.x & 31) == 0) base = atomicAdd(&P.ctl[4 * par], tot);
+  base = __shfl_sync(FULL, base, 0);
+  float4* q = P.queue[par];
+  if (n1) {
+    const size_t at = 2 * (size_t)(base + __popc(b1 & lt));
+    q[at] = make_float4(ext_o.x, ext_o.y, ext_o.z, p.rd.x);
+    q[at + 1] = make_float4(p.rd.y, p.rd.z, __uint_as_float((uint32_t)slot << 1), __uint_as_float(job));
+  }
+  if (n2) {
+    const size_t at = 2 * (size_t)(base + __popc(b1) + __popc(b2 & lt));
+    q[at] = make_float4(p.ro.x, p.ro.y, p.ro.z, p.sd.x);
+    q[at + 1] = make_float4(p.sd.y, p.sd.z, __uint_as_float(((uint32_t)slot << 1) | 1u), __uint_as_float(job));
+  }
+}
+
+__device__ __forceinline__ uint32_t slot_flags(const Path& p, uint32_t emit) {
+  return SL_ACTIVE | (uint32_t)(p.bounces & 0xff) | (p.primary ? SL_PRIMARY : 0u) | (p.has_cont ? SL_HAS_CONT : 0u) |
+         ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u) | ((uint32_t)(p.nee_nf & 7) << 14);
+}
+
 // One round of shading: consume the segment results of the previous trace,
-// retire finished paths into the sample buffer, start new items, and append
-// the next segments to queue[par] (warp-aggregated).
+// retire finished paths into the sample buffer, append the next segments to
+// queue[par] and the slots that need a new path to the free list (both
+// warp-aggregated).  New paths are started by k_wf_regen.
 // Eight resident blocks per SM (64 registers): the extra warps hide more of
 // the state-load and instruction-fetch latency than the few spills cost.
 template <bool kCount, class Tab>
@@ -183,7 +216,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_shade(const WfParams P, const __g
   Cnt<kCount> cnt;
 #pragma unroll
   for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
-  uint32_t fl = in_range ? P.st.flags[slot] : SL_DEAD;
+  const uint32_t fl = in_range ? P.st.flags[slot] : SL_DEAD;
   bool active = (fl & SL_ACTIVE) != 0;
   bool need_new = !active && !(fl & SL_DEAD);
   Path p;
@@ -213,80 +246,89 @@ __global__ void __launch_bounds__(128, 8) k_wf_shade(const WfParams P, const __g
       need_new = true;
     }
   }
-  // start new items, warp-aggregated; a path that misses the volume is
-  // finished at once and its lane asks again
-  bool dead = (fl & SL_DEAD) != 0;
-  for (;;) {
-    const unsigned want = __ballot_sync(FULL, need_new);
-    if (!want) break;
-    const int leader = __ffs(want) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(P.next_item, (unsigned long long)__popc(want));
-    base = __shfl_sync(FULL, base, leader);
-    if (need_new) {
-      const unsigned long long my = base + __popc(want & lt);
-      if (my >= P.n_items) {
-        need_new = false;
-        dead = true;
-      } else {
-        item = (uint32_t)my;
-        job = (uint32_t)job_of(P, T, my);
-        const JobEntry& E = job_entry(P, T, job);
-        const long long r = (long long)my - (long long)E.tile_begin;
-        const int pass = (int)(r / E.n_pixels);
-        const int pixel = (int)(r - (long long)pass * E.n_pixels);
-        const int px = pixel % E.F.width, py = pixel / E.F.width;
-        if (path_start(E.F, E.J, p, px, py, E.sample_base + pass, cnt)) {
-          active = true;
-          need_new = false;
-          emit = 1u;
-        } else {
-          P.sbuf[item] = path_output(E.F, p);
-        }
-      }
-    }
-  }
-  // append the next segments as 32-byte ray records {o.xyz, d.x} {d.yz,
-  // slot << 1 | kind, job}: the warp's extension records first, then its
-  // shadow records; a primary ray starts at its volume entry point
-  const uint32_t n1 = (emit & 1u) ? 1u : 0u, n2 = (emit & 2u) ? 1u : 0u;
-  const unsigned b1 = __ballot_sync(FULL, n1), b2 = __ballot_sync(FULL, n2);
-  const uint32_t tot = __popc(b1) + __popc(b2);
-  if (tot) {
+  append_segments(P, par, emit, slot, job, p.ro, p);
+  // free slots, warp-aggregated into the free list
+  const unsigned want = __ballot_sync(FULL, need_new);
+  if (want) {
     uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&P.ctl[4 * par], tot);
+    if (lane == 0) base = atomicAdd(&P.ctl[4 * par + 3], (uint32_t)__popc(want));
     base = __shfl_sync(FULL, base, 0);
-    float4* q = P.queue[par];
-    if (n1) {
-      v3 o = p.ro;
-      if (p.primary) {
-        const Frame& F = job_entry(P, T, job).F;
-        o = primary_origin(p.ro, p.rd, ld3(F.bmin), ld3(F.bmax));
-      }
-      const size_t at = 2 * (size_t)(base + __popc(b1 & lt));
-      q[at] = make_float4(o.x, o.y, o.z, p.rd.x);
-      q[at + 1] = make_float4(p.rd.y, p.rd.z, __uint_as_float((uint32_t)slot << 1), __uint_as_float(job));
-    }
-    if (n2) {
-      const size_t at = 2 * (size_t)(base + __popc(b1) + __popc(b2 & lt));
-      q[at] = make_float4(p.ro.x, p.ro.y, p.ro.z, p.sd.x);
-      q[at + 1] = make_float4(p.sd.y, p.sd.z, __uint_as_float(((uint32_t)slot << 1) | 1u), __uint_as_float(job));
-    }
+    if (need_new) P.free_slots[base + __popc(want & lt)] = (uint32_t)slot;
   }
-  if (in_range) {
-    uint32_t nf;
-    if (active) {
-      store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
-      nf = SL_ACTIVE | (uint32_t)(p.bounces & 0xff) | (p.primary ? SL_PRIMARY : 0u) |
-           (p.has_cont ? SL_HAS_CONT : 0u) | ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u) |
-           ((uint32_t)(p.nee_nf & 7) << 14);
-    } else {
-      nf = dead ? SL_DEAD : 0u;
-    }
-    P.st.flags[slot] = nf;
+  if (active) {
+    store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
+    P.st.flags[slot] = slot_flags(p, emit);
   }
   const unsigned live = __ballot_sync(FULL, active);
   if (lane == 0 && live) atomicAdd(&P.ctl[4 * par + 2], (uint32_t)__popc(live));
+  flush_counters(cnt, P.counters);
+}
+
+// New paths for the slots on the free list: each lane takes items
+// (warp-aggregated) until one enters its job's volume or the items run out;
+// a path that misses the volume is finished at once.  The primary segment
+// starts at the volume entry point.  A grid-stride loop over whole warps.
+template <bool kCount, class Tab>
+__global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __grid_constant__ Tab T, int par) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const uint32_t n_free = *(volatile uint32_t*)&P.ctl[4 * par + 3];
+  Cnt<kCount> cnt;
+#pragma unroll
+  for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t w = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w < n_free; w += stride) {
+    const uint32_t i = w + (uint32_t)lane;
+    const bool mine = i < n_free;
+    const int slot = mine ? (int)P.free_slots[i] : 0;
+    bool need_new = mine, active = false, dead = false;
+    Path p;
+    uint32_t job = 0, item = 0;
+    for (;;) {
+      const unsigned want = __ballot_sync(FULL, need_new);
+      if (!want) break;
+      const int leader = __ffs(want) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(P.next_item, (unsigned long long)__popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      if (need_new) {
+        const unsigned long long my = base + __popc(want & lt);
+        if (my >= P.n_items) {
+          need_new = false;
+          dead = true;
+        } else {
+          item = (uint32_t)my;
+          job = (uint32_t)job_of(P, T, my);
+          const JobEntry& E = job_entry(P, T, job);
+          const long long r = (long long)my - (long long)E.tile_begin;
+          const int pass = (int)(r / E.n_pixels);
+          const int pixel = (int)(r - (long long)pass * E.n_pixels);
+          const int px = pixel % E.F.width, py = pixel / E.F.width;
+          if (path_start(E.F, E.J, p, px, py, E.sample_base + pass, cnt)) {
+            active = true;
+            need_new = false;
+          } else {
+            P.sbuf[item] = path_output(E.F, p);
+          }
+        }
+      }
+    }
+    v3 o = p.ro;
+    if (active) {
+      const Frame& F = job_entry(P, T, job).F;
+      o = primary_origin(p.ro, p.rd, ld3(F.bmin), ld3(F.bmax));
+    }
+    append_segments(P, par, active ? 1u : 0u, slot, job, o, p);
+    if (active) {
+      store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
+      P.st.flags[slot] = slot_flags(p, 1u);
+    } else if (mine) {
+      P.st.flags[slot] = dead ? SL_DEAD : 0u;
+    }
+    const unsigned live = __ballot_sync(FULL, active);
+    if (lane == 0 && live) atomicAdd(&P.ctl[4 * par + 2], (uint32_t)__popc(live));
+  }
   flush_counters(cnt, P.counters);
 }
 
@@ -368,15 +410,21 @@ __global__ void k_wf_accumulate(const JobEntry* jobs, const float4* sbuf) {
 }
 
 template <class Tab>
-static void wf_shade(const WfParams& P, const Tab& T, int par, bool count, cudaStream_t st) {
+static void wf_shade(const WfParams& P, const Tab& T, int par, int regen_blocks, bool count, cudaStream_t st) {
   const int blocks = (P.n_slots + 127) / 128;
-  if (count) k_wf_shade<true, Tab><<<blocks, 128, 0, st>>>(P, T, par);
-  else k_wf_shade<false, Tab><<<blocks, 128, 0, st>>>(P, T, par);
+  if (count) {
+    k_wf_shade<true, Tab><<<blocks, 128, 0, st>>>(P, T, par);
+    k_wf_regen<true, Tab><<<regen_blocks, 128, 0, st>>>(P, T, par);
+  } else {
+    k_wf_shade<false, Tab><<<blocks, 128, 0, st>>>(P, T, par);
+    k_wf_regen<false, Tab><<<regen_blocks, 128, 0, st>>>(P, T, par);
+  }
 }
 
-cudaError_t launch_wf_shade(const WfParams& P, int par, bool count, cudaStream_t st, const WfJobTable* T) {
-  if (T && P.n_jobs <= kWfParamJobs) wf_shade(P, *T, par, count, st);
-  else wf_shade(P, WfNoTable{0}, par, count, st);
+cudaError_t launch_wf_shade(const WfParams& P, int par, int regen_blocks, bool count, cudaStream_t st,
+                            const WfJobTable* T) {
+  if (T && P.n_jobs <= kWfParamJobs) wf_shade(P, *T, par, regen_blocks, count, st);
+  else wf_shade(P, WfNoTable{0}, par, regen_blocks, count, st);
   return cudaGetLastError();
 }
 
