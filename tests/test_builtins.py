@@ -38,6 +38,11 @@ def test_pow(orc):
     # gamma of the tonemapper and Schlick's fifth power
     g = orc.builtins(2, np.float32([0.0, 1.0, 2.0, 1e-3]), np.float32([1 / 2.2] * 4))
     np.testing.assert_allclose(g, np.power([0.0, 1.0, 2.0, 1e-3], 1 / 2.2), rtol=1e-6)
+    # the fifth power is three products, within 3 ulp
+    x5 = rng.uniform(1e-3, 1.0, 10000).astype(np.float32)
+    got5 = orc.builtins(2, x5, np.full_like(x5, 5.0)).astype(np.float64)
+    want5 = x5.astype(np.float64) ** 5
+    assert np.all(np.abs(got5 - want5) <= 3 * np.spacing(want5.astype(np.float32)).astype(np.float64))
     # conventions where GLSL leaves pow undefined
     assert orc.builtins(2, np.float32([-0.5, 0.0, -2.0]), np.float32([5.0, 3.0, 0.0])).tolist() == [0.0, 0.0, 1.0]
 

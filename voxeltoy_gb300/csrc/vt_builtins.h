@@ -17,7 +17,7 @@
 //   log2      exponent/mantissa split, mantissa in [sqrt(1/2), sqrt(2)),
 //             ln(m) = 2 atanh((m-1)/(m+1)) by its odd power series.
 //   exp2      2^y = 2^k * e^(f ln 2), k = rint(y), Taylor series of e^x.
-//   pow       exp2(y * log2(x)).
+//   pow       exp2(y * log2(x)); y == 5 (Schlick) as (x*x)^2 * x.
 //   atan      reduction to [0, tan(pi/12)] by the identities
 //             atan(t) = pi/2 - atan(1/t) and
 //             atan(t) = pi/6 + atan((sqrt(3) t - 1) / (sqrt(3) + t))
@@ -173,6 +173,10 @@ VT_HD float vpow(float x, float y) {
   if (y == 0.0f) return 1.0f;
   if (!(x > 0.0f)) return 0.0f;
   if (x == 1.0f) return 1.0f;
+  if (y == 5.0f) {                 // Schlick's fifth power: three correctly rounded products
+    const float x2 = x * x;
+    return (x2 * x2) * x;
+  }
   return vexp2(y * vlog2(x));
 }
 

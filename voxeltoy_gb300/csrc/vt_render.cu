@@ -132,8 +132,8 @@ __device__ __forceinline__ int job_of(const WfParams& P, const Tab& T, unsigned 
 }
 
 // Slot state layout: a0 = (ro, job), a1 = (rd, item), a2 = (sd, light),
-// a3 = (L, rng), a4 = (T, bsdf_pdf), a5 = (nee_P, -); pixel and sample are
-// derived from the item; bounces and flag bits live in `flags`.
+// a3 = (L, rng), a4 = (T, bsdf_pdf), a5 = (nee_P, sample); the pixel is
+// derived from the item and sample; bounces and flag bits live in `flags`.
 __device__ __forceinline__ void load_path(const WfSlots& st, int slot, uint32_t fl, const JobEntry& E, uint32_t item,
                                           Path& p) {
   const float4 a0 = st.a0[slot], a1 = st.a1[slot], a2 = st.a2[slot];
@@ -148,11 +148,12 @@ __device__ __forceinline__ void load_path(const WfSlots& st, int slot, uint32_t 
   p.primary = (fl & SL_PRIMARY) ? 1 : 0;
   p.has_cont = (fl & SL_HAS_CONT) ? 1 : 0;
   p.nee_nf = (int)((fl >> 14) & 7u);
-  const long long r = (long long)item - E.tile_begin;
-  const long long pass = r / E.n_pixels;
+  // item - tile_begin = pass * n_pixels + pixel (< 2^32 items per launch)
+  const uint32_t sample = __float_as_uint(a5.w);
+  const uint32_t pass = sample - (uint32_t)E.sample_base;
   const uint32_t rng = __float_as_uint(a3.w);
-  p.rng.pixel = (uint32_t)(r - pass * E.n_pixels);
-  p.rng.sample = (uint32_t)(E.sample_base + pass);
+  p.rng.pixel = (item - (uint32_t)E.tile_begin) - pass * (uint32_t)E.n_pixels;
+  p.rng.sample = sample;
   if (E.F.rng_mode == 1) { p.rng.ox = (int32_t)(rng & 0xffffu); p.rng.oy = (int32_t)(rng >> 16); p.rng.call = 0; }
   else { p.rng.call = rng; p.rng.ox = p.rng.oy = 0; }
 }
@@ -165,7 +166,7 @@ __device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Fr
   st.a2[slot] = pack4(p.sd, __int_as_float(p.light));
   st.a3[slot] = pack4(p.L, __uint_as_float(rng));
   st.a4[slot] = pack4(p.T, p.bsdf_pdf);
-  st.a5[slot] = pack4(p.nee_P, 0.0f);
+  st.a5[slot] = pack4(p.nee_P, __uint_as_float(p.rng.sample));
 }
 
 // Append this warp's next segments to queue[par] as 32-byte ray records
@@ -285,6 +286,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
     bool need_new = mine, active = false, dead = false;
     Path p;
     uint32_t job = 0, item = 0;
+    float t_enter = 0.0f;
     for (;;) {
       const unsigned want = __ballot_sync(FULL, need_new);
       if (!want) break;
@@ -301,11 +303,13 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
           item = (uint32_t)my;
           job = (uint32_t)job_of(P, T, my);
           const JobEntry& E = job_entry(P, T, job);
-          const long long r = (long long)my - (long long)E.tile_begin;
-          const int pass = (int)(r / E.n_pixels);
-          const int pixel = (int)(r - (long long)pass * E.n_pixels);
-          const int px = pixel % E.F.width, py = pixel / E.F.width;
-          if (path_start(E.F, E.J, p, px, py, E.sample_base + pass, cnt)) {
+          const uint32_t r = (uint32_t)(my - (unsigned long long)E.tile_begin);   // < 2^32 items per launch
+          const uint32_t np = (uint32_t)E.n_pixels;
+          const uint32_t pass = r / np;
+          const uint32_t pixel = r - pass * np;
+          const uint32_t w = (uint32_t)E.F.width;
+          const int py = (int)(pixel / w), px = (int)(pixel - (uint32_t)py * w);
+          if (path_start(E.F, E.J, p, px, py, E.sample_base + (int)pass, cnt, t_enter)) {
             active = true;
             need_new = false;
           } else {
@@ -314,11 +318,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
         }
       }
     }
-    v3 o = p.ro;
-    if (active) {
-      const Frame& F = job_entry(P, T, job).F;
-      o = primary_origin(p.ro, p.rd, ld3(F.bmin), ld3(F.bmax));
-    }
+    const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
     append_segments(P, par, active ? 1u : 0u, slot, job, o, p);
     if (active) {
       store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);

@@ -628,9 +628,10 @@ VT_D float4 path_output(const Frame& F, const Path& p) {
 
 // main() up to the primary traversal (pathTracer.fs:172-196).  Returns true
 // if the primary ray enters the volume; its segment then starts at
-// ro + t*rd with t = ray_aabb(ro, rd, bounds) (see primary_origin).
+// ro + t_enter*rd with t_enter = ray_aabb(ro, rd, bounds).
 template <bool kCount>
-VT_D bool path_start(const Frame& F, const JobDev& J, Path& p, int px, int py, int sample, Cnt<kCount>& cnt) {
+VT_D bool path_start(const Frame& F, const JobDev& J, Path& p, int px, int py, int sample, Cnt<kCount>& cnt,
+                     float& t_enter) {
   rng_init(F, p.rng, px, py, sample);
   cnt.add(C_PATHS, 1);
   p.L = mk3(0.0f, 0.0f, 0.0f);
@@ -648,17 +649,13 @@ VT_D bool path_start(const Frame& F, const JobDev& J, Path& p, int px, int py, i
   p.rd = d;
   p.sd = d;
   const float t = ray_aabb(o, d, ld3(F.bmin), ld3(F.bmax));
+  t_enter = t;
   if (t < 0.0f) {
     p.L = background(F, J, d, cnt);
     return false;
   }
   cnt.add(C_SEGMENTS, 1);
   return true;
-}
-// Volume entry point of the primary ray (pathTracer.fs:196).
-VT_D v3 primary_origin(v3 o, v3 d, v3 bmin, v3 bmax) {
-  const float t = ray_aabb(o, d, bmin, bmax);
-  return o + t * d;
 }
 
 // directLighting (pathTracer.fs:64-170) up to the shadow ray: picks a light,
@@ -821,8 +818,9 @@ VT_D float4 trace_sample(const Frame& F, const JobDev& J, int px, int py, int sa
   Path p;
   Dda s;
   if (first_hit) { first_hit->x = -1; first_hit->y = -1; first_hit->z = -1; first_hit->flags = 0; }
-  if (!path_start(F, J, p, px, py, sample, cnt)) return path_output(F, p);
-  dda_begin(g, s, primary_origin(p.ro, p.rd, ld3(F.bmin), ld3(F.bmax)), p.rd);
+  float t_enter;
+  if (!path_start(F, J, p, px, py, sample, cnt, t_enter)) return path_output(F, p);
+  dda_begin(g, s, p.ro + t_enter * p.rd, p.rd);
   if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
   if (first_hit) {
     const bool h = dda_hit(F, s);
