@@ -1085,7 +1085,7 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     ctx->sbuf_items = items;
   }
   if (!ctx->wf_ctl) {
-    int rc = ctx->alloc((void**)&ctx->wf_ctl, 64);
+    int rc = ctx->alloc((void**)&ctx->wf_ctl, kCtlBytes);
     if (rc != VT_OK) return rc;
   }
   if (!ctx->h_live) {
@@ -1144,7 +1144,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   P.queue[0] = qmem;
   P.queue[1] = qmem + 4 * ctx->wf_slots;
   P.ctl = ctx->wf_ctl;
-  P.next_item = (unsigned long long*)(ctx->wf_ctl + 8);
+  P.next_item = (unsigned long long*)(ctx->wf_ctl + kCtlNextItem);
   P.free_slots = P.st.flags + ctx->wf_slots;
   P.n_items = (unsigned long long)items;
   P.sbuf = ctx->sbuf;
@@ -1160,19 +1160,21 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     T = &table;
   }
   VT_CUDA(cudaMemsetAsync(P.st.flags, 0, sizeof(uint32_t) * (size_t)slots, st), "slot flags");
-  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, 64, st), "wavefront control");
+  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, kCtlBytes, st), "wavefront control");
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
   const int bps = blocks_per_sm > 0 ? blocks_per_sm
                                     : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
   const int trace_blocks = ctx->sm_count * bps;
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
-    VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + 4 * par, 0, 4 * sizeof(uint32_t), st), "round counters");
+    VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + ctl_index(par, 0), 0, 4 * kCtlStride * sizeof(uint32_t), st),
+            "round counters");
     VT_CUDA(launch_wf_shade(P, par, ctx->sm_count * 8, count, st, T), "wavefront shade");
     VT_CUDA(launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st, T), "wavefront trace");
     ctx->launches += 3;
     if ((iter & 7) == 7) {
-      VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + 4 * par + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st),
+      VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + ctl_index(par, CTL_LIVE), sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, st),
               "live count");
       VT_CUDA(cudaStreamSynchronize(st), "wavefront round");
       if (*(volatile uint32_t*)ctx->h_live == 0) break;

@@ -2,8 +2,8 @@
 // working memory in one file-scope device array instead of context buffers.
 //
 // Layout of the array (every part starts on a 256-byte boundary):
-//   control     16 words: per parity {queue count, queue head, live, -}, then
-//               the 64-bit next-item counter at word 8 (must start at zero)
+//   control     the wavefront control words (kCtlBytes, one 128-byte line
+//               per counter; must start at zero)
 //   job table   VT_FIXED_MAX_JOBS JobEntry records
 //   grid table  VT_FIXED_MAX_JOBS Grid records
 //   path slots  VT_FIXED_MAX_PATH_SLOTS x (six float4 of state, two int4
@@ -26,7 +26,7 @@ constexpr size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 constexpr size_t kSlotBytes = 6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 2 * sizeof(uint32_t);
 constexpr size_t kCtlOff = 0;
-constexpr size_t kJobsOff = kCtlOff + 256;
+constexpr size_t kJobsOff = kCtlOff + round256(kCtlBytes);
 constexpr size_t kGridsOff = kJobsOff + round256(sizeof(JobEntry) * VT_FIXED_MAX_JOBS);
 constexpr size_t kSlotsOff = kGridsOff + round256(sizeof(Grid) * VT_FIXED_MAX_JOBS);
 constexpr size_t kSamplesOff = kSlotsOff + round256(kSlotBytes * (size_t)VT_FIXED_MAX_PATH_SLOTS);
@@ -96,7 +96,7 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   P.free_slots = P.st.flags + S;
   P.n_slots = (int32_t)slots;
   P.ctl = ctl;
-  P.next_item = (unsigned long long*)(ctl + 8);
+  P.next_item = (unsigned long long*)(ctl + kCtlNextItem);
   P.n_items = (unsigned long long)items;
   P.sbuf = (float4*)(base + kSamplesOff);
   P.counters = nullptr;
@@ -107,14 +107,14 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   if (e != cudaSuccess) return cuda_fail(e, "fixed grid table");
   e = cudaMemsetAsync(P.st.flags, 0, sizeof(uint32_t) * (size_t)slots, st);
   if (e != cudaSuccess) return cuda_fail(e, "fixed slot flags");
-  e = cudaMemsetAsync(ctl, 0, 64, st);
+  e = cudaMemsetAsync(ctl, 0, kCtlBytes, st);
   if (e != cudaSuccess) return cuda_fail(e, "fixed control words");
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
   const int bps = ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy;
   const int trace_blocks = ctx->sm_count * bps;
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
-    e = cudaMemsetAsync(ctl + 4 * par, 0, 4 * sizeof(uint32_t), st);
+    e = cudaMemsetAsync(ctl + ctl_index(par, 0), 0, 4 * kCtlStride * sizeof(uint32_t), st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed round counters");
     e = launch_wf_shade(P, par, ctx->sm_count * 8, false, st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed wavefront shade");
@@ -123,7 +123,7 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
     ctx->launches += 3;
     if ((iter & 7) == 7) {
       uint32_t live = 0;   // pageable: the copy has completed when it returns
-      e = cudaMemcpyAsync(&live, ctl + 4 * par + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+      e = cudaMemcpyAsync(&live, ctl + ctl_index(par, CTL_LIVE), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) return cuda_fail(e, "fixed live count");
       if (live == 0) break;

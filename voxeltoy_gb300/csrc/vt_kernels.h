@@ -35,6 +35,17 @@ struct WfSlots {
   uint32_t* flags; // bounces | primary | has_cont | ext | shadow | active | dead
   int4* hits;      // [2][n_slots] segment ends: extension, shadow
 };
+// Control words of a wavefront launch.  Per parity: entries appended to the
+// queue, entries taken by the tracer, active slots after shade + regen,
+// entries appended to the free list; then the 64-bit item counter.  Each
+// word has its own 128-byte line, so atomics on different counters never
+// queue behind each other in one L2 sector.
+enum { CTL_QCOUNT = 0, CTL_QHEAD = 1, CTL_LIVE = 2, CTL_FREE = 3 };
+constexpr int kCtlStride = 32;                                   // words per counter line
+constexpr int kCtlNextItem = 8 * kCtlStride;                     // word index of the item counter
+constexpr size_t kCtlBytes = (size_t)9 * kCtlStride * sizeof(uint32_t);
+__host__ __device__ constexpr int ctl_index(int par, int k) { return (4 * par + k) * kCtlStride; }
+
 struct WfParams {
   const JobEntry* jobs;            // device array, tile_begin = first item of the job
   int32_t n_jobs;
@@ -43,10 +54,7 @@ struct WfParams {
   int32_t n_slots;
   float4* queue[2];                // segment records, two float4 each:
                                    // {origin.xyz, dir.x} {dir.yz, slot << 1 | kind, job}
-  uint32_t* ctl;                   // per parity i: ctl[4i] entries appended to queue[i],
-                                   // ctl[4i+1] entries taken by the tracer,
-                                   // ctl[4i+2] active slots after the shade and regen,
-                                   // ctl[4i+3] entries appended to free_slots
+  uint32_t* ctl;                   // control words, see ctl_index
   uint32_t* free_slots;            // slots that need a new path (n_slots entries)
   unsigned long long* next_item;
   unsigned long long n_items;

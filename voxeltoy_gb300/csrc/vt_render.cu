@@ -169,20 +169,55 @@ __device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Fr
   st.a5[slot] = pack4(p.nee_P, __uint_as_float(p.rng.sample));
 }
 
-// Append this warp's next segments to queue[par] as 32-byte ray records
-// {o.xyz, d.x} {d.yz, slot << 1 | kind, job}: the warp's extension records
-// first, then its shadow records.  emit: 1 extension (from `ext_o`), 2 shadow.
-__device__ __forceinline__ void append_segments(const WfParams& P, int par, uint32_t emit, int slot, uint32_t job,
-                                                v3 ext_o, const Path& p) {
+// Block-wide reservation of queue entries, free-list entries and the live
+// count: one atomic per counter and block instead of per warp.  `nq`, `nf`
+// and `live` are this thread's counts; returns (through qb, fb) the first
+// queue entry and free-list entry of the thread's warp, and the thread's
+// offsets within the warp come from the ballots.  Every thread of the block
+// must call it (two barriers).
+constexpr int kWfWarps = 4;   // warps per shade / regen block (128 threads)
+__device__ __forceinline__ void block_reserve(const WfParams& P, int par, uint32_t nq, uint32_t nf, uint32_t nl,
+                                              uint32_t& qb, uint32_t& fb) {
+  __shared__ uint32_t s_q[kWfWarps], s_f[kWfWarps], s_l[kWfWarps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t q = nq, f = nf, l = nl;
+  for (int o = 16; o > 0; o >>= 1) {
+    q += __shfl_down_sync(0xffffffffu, q, o);
+    f += __shfl_down_sync(0xffffffffu, f, o);
+    l += __shfl_down_sync(0xffffffffu, l, o);
+  }
+  if (lane == 0) { s_q[warp] = q; s_f[warp] = f; s_l[warp] = l; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t tq = 0, tf = 0, tl = 0;
+    uint32_t pq[kWfWarps], pf[kWfWarps];
+#pragma unroll
+    for (int w = 0; w < kWfWarps; ++w) {
+      pq[w] = tq; pf[w] = tf;
+      tq += s_q[w]; tf += s_f[w]; tl += s_l[w];
+    }
+    const uint32_t bq = tq ? atomicAdd(&P.ctl[ctl_index(par, CTL_QCOUNT)], tq) : 0u;
+    const uint32_t bf = tf ? atomicAdd(&P.ctl[ctl_index(par, CTL_FREE)], tf) : 0u;
+    if (tl) atomicAdd(&P.ctl[ctl_index(par, CTL_LIVE)], tl);
+#pragma unroll
+    for (int w = 0; w < kWfWarps; ++w) { s_q[w] = bq + pq[w]; s_f[w] = bf + pf[w]; }
+  }
+  __syncthreads();
+  qb = s_q[warp];
+  fb = s_f[warp];
+  __syncthreads();   // the next call may overwrite s_q / s_f
+}
+
+// Write this warp's next segments (queue entries from `base`) as 32-byte ray
+// records {o.xyz, d.x} {d.yz, slot << 1 | kind, job}: the warp's extension
+// records first, then its shadow records.  emit: 1 extension (from
+// `ext_o`), 2 shadow.
+__device__ __forceinline__ void write_segments(const WfParams& P, int par, uint32_t base, uint32_t emit, int slot,
+                                               uint32_t job, v3 ext_o, const Path& p) {
   const unsigned FULL = 0xffffffffu;
   const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
   const uint32_t n1 = (emit & 1u) ? 1u : 0u, n2 = (emit & 2u) ? 1u : 0u;
   const unsigned b1 = __ballot_sync(FULL, n1), b2 = __ballot_sync(FULL, n2);
-  const uint32_t tot = __popc(b1) + __popc(b2);
-  if (tot == 0) return;
-  uint32_t base = 0;
-  if ((threadIdx.x & 31) == 0) base = atomicAdd(&P.ctl[4 * par], tot);
-  base = __shfl_sync(FULL, base, 0);
   float4* q = P.queue[par];
   if (n1) {
     const size_t at = 2 * (size_t)(base + __popc(b1 & lt));
@@ -247,21 +282,15 @@ __global__ void __launch_bounds__(128, 8) k_wf_shade(const WfParams P, const __g
       need_new = true;
     }
   }
-  append_segments(P, par, emit, slot, job, p.ro, p);
-  // free slots, warp-aggregated into the free list
+  uint32_t qb, fb;
+  block_reserve(P, par, (emit & 1u) + (emit >> 1), need_new ? 1u : 0u, active ? 1u : 0u, qb, fb);
+  write_segments(P, par, qb, emit, slot, job, p.ro, p);
   const unsigned want = __ballot_sync(FULL, need_new);
-  if (want) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(&P.ctl[4 * par + 3], (uint32_t)__popc(want));
-    base = __shfl_sync(FULL, base, 0);
-    if (need_new) P.free_slots[base + __popc(want & lt)] = (uint32_t)slot;
-  }
+  if (need_new) P.free_slots[fb + __popc(want & lt)] = (uint32_t)slot;
   if (active) {
     store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
     P.st.flags[slot] = slot_flags(p, emit);
   }
-  const unsigned live = __ballot_sync(FULL, active);
-  if (lane == 0 && live) atomicAdd(&P.ctl[4 * par + 2], (uint32_t)__popc(live));
   flush_counters(cnt, P.counters);
 }
 
@@ -274,28 +303,27 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const uint32_t n_free = *(volatile uint32_t*)&P.ctl[4 * par + 3];
+  __shared__ unsigned long long s_item;
+  const uint32_t n_free = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_FREE)];
   Cnt<kCount> cnt;
 #pragma unroll
   for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t w = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w < n_free; w += stride) {
-    const uint32_t i = w + (uint32_t)lane;
+  for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n_free; b0 += stride) {   // block-uniform
+    const uint32_t i = b0 + threadIdx.x;
     const bool mine = i < n_free;
     const int slot = mine ? (int)P.free_slots[i] : 0;
+    // one item per listed slot, claimed for the whole block with one atomic
+    if (threadIdx.x == 0) s_item = atomicAdd(P.next_item, (unsigned long long)min(blockDim.x, n_free - b0));
+    __syncthreads();
+    unsigned long long my = s_item + threadIdx.x;
+    __syncthreads();
     bool need_new = mine, active = false, dead = false;
     Path p;
     uint32_t job = 0, item = 0;
     float t_enter = 0.0f;
     for (;;) {
-      const unsigned want = __ballot_sync(FULL, need_new);
-      if (!want) break;
-      const int leader = __ffs(want) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(P.next_item, (unsigned long long)__popc(want));
-      base = __shfl_sync(FULL, base, leader);
       if (need_new) {
-        const unsigned long long my = base + __popc(want & lt);
         if (my >= P.n_items) {
           need_new = false;
           dead = true;
@@ -313,21 +341,28 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
             active = true;
             need_new = false;
           } else {
-            P.sbuf[item] = path_output(E.F, p);
+            P.sbuf[item] = path_output(E.F, p);   // missed the volume: finished, take another item
           }
         }
       }
+      const unsigned want = __ballot_sync(FULL, need_new);
+      if (!want) break;
+      const int leader = __ffs(want) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(P.next_item, (unsigned long long)__popc(want));
+      base = __shfl_sync(FULL, base, leader);
+      my = base + __popc(want & lt);
     }
     const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
-    append_segments(P, par, active ? 1u : 0u, slot, job, o, p);
+    uint32_t qb, fb;
+    block_reserve(P, par, active ? 1u : 0u, 0u, active ? 1u : 0u, qb, fb);
+    write_segments(P, par, qb, active ? 1u : 0u, slot, job, o, p);
     if (active) {
       store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
       P.st.flags[slot] = slot_flags(p, 1u);
     } else if (mine) {
       P.st.flags[slot] = dead ? SL_DEAD : 0u;
     }
-    const unsigned live = __ballot_sync(FULL, active);
-    if (lane == 0 && live) atomicAdd(&P.ctl[4 * par + 2], (uint32_t)__popc(live));
   }
   flush_counters(cnt, P.counters);
 }
@@ -344,7 +379,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const uint32_t n = *(volatile uint32_t*)&P.ctl[4 * par];
+  const uint32_t n = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_QCOUNT)];
   if (n == 0) return;
   const float4* q = P.queue[par];
   Cnt<kCount> cnt;
@@ -369,7 +404,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
     while (need && !exhausted) {          // prefetch next records
       if (pool >= pool_end) {
         uint32_t c = 0;
-        if (lane == 0) c = atomicAdd(&P.ctl[4 * par + 1], kTraceChunk);
+        if (lane == 0) c = atomicAdd(&P.ctl[ctl_index(par, CTL_QHEAD)], kTraceChunk);
         c = __shfl_sync(FULL, c, 0);
         if (c >= n) { exhausted = true; break; }
         pool = c;

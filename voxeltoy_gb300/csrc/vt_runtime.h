@@ -34,7 +34,7 @@ struct vt_context {
   int64_t wf_slots = 0;
   float4* sbuf = nullptr;        // per-sample outputs of one launch
   int64_t sbuf_items = 0;
-  uint32_t* wf_ctl = nullptr;    // [2][4] qcount, qhead, live, pad + next_item
+  uint32_t* wf_ctl = nullptr;    // control words (kCtlBytes, layout of ctl_index)
   uint32_t* h_live = nullptr;    // pinned host copy of a live counter
   int64_t max_slots = 1 << 23;   // path slots per launch
   int64_t max_items = 1 << 28;   // samples per launch (sample buffer entries)
