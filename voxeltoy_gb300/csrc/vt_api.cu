@@ -1069,9 +1069,10 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     ctx->release(ctx->wf_mem);
     ctx->wf_mem = nullptr;
     ctx->wf_slots = 0;
-    // six float4 of state, two int4 segment ends, two queues of 2 records x 32 B, flags, free list
+    // six float4 of state, two int4 segment ends, two queues of 2 records x 32 B, flags, free list,
+    // hit list
     const size_t bytes =
-        (size_t)slots * (6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 2 * sizeof(uint32_t));
+        (size_t)slots * (6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 3 * sizeof(uint32_t));
     int rc = ctx->alloc(&ctx->wf_mem, bytes);
     if (rc != VT_OK) return rc;
     ctx->wf_slots = slots;
@@ -1146,6 +1147,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   P.ctl = ctx->wf_ctl;
   P.next_item = (unsigned long long*)(ctx->wf_ctl + kCtlNextItem);
   P.free_slots = P.st.flags + ctx->wf_slots;
+  P.hit_slots = P.free_slots + ctx->wf_slots;
   P.n_items = (unsigned long long)items;
   P.sbuf = ctx->sbuf;
   P.counters = count ? ctx->d_counters : nullptr;
@@ -1167,11 +1169,11 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   const int trace_blocks = ctx->sm_count * bps;
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
-    VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + ctl_index(par, 0), 0, 4 * kCtlStride * sizeof(uint32_t), st),
+    VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t), st),
             "round counters");
     VT_CUDA(launch_wf_shade(P, par, ctx->sm_count * 8, count, st, T), "wavefront shade");
     VT_CUDA(launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st, T), "wavefront trace");
-    ctx->launches += 3;
+    ctx->launches += 4;
     if ((iter & 7) == 7) {
       VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + ctl_index(par, CTL_LIVE), sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, st),

@@ -8,7 +8,8 @@
 //   grid table  VT_FIXED_MAX_JOBS Grid records
 //   path slots  VT_FIXED_MAX_PATH_SLOTS x (six float4 of state, two int4
 //               segment ends, two queues of two 32-byte records, a flag word,
-//               a free-list entry); the flags must start at zero
+//               a free-list entry, a hit-list entry); the flags must start at
+//               zero
 //   samples     VT_FIXED_MAX_SAMPLES float4 per-sample outputs
 // The kernels are the ones vt_render_batch runs; only where their buffers
 // live differs, so results are bit-identical.
@@ -24,7 +25,7 @@ namespace {
 
 constexpr size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-constexpr size_t kSlotBytes = 6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 2 * sizeof(uint32_t);
+constexpr size_t kSlotBytes = 6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 3 * sizeof(uint32_t);
 constexpr size_t kCtlOff = 0;
 constexpr size_t kJobsOff = kCtlOff + round256(kCtlBytes);
 constexpr size_t kGridsOff = kJobsOff + round256(sizeof(JobEntry) * VT_FIXED_MAX_JOBS);
@@ -94,6 +95,7 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   P.queue[1] = P.queue[0] + 4 * S;
   P.st.flags = (uint32_t*)(P.queue[1] + 4 * S);
   P.free_slots = P.st.flags + S;
+  P.hit_slots = P.free_slots + S;
   P.n_slots = (int32_t)slots;
   P.ctl = ctl;
   P.next_item = (unsigned long long*)(ctl + kCtlNextItem);
@@ -114,13 +116,13 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   const int trace_blocks = ctx->sm_count * bps;
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
-    e = cudaMemsetAsync(ctl + ctl_index(par, 0), 0, 4 * kCtlStride * sizeof(uint32_t), st);
+    e = cudaMemsetAsync(ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t), st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed round counters");
     e = launch_wf_shade(P, par, ctx->sm_count * 8, false, st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed wavefront shade");
     e = launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, false, st);
     if (e != cudaSuccess) return cuda_fail(e, "fixed wavefront trace");
-    ctx->launches += 3;
+    ctx->launches += 4;
     if ((iter & 7) == 7) {
       uint32_t live = 0;   // pageable: the copy has completed when it returns
       e = cudaMemcpyAsync(&live, ctl + ctl_index(par, CTL_LIVE), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);

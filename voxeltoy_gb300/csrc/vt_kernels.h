@@ -36,15 +36,17 @@ struct WfSlots {
   int4* hits;      // [2][n_slots] segment ends: extension, shadow
 };
 // Control words of a wavefront launch.  Per parity: entries appended to the
-// queue, entries taken by the tracer, active slots after shade + regen,
-// entries appended to the free list; then the 64-bit item counter.  Each
+// queue, entries taken by the tracer, active slots after the round, entries
+// appended to the free list, Lambert and other entries of the hit list; then
+// the 64-bit item counter.  Each
 // word has its own 128-byte line, so atomics on different counters never
 // queue behind each other in one L2 sector.
-enum { CTL_QCOUNT = 0, CTL_QHEAD = 1, CTL_LIVE = 2, CTL_FREE = 3 };
+enum { CTL_QCOUNT = 0, CTL_QHEAD = 1, CTL_LIVE = 2, CTL_FREE = 3, CTL_HITS_LAMBERT = 4, CTL_HITS_OTHER = 5,
+       CTL_PER_PARITY = 8 };
 constexpr int kCtlStride = 32;                                   // words per counter line
-constexpr int kCtlNextItem = 8 * kCtlStride;                     // word index of the item counter
-constexpr size_t kCtlBytes = (size_t)9 * kCtlStride * sizeof(uint32_t);
-__host__ __device__ constexpr int ctl_index(int par, int k) { return (4 * par + k) * kCtlStride; }
+constexpr int kCtlNextItem = 2 * CTL_PER_PARITY * kCtlStride;    // word index of the item counter
+constexpr size_t kCtlBytes = (size_t)(2 * CTL_PER_PARITY + 1) * kCtlStride * sizeof(uint32_t);
+__host__ __device__ constexpr int ctl_index(int par, int k) { return (CTL_PER_PARITY * par + k) * kCtlStride; }
 
 struct WfParams {
   const JobEntry* jobs;            // device array, tile_begin = first item of the job
@@ -56,6 +58,7 @@ struct WfParams {
                                    // {origin.xyz, dir.x} {dir.yz, slot << 1 | kind, job}
   uint32_t* ctl;                   // control words, see ctl_index
   uint32_t* free_slots;            // slots that need a new path (n_slots entries)
+  uint32_t* hit_slots;             // hits to shade: Lambert from the front, others from the back
   unsigned long long* next_item;
   unsigned long long n_items;
   float4* sbuf;                    // per-item sample outputs
@@ -69,9 +72,9 @@ struct WfJobTable {
   JobEntry e[kWfParamJobs];
   Grid g[kWfParamJobs];
 };
-// k_wf_shade over every slot, then k_wf_regen (regen_blocks blocks of 128)
-// over the free list it leaves.
-cudaError_t launch_wf_shade(const WfParams& P, int par, int regen_blocks, bool count, cudaStream_t st,
+// k_wf_shade over every slot, then k_wf_hit over the hit list and
+// k_wf_regen over the free list it leaves (persist_blocks blocks of 128).
+cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool count, cudaStream_t st,
                             const WfJobTable* T = nullptr);
 cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,
                             const WfJobTable* T = nullptr);

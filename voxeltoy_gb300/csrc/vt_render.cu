@@ -169,43 +169,36 @@ __device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Fr
   st.a5[slot] = pack4(p.nee_P, __uint_as_float(p.rng.sample));
 }
 
-// Block-wide reservation of queue entries, free-list entries and the live
-// count: one atomic per counter and block instead of per warp.  `nq`, `nf`
-// and `live` are this thread's counts; returns (through qb, fb) the first
-// queue entry and free-list entry of the thread's warp, and the thread's
-// offsets within the warp come from the ballots.  Every thread of the block
-// must call it (two barriers).
-constexpr int kWfWarps = 4;   // warps per shade / regen block (128 threads)
-__device__ __forceinline__ void block_reserve(const WfParams& P, int par, uint32_t nq, uint32_t nf, uint32_t nl,
-                                              uint32_t& qb, uint32_t& fb) {
-  __shared__ uint32_t s_q[kWfWarps], s_f[kWfWarps], s_l[kWfWarps];
+// Block-wide reservation on N counters with one atomic per counter and
+// block instead of per warp: `n[i]` is this thread's count for counter i;
+// returns in base[i] the first entry of the thread's warp (the offsets of
+// the thread within its warp come from ballots).  Every thread of the block
+// must call it (three barriers).
+constexpr int kWfWarps = 4;   // warps per shade / hit / regen block (128 threads)
+template <int N>
+__device__ __forceinline__ void block_reserve(uint32_t* const (&ctr)[N], const uint32_t (&n)[N], uint32_t (&base)[N]) {
+  __shared__ uint32_t s_n[N][kWfWarps];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  uint32_t q = nq, f = nf, l = nl;
-  for (int o = 16; o > 0; o >>= 1) {
-    q += __shfl_down_sync(0xffffffffu, q, o);
-    f += __shfl_down_sync(0xffffffffu, f, o);
-    l += __shfl_down_sync(0xffffffffu, l, o);
-  }
-  if (lane == 0) { s_q[warp] = q; s_f[warp] = f; s_l[warp] = l; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t tq = 0, tf = 0, tl = 0;
-    uint32_t pq[kWfWarps], pf[kWfWarps];
 #pragma unroll
-    for (int w = 0; w < kWfWarps; ++w) {
-      pq[w] = tq; pf[w] = tf;
-      tq += s_q[w]; tf += s_f[w]; tl += s_l[w];
-    }
-    const uint32_t bq = tq ? atomicAdd(&P.ctl[ctl_index(par, CTL_QCOUNT)], tq) : 0u;
-    const uint32_t bf = tf ? atomicAdd(&P.ctl[ctl_index(par, CTL_FREE)], tf) : 0u;
-    if (tl) atomicAdd(&P.ctl[ctl_index(par, CTL_LIVE)], tl);
-#pragma unroll
-    for (int w = 0; w < kWfWarps; ++w) { s_q[w] = bq + pq[w]; s_f[w] = bf + pf[w]; }
+  for (int i = 0; i < N; ++i) {
+    uint32_t v = n[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) s_n[i][warp] = v;
   }
   __syncthreads();
-  qb = s_q[warp];
-  fb = s_f[warp];
-  __syncthreads();   // the next call may overwrite s_q / s_f
+  if (threadIdx.x < N) {
+    const int i = threadIdx.x;
+    uint32_t t = 0, pre[kWfWarps];
+#pragma unroll
+    for (int w = 0; w < kWfWarps; ++w) { pre[w] = t; t += s_n[i][w]; }
+    const uint32_t b0 = t ? atomicAdd(ctr[i], t) : 0u;
+#pragma unroll
+    for (int w = 0; w < kWfWarps; ++w) s_n[i][w] = b0 + pre[w];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < N; ++i) base[i] = s_n[i][warp];
+  __syncthreads();   // the next call may overwrite s_n
 }
 
 // Write this warp's next segments (queue entries from `base`) as 32-byte ray
@@ -236,14 +229,20 @@ __device__ __forceinline__ uint32_t slot_flags(const Path& p, uint32_t emit) {
          ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u) | ((uint32_t)(p.nee_nf & 7) << 14);
 }
 
-// One round of shading: consume the segment results of the previous trace,
-// retire finished paths into the sample buffer, append the next segments to
-// queue[par] and the slots that need a new path to the free list (both
-// warp-aggregated).  New paths are started by k_wf_regen.
-// Eight resident blocks per SM (64 registers): the extra warps hide more of
-// the state-load and instruction-fetch latency than the few spills cost.
+// A round has four kernels:
+//   k_wf_shade  every slot: shadow results, misses (environment), bounce
+//               limit, finished paths -> sample buffer + free list; hits go
+//               to the hit list, Lambert hits from its front, the others
+//               from its back, so that k_wf_hit's warps mostly run one BSDF
+//   k_wf_hit    the hit list: vertex shading, light and BSDF samples, next
+//               segments -> queue
+//   k_wf_regen  the free list: new paths, primary segments -> queue
+//   k_wf_trace  the queue: DDA of every segment
+// k_wf_hit and k_wf_regen keep eight resident blocks per SM (64 registers):
+// the extra warps hide more of the state-load and instruction-fetch latency
+// than the few spills cost; the lighter k_wf_shade fits twelve.
 template <bool kCount, class Tab>
-__global__ void __launch_bounds__(128, 8) k_wf_shade(const WfParams P, const __grid_constant__ Tab T, int par) {
+__global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -253,14 +252,14 @@ __global__ void __launch_bounds__(128, 8) k_wf_shade(const WfParams P, const __g
 #pragma unroll
   for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
   const uint32_t fl = in_range ? P.st.flags[slot] : SL_DEAD;
-  bool active = (fl & SL_ACTIVE) != 0;
+  const bool active = (fl & SL_ACTIVE) != 0;
   bool need_new = !active && !(fl & SL_DEAD);
+  bool hit = false;
+  int cls = 0;
   Path p;
-  uint32_t job = 0, item = 0;
-  uint32_t emit = 0;   // 1: extension, 2: shadow
   if (active) {
-    job = __float_as_uint(P.st.a0[slot].w);
-    item = __float_as_uint(P.st.a1[slot].w);
+    const uint32_t job = __float_as_uint(P.st.a0[slot].w);
+    const uint32_t item = __float_as_uint(P.st.a1[slot].w);
     const JobEntry& E = job_entry(P, T, job);
     load_path(P.st, slot, fl, E, item, p);
     if (fl & SL_SHADOW) {
@@ -268,36 +267,80 @@ __global__ void __launch_bounds__(128, 8) k_wf_shade(const WfParams P, const __g
       SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
       shadow_end(E.F, p, e);
     }
-    bool alive = false;
     if (fl & SL_EXT) {
       const int4 h = P.st.hits[slot];
       SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
-      alive = ext_end(E.F, E.J, p, e, cnt);
+      hit = ext_resolve(E.F, E.J, p, e, cnt);
+      if (hit) cls = hit_class(E.F, E.J, e);
     }
-    if (alive) {
-      emit = 2u | (p.has_cont ? 1u : 0u);
+    if (hit) {
+      // L and the bounce count for k_wf_hit
+      P.st.a3[slot] = make_float4(p.L.x, p.L.y, p.L.z, P.st.a3[slot].w);
+      P.st.flags[slot] = slot_flags(p, 1u);
     } else {
       P.sbuf[item] = path_output(E.F, p);
-      active = false;
       need_new = true;
     }
   }
-  uint32_t qb, fb;
-  block_reserve(P, par, (emit & 1u) + (emit >> 1), need_new ? 1u : 0u, active ? 1u : 0u, qb, fb);
-  write_segments(P, par, qb, emit, slot, job, p.ro, p);
-  const unsigned want = __ballot_sync(FULL, need_new);
-  if (need_new) P.free_slots[fb + __popc(want & lt)] = (uint32_t)slot;
-  if (active) {
-    store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
-    P.st.flags[slot] = slot_flags(p, emit);
+  uint32_t* const ctr[4] = {&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)], &P.ctl[ctl_index(par, CTL_HITS_OTHER)],
+                            &P.ctl[ctl_index(par, CTL_FREE)], &P.ctl[ctl_index(par, CTL_LIVE)]};
+  const uint32_t n[4] = {(hit && cls == 0) ? 1u : 0u, (hit && cls != 0) ? 1u : 0u, need_new ? 1u : 0u, hit ? 1u : 0u};
+  uint32_t base[4];
+  block_reserve<4>(ctr, n, base);
+  const unsigned bl = __ballot_sync(FULL, n[0]), bo = __ballot_sync(FULL, n[1]), bf = __ballot_sync(FULL, n[2]);
+  if (n[0]) P.hit_slots[base[0] + __popc(bl & lt)] = (uint32_t)slot;
+  if (n[1]) P.hit_slots[P.n_slots - 1 - (base[1] + __popc(bo & lt))] = (uint32_t)slot;
+  if (n[2]) P.free_slots[base[2] + __popc(bf & lt)] = (uint32_t)slot;
+  flush_counters(cnt, P.counters);
+}
+
+// Hits kept by k_wf_shade: entries [0, n_lambert) of the hit list, then the
+// other class from the back.  A block-uniform grid-stride loop.
+template <bool kCount, class Tab>
+__global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __grid_constant__ Tab T, int par) {
+  const uint32_t nl = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)];
+  const uint32_t no = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_OTHER)];
+  const uint32_t n_hits = nl + no;
+  Cnt<kCount> cnt;
+#pragma unroll
+  for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n_hits; b0 += stride) {   // block-uniform
+    const uint32_t v = b0 + threadIdx.x;
+    const bool mine = v < n_hits;
+    const int slot = !mine ? 0 : (int)P.hit_slots[v < nl ? v : P.n_slots - 1 - (v - nl)];
+    Path p;
+    uint32_t job = 0, item = 0;
+    uint32_t emit = 0;
+    if (mine) {
+      const uint32_t fl = P.st.flags[slot];
+      job = __float_as_uint(P.st.a0[slot].w);
+      item = __float_as_uint(P.st.a1[slot].w);
+      const JobEntry& E = job_entry(P, T, job);
+      load_path(P.st, slot, fl, E, item, p);
+      const int4 h = P.st.hits[slot];
+      SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
+      ext_hit(E.F, E.J, p, e, cnt);
+      emit = 2u | (p.has_cont ? 1u : 0u);
+    }
+    uint32_t* const ctr[1] = {&P.ctl[ctl_index(par, CTL_QCOUNT)]};
+    const uint32_t n[1] = {(emit & 1u) + (emit >> 1)};
+    uint32_t base[1];
+    block_reserve<1>(ctr, n, base);
+    write_segments(P, par, base[0], emit, slot, job, p.ro, p);
+    if (mine) {
+      store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
+      P.st.flags[slot] = slot_flags(p, emit);
+    }
   }
   flush_counters(cnt, P.counters);
 }
 
-// New paths for the slots on the free list: each lane takes items
-// (warp-aggregated) until one enters its job's volume or the items run out;
-// a path that misses the volume is finished at once.  The primary segment
-// starts at the volume entry point.  A grid-stride loop over whole warps.
+// New paths for the slots on the free list: each lane takes items until one
+// enters its job's volume or the items run out; a path that misses the
+// volume is finished at once.  The primary segment starts at the volume
+// entry point.  A block-uniform grid-stride loop; the first item of every
+// listed slot is claimed for the whole block with one atomic.
 template <bool kCount, class Tab>
 __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
@@ -313,7 +356,6 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
     const uint32_t i = b0 + threadIdx.x;
     const bool mine = i < n_free;
     const int slot = mine ? (int)P.free_slots[i] : 0;
-    // one item per listed slot, claimed for the whole block with one atomic
     if (threadIdx.x == 0) s_item = atomicAdd(P.next_item, (unsigned long long)min(blockDim.x, n_free - b0));
     __syncthreads();
     unsigned long long my = s_item + threadIdx.x;
@@ -354,9 +396,11 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
       my = base + __popc(want & lt);
     }
     const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
-    uint32_t qb, fb;
-    block_reserve(P, par, active ? 1u : 0u, 0u, active ? 1u : 0u, qb, fb);
-    write_segments(P, par, qb, active ? 1u : 0u, slot, job, o, p);
+    uint32_t* const ctr[2] = {&P.ctl[ctl_index(par, CTL_QCOUNT)], &P.ctl[ctl_index(par, CTL_LIVE)]};
+    const uint32_t n[2] = {active ? 1u : 0u, active ? 1u : 0u};
+    uint32_t base[2];
+    block_reserve<2>(ctr, n, base);
+    write_segments(P, par, base[0], active ? 1u : 0u, slot, job, o, p);
     if (active) {
       store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
       P.st.flags[slot] = slot_flags(p, 1u);
@@ -445,21 +489,23 @@ __global__ void k_wf_accumulate(const JobEntry* jobs, const float4* sbuf) {
 }
 
 template <class Tab>
-static void wf_shade(const WfParams& P, const Tab& T, int par, int regen_blocks, bool count, cudaStream_t st) {
+static void wf_shade(const WfParams& P, const Tab& T, int par, int persist_blocks, bool count, cudaStream_t st) {
   const int blocks = (P.n_slots + 127) / 128;
   if (count) {
     k_wf_shade<true, Tab><<<blocks, 128, 0, st>>>(P, T, par);
-    k_wf_regen<true, Tab><<<regen_blocks, 128, 0, st>>>(P, T, par);
+    k_wf_hit<true, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
+    k_wf_regen<true, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
   } else {
     k_wf_shade<false, Tab><<<blocks, 128, 0, st>>>(P, T, par);
-    k_wf_regen<false, Tab><<<regen_blocks, 128, 0, st>>>(P, T, par);
+    k_wf_hit<false, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
+    k_wf_regen<false, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
   }
 }
 
-cudaError_t launch_wf_shade(const WfParams& P, int par, int regen_blocks, bool count, cudaStream_t st,
+cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool count, cudaStream_t st,
                             const WfJobTable* T) {
-  if (T && P.n_jobs <= kWfParamJobs) wf_shade(P, *T, par, regen_blocks, count, st);
-  else wf_shade(P, WfNoTable{0}, par, regen_blocks, count, st);
+  if (T && P.n_jobs <= kWfParamJobs) wf_shade(P, *T, par, persist_blocks, count, st);
+  else wf_shade(P, WfNoTable{0}, par, persist_blocks, count, st);
   return cudaGetLastError();
 }
 

@@ -740,12 +740,12 @@ VT_D void shadow_end(const Frame& F, Path& p, SegEnd e) {
   }
 }
 
-// End of an extension segment: the body of the bounce loop
-// (pathTracer.fs:202-292).  Returns false when the path ends here; true when
-// it leaves a shadow segment (ro, sd) and, if p.has_cont, a continuation
-// segment (ro, rd).
+// End of an extension segment, first part of the body of the bounce loop
+// (pathTracer.fs:202-233): a miss adds the environment, and the bounce
+// limit and the selected voxel end the path.  Returns true when the hit is
+// shaded (ext_hit).
 template <bool kCount>
-VT_D bool ext_end(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount>& cnt) {
+VT_D bool ext_resolve(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount>& cnt) {
   const bool hit = seg_hit(F.quirks, e.state, e.y);
   if (!hit) {
     if (p.primary) {
@@ -760,12 +760,21 @@ VT_D bool ext_end(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount
   }
   if (!p.primary) p.bounces += 1;                                 // :291
   if (p.bounces >= F.max_bounces) return false;                   // :214
-  const Basis b = voxel_basis(F, e.x, e.y, e.z, p.ro, p.rd, !(F.quirks & Q_UNGUARDED));   // :220-223
-  const Mat m = voxel_mat(F, J, e.x, e.y, e.z, cnt);              // :225-226
   if (F.sel_enabled && e.x == F.sel[0] && e.y == F.sel[1] && e.z == F.sel[2]) {
+    cnt.add(C_PALETTE, 1);                                        // the material fetch of :225-226
     p.L = p.L + mk3(1.0f, 0.0f, 0.0f);                            // :228-233
     return false;
   }
+  return true;
+}
+
+// Second part (pathTracer.fs:220-279): shade a hit that ext_resolve kept.
+// Leaves a shadow segment (ro, sd) and, if p.has_cont, a continuation
+// segment (ro, rd).
+template <bool kCount>
+VT_D void ext_hit(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount>& cnt) {
+  const Basis b = voxel_basis(F, e.x, e.y, e.z, p.ro, p.rd, !(F.quirks & Q_UNGUARDED));   // :220-223
+  const Mat m = voxel_mat(F, J, e.x, e.y, e.z, cnt);              // :225-226
   const v3 wo = -p.rd;
   const v3 lwo = world_to_local(wo, b);
   if (p.bounces == 0) p.L = p.L + p.T * m.emission;               // :241-245
@@ -807,7 +816,24 @@ VT_D bool ext_end(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount
   p.rd = wwi;
   p.bsdf_pdf = bs.pdf;
   p.primary = 0;
+}
+
+// The whole bounce-loop body: false when the path ends here.
+template <bool kCount>
+VT_D bool ext_end(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount>& cnt) {
+  if (!ext_resolve(F, J, p, e, cnt)) return false;
+  ext_hit(F, J, p, e, cnt);
   return true;
+}
+
+// Material class of a hit for grouping hits before ext_hit: 0 Lambert,
+// 1 anything else (the microfacet path).  No counter: ext_hit counts the
+// material fetch.
+VT_D int hit_class(const Frame& F, const JobDev& J, SegEnd e) {
+  if (e.y < 0) return load_mat(J, F.ground_mat).type == 0 ? 0 : 1;
+  const uint8_t g = __ldg(&J.grid[(size_t)e.x + (size_t)F.res[0] * ((size_t)e.y + (size_t)F.res[1] * (size_t)e.z)]);
+  if (g == 0) return 1;
+  return load_mat(J, (int)g - 1).type == 0 ? 0 : 1;
 }
 
 // One complete sample, run to the end by a single lane (megakernel form).
