@@ -72,8 +72,16 @@ struct WfJobTable {
   JobEntry e[kWfParamJobs];
   Grid g[kWfParamJobs];
 };
+// A launch of one job: its records at fixed offsets of the parameter block,
+// which the kernels read as constant operands.
+struct WfOneJob {
+  JobEntry e;
+  Grid g;
+};
 // k_wf_shade over every slot, then k_wf_hit over the hit list and
 // k_wf_regen over the free list it leaves (persist_blocks blocks of 128).
+// T (nullable): the launch's job and grid records; a one-job launch uses
+// the WfOneJob form.
 cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool count, cudaStream_t st,
                             const WfJobTable* T = nullptr);
 cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,

@@ -119,8 +119,11 @@ __device__ __forceinline__ const Grid& grid_entry(const WfParams& P, const WfNoT
 __device__ __forceinline__ const Grid& grid_entry(const WfParams&, const WfJobTable& T, uint32_t j) {
   return T.g[j];
 }
+__device__ __forceinline__ const JobEntry& job_entry(const WfParams&, const WfOneJob& T, uint32_t) { return T.e; }
+__device__ __forceinline__ const Grid& grid_entry(const WfParams&, const WfOneJob& T, uint32_t) { return T.g; }
 
 // Job of a global item index (binary search over tile_begin).
+__device__ __forceinline__ int job_of(const WfParams&, const WfOneJob&, unsigned long long) { return 0; }
 template <class Tab>
 __device__ __forceinline__ int job_of(const WfParams& P, const Tab& T, unsigned long long item) {
   int lo = 0, hi = P.n_jobs - 1;
@@ -411,6 +414,20 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
   flush_counters(cnt, P.counters);
 }
 
+// The grid record of a lane's current segment: a register copy, or with one
+// job the record in the parameter block itself (constant operands).
+template <class Tab>
+struct GridHold {
+  Grid g;
+  __device__ __forceinline__ void set(const WfParams& P, const Tab& T, uint32_t job) { g = grid_entry(P, T, job); }
+  __device__ __forceinline__ const Grid& get(const Tab&) const { return g; }
+};
+template <>
+struct GridHold<WfOneJob> {
+  __device__ __forceinline__ void set(const WfParams&, const WfOneJob&, uint32_t) {}
+  __device__ __forceinline__ const Grid& get(const WfOneJob& T) const { return T.g; }
+};
+
 // One round of tracing: every queued segment runs its DDA to the end.  Each
 // warp takes chunks of queue records with one atomic and hands them to its
 // lanes; every lane keeps the record of its next segment loaded while it
@@ -432,15 +449,15 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
   uint32_t pool = 0, pool_end = 0;
   bool exhausted = false, have = false, have_next = false;
   float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
-  Grid g;
+  GridHold<Tab> gh;
   Dda s;
   uint32_t tag = 0;   // slot << 1 | kind of the current segment
   for (;;) {
     if (!have && have_next) {            // start the prefetched segment
       have_next = false;
       tag = __float_as_uint(nb.z);
-      g = grid_entry(P, T, __float_as_uint(nb.w));
-      dda_begin(g, s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
+      gh.set(P, T, __float_as_uint(nb.w));
+      dda_begin(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
       if (s.state == DDA_RUNNING) have = true;
       else P.st.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
     }
@@ -466,7 +483,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
     }
     if (__ballot_sync(FULL, have || have_next) == 0u) break;
     if (have) {
-      dda_advance(g, s, kTraceSteps, cnt);
+      dda_advance(gh.get(T), s, kTraceSteps, cnt);
       if (s.state != DDA_RUNNING) {
         P.st.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
         have = false;
@@ -502,9 +519,17 @@ static void wf_shade(const WfParams& P, const Tab& T, int par, int persist_block
   }
 }
 
+static WfOneJob one_job(const WfJobTable& T) {
+  WfOneJob o;
+  o.e = T.e[0];
+  o.g = T.g[0];
+  return o;
+}
+
 cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool count, cudaStream_t st,
                             const WfJobTable* T) {
-  if (T && P.n_jobs <= kWfParamJobs) wf_shade(P, *T, par, persist_blocks, count, st);
+  if (T && P.n_jobs == 1) wf_shade(P, one_job(*T), par, persist_blocks, count, st);
+  else if (T && P.n_jobs <= kWfParamJobs) wf_shade(P, *T, par, persist_blocks, count, st);
   else wf_shade(P, WfNoTable{0}, par, persist_blocks, count, st);
   return cudaGetLastError();
 }
@@ -519,7 +544,8 @@ static void wf_trace(const WfParams& P, const Tab& T, int par, int blocks, int s
 
 cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,
                             const WfJobTable* T) {
-  if (T && P.n_jobs <= kWfParamJobs) wf_trace(P, *T, par, blocks, steps, count, st);
+  if (T && P.n_jobs == 1) wf_trace(P, one_job(*T), par, blocks, steps, count, st);
+  else if (T && P.n_jobs <= kWfParamJobs) wf_trace(P, *T, par, blocks, steps, count, st);
   else wf_trace(P, WfNoTable{0}, par, blocks, steps, count, st);
   return cudaGetLastError();
 }
