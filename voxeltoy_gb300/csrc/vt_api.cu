@@ -1193,6 +1193,14 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
 // launches whose sample buffers stay within ctx->max_items.
 int vt::render_wavefront(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int slots,
                          int blocks_per_sm, bool count) {
+  if (n > kWfMaxJobs) {   // launches of at most kWfMaxJobs jobs
+    for (int32_t i = 0; i < n; i += kWfMaxJobs) {
+      const int rc = render_wavefront(ctx, jobs + i, std::min<int32_t>(kWfMaxJobs, n - i), passes + i, slots,
+                                      blocks_per_sm, count);
+      if (rc != VT_OK) return rc;
+    }
+    return VT_OK;
+  }
   std::vector<int32_t> done(n, 0);
   const int64_t slots_cap = slots > 0 ? slots : ctx->max_slots;
   for (;;) {

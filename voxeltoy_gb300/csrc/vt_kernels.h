@@ -68,6 +68,7 @@ struct WfParams {
 // kernel parameter as well, so the kernels read them through the constant
 // cache instead of global memory.
 constexpr int kWfParamJobs = 8;
+constexpr int kWfMaxJobs = 1 << 15;   // jobs per wavefront launch (bits of the slot flags)
 struct WfJobTable {
   JobEntry e[kWfParamJobs];
   Grid g[kWfParamJobs];

@@ -97,7 +97,10 @@ enum : uint32_t {
   SL_ACTIVE = 1u << 12,
   SL_DEAD = 1u << 13,     // no work left for this slot in this launch
   // bits 14..16: non-finite throughput components of the pending light sample
+  // bits 17..31: job of the path
 };
+constexpr int kSlotJobShift = 17;
+static_assert(kWfMaxJobs == (1 << (32 - kSlotJobShift)), "job bits of the slot flags");
 
 __device__ __forceinline__ v3 xyz4(float4 v) { return mk3(v.x, v.y, v.z); }
 __device__ __forceinline__ float4 pack4(v3 a, float w) { return make_float4(a.x, a.y, a.z, w); }
@@ -134,42 +137,62 @@ __device__ __forceinline__ int job_of(const WfParams& P, const Tab& T, unsigned 
   return lo;
 }
 
-// Slot state layout: a0 = (ro, job), a1 = (rd, item), a2 = (sd, light),
-// a3 = (L, rng), a4 = (T, bsdf_pdf), a5 = (nee_P, sample); the pixel is
-// derived from the item and sample; bounces and flag bits live in `flags`.
-__device__ __forceinline__ void load_path(const WfSlots& st, int slot, uint32_t fl, const JobEntry& E, uint32_t item,
-                                          Path& p) {
-  const float4 a0 = st.a0[slot], a1 = st.a1[slot], a2 = st.a2[slot];
-  const float4 a3 = st.a3[slot], a4 = st.a4[slot], a5 = st.a5[slot];
-  p.ro = xyz4(a0);
-  p.rd = xyz4(a1);
-  p.sd = xyz4(a2); p.light = __float_as_int(a2.w);
-  p.L = xyz4(a3);
-  p.T = xyz4(a4); p.bsdf_pdf = a4.w;
-  p.nee_P = xyz4(a5);
+// Slot state layout: a0 = (ro, -), a1 = (rd, item), a2 = (sd, -),
+// a3 = (L, rng), a4 = (T, bsdf_pdf), a5 = (nee_P, light); the job, bounces
+// and flag bits live in `flags`, and pixel and sample follow from the item.
+// k_wf_shade reads only what ending a segment needs (a1, a3, a4, and a5 for a
+// shadow result); k_wf_hit reads what shading a hit needs (a0, a1, a3, a4).
+__device__ __forceinline__ void load_flags(uint32_t fl, Path& p) {
   p.bounces = (int)(fl & SL_BOUNCES);
   p.primary = (fl & SL_PRIMARY) ? 1 : 0;
   p.has_cont = (fl & SL_HAS_CONT) ? 1 : 0;
   p.nee_nf = (int)((fl >> 14) & 7u);
+}
+
+__device__ __forceinline__ void load_for_shade(const WfSlots& st, int slot, uint32_t fl, Path& p, uint32_t& item,
+                                               float& rng_word) {
+  const float4 a1 = st.a1[slot], a3 = st.a3[slot], a4 = st.a4[slot];
+  p.rd = xyz4(a1);
+  item = __float_as_uint(a1.w);
+  p.L = xyz4(a3);
+  rng_word = a3.w;
+  p.T = xyz4(a4); p.bsdf_pdf = a4.w;
+  if (fl & SL_SHADOW) {
+    const float4 a5 = st.a5[slot];
+    p.nee_P = xyz4(a5); p.light = __float_as_int(a5.w);
+  }
+  load_flags(fl, p);
+}
+
+__device__ __forceinline__ void load_for_hit(const WfSlots& st, int slot, uint32_t fl, const JobEntry& E, Path& p,
+                                             uint32_t& item) {
+  const float4 a0 = st.a0[slot], a1 = st.a1[slot], a3 = st.a3[slot], a4 = st.a4[slot];
+  p.ro = xyz4(a0);
+  p.rd = xyz4(a1);
+  item = __float_as_uint(a1.w);
+  p.L = xyz4(a3);
+  p.T = xyz4(a4); p.bsdf_pdf = a4.w;
+  load_flags(fl, p);
   // item - tile_begin = pass * n_pixels + pixel (< 2^32 items per launch)
-  const uint32_t sample = __float_as_uint(a5.w);
-  const uint32_t pass = sample - (uint32_t)E.sample_base;
+  const uint32_t r = item - (uint32_t)E.tile_begin;
+  const uint32_t np = (uint32_t)E.n_pixels;
+  const uint32_t pass = r / np;
   const uint32_t rng = __float_as_uint(a3.w);
-  p.rng.pixel = (item - (uint32_t)E.tile_begin) - pass * (uint32_t)E.n_pixels;
-  p.rng.sample = sample;
+  p.rng.pixel = r - pass * np;
+  p.rng.sample = (uint32_t)E.sample_base + pass;
   if (E.F.rng_mode == 1) { p.rng.ox = (int32_t)(rng & 0xffffu); p.rng.oy = (int32_t)(rng >> 16); p.rng.call = 0; }
   else { p.rng.call = rng; p.rng.ox = p.rng.oy = 0; }
 }
 
-__device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Frame& F, const Path& p, uint32_t job,
+__device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Frame& F, const Path& p,
                                            uint32_t item) {
   const uint32_t rng = (F.rng_mode == 1) ? ((uint32_t)p.rng.ox | ((uint32_t)p.rng.oy << 16)) : p.rng.call;
-  st.a0[slot] = pack4(p.ro, __uint_as_float(job));
+  st.a0[slot] = pack4(p.ro, 0.0f);
   st.a1[slot] = pack4(p.rd, __uint_as_float(item));
-  st.a2[slot] = pack4(p.sd, __int_as_float(p.light));
+  st.a2[slot] = pack4(p.sd, 0.0f);
   st.a3[slot] = pack4(p.L, __uint_as_float(rng));
   st.a4[slot] = pack4(p.T, p.bsdf_pdf);
-  st.a5[slot] = pack4(p.nee_P, __uint_as_float(p.rng.sample));
+  st.a5[slot] = pack4(p.nee_P, __int_as_float(p.light));
 }
 
 // Block-wide reservation on N counters with one atomic per counter and
@@ -227,9 +250,10 @@ __device__ __forceinline__ void write_segments(const WfParams& P, int par, uint3
   }
 }
 
-__device__ __forceinline__ uint32_t slot_flags(const Path& p, uint32_t emit) {
+__device__ __forceinline__ uint32_t slot_flags(const Path& p, uint32_t emit, uint32_t job) {
   return SL_ACTIVE | (uint32_t)(p.bounces & 0xff) | (p.primary ? SL_PRIMARY : 0u) | (p.has_cont ? SL_HAS_CONT : 0u) |
-         ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u) | ((uint32_t)(p.nee_nf & 7) << 14);
+         ((emit & 1u) ? SL_EXT : 0u) | ((emit & 2u) ? SL_SHADOW : 0u) | ((uint32_t)(p.nee_nf & 7) << 14) |
+         (job << kSlotJobShift);
 }
 
 // A round has four kernels:
@@ -261,10 +285,11 @@ __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __
   int cls = 0;
   Path p;
   if (active) {
-    const uint32_t job = __float_as_uint(P.st.a0[slot].w);
-    const uint32_t item = __float_as_uint(P.st.a1[slot].w);
+    const uint32_t job = fl >> kSlotJobShift;
     const JobEntry& E = job_entry(P, T, job);
-    load_path(P.st, slot, fl, E, item, p);
+    uint32_t item;
+    float rng_word;
+    load_for_shade(P.st, slot, fl, p, item, rng_word);
     if (fl & SL_SHADOW) {
       const int4 h = P.st.hits[(size_t)P.n_slots + slot];
       SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
@@ -278,8 +303,8 @@ __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __
     }
     if (hit) {
       // L and the bounce count for k_wf_hit
-      P.st.a3[slot] = make_float4(p.L.x, p.L.y, p.L.z, P.st.a3[slot].w);
-      P.st.flags[slot] = slot_flags(p, 1u);
+      P.st.a3[slot] = make_float4(p.L.x, p.L.y, p.L.z, rng_word);
+      P.st.flags[slot] = slot_flags(p, 1u, job);
     } else {
       P.sbuf[item] = path_output(E.F, p);
       need_new = true;
@@ -317,10 +342,9 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
     uint32_t emit = 0;
     if (mine) {
       const uint32_t fl = P.st.flags[slot];
-      job = __float_as_uint(P.st.a0[slot].w);
-      item = __float_as_uint(P.st.a1[slot].w);
+      job = fl >> kSlotJobShift;
       const JobEntry& E = job_entry(P, T, job);
-      load_path(P.st, slot, fl, E, item, p);
+      load_for_hit(P.st, slot, fl, E, p, item);
       const int4 h = P.st.hits[slot];
       SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
       ext_hit(E.F, E.J, p, e, cnt);
@@ -332,8 +356,8 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
     block_reserve<1>(ctr, n, base);
     write_segments(P, par, base[0], emit, slot, job, p.ro, p);
     if (mine) {
-      store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
-      P.st.flags[slot] = slot_flags(p, emit);
+      store_path(P.st, slot, job_entry(P, T, job).F, p, item);
+      P.st.flags[slot] = slot_flags(p, emit, job);
     }
   }
   flush_counters(cnt, P.counters);
@@ -405,8 +429,8 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
     block_reserve<2>(ctr, n, base);
     write_segments(P, par, base[0], active ? 1u : 0u, slot, job, o, p);
     if (active) {
-      store_path(P.st, slot, job_entry(P, T, job).F, p, job, item);
-      P.st.flags[slot] = slot_flags(p, 1u);
+      store_path(P.st, slot, job_entry(P, T, job).F, p, item);
+      P.st.flags[slot] = slot_flags(p, 1u, job);
     } else if (mine) {
       P.st.flags[slot] = dead ? SL_DEAD : 0u;
     }
