@@ -479,7 +479,7 @@ def main():
     ap.add_argument("--spp", type=int, default=256)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 persistent")
+    ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 wavefront")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     ap.add_argument("--slots", type=int, default=0, help="path slots per launch (skips the autotuner)")
     ap.add_argument("--trace-steps", type=int, default=0, help="DDA steps between refills (with --slots)")
@@ -615,7 +615,8 @@ def main():
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         t = json.loads(tf.read_text())
-        if t.get("workload") == "config2" and t.get("grid") == args.edge and t.get("res") == args.res:
+        if (t.get("workload") == "config2" and t.get("grid") == args.edge and t.get("res") == args.res
+                and t.get("spp") == args.spp):
             traffic = t["dram_bytes_per_launch"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -627,7 +628,8 @@ def main():
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
-                     "peak_source": pk["source"], "kernel": "k_wf_trace + k_wf_shade (one frame)",
+                     "peak_source": pk["source"],
+                     "kernel": "k_wf_shade + k_wf_hit + k_wf_regen + k_wf_trace + k_wf_accumulate (one frame = one launch)",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "bytes_model": "1 B/DDA cell + 16 B/palette record + 8 B/env texel eval + 4 B/CDF probe + "
                                     "4 B/emissive read + 64 B/path framebuffer"},

@@ -337,11 +337,12 @@ VT_API int vt_job_pick(vt_job* job, float x, float y, float* distance,
 VT_API int vt_job_destroy(vt_job* job);
 
 /* ------------------------------------------------------------- batching -- */
-/* Trace `passes` samples per pixel for every job in one persistent launch
- * that pulls (job, pixel-tile) work items from a device queue, instead of one
- * launch per job and pass.  Results are identical to rendering each job alone
- * (counter-based random streams, per-pixel sample order).  opts may be NULL
- * (autotuned defaults). */
+/* Trace `passes` samples per pixel for every job in one wavefront launch:
+ * path slots pull (job, pass, pixel) work items from a device counter and
+ * rounds of shading and DDA kernels run over all jobs' paths at once,
+ * instead of one launch per job and pass.  Results are identical to rendering
+ * each job alone (counter-based random streams, per-pixel sample order).
+ * opts may be NULL (context defaults). */
 typedef struct vt_batch_opts {
   int32_t path_slots;      /* paths in flight per launch, 0 = context default (8M) */
   int32_t blocks_per_sm;   /* resident blocks per SM, 0 = auto                  */

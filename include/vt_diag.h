@@ -46,7 +46,7 @@ VT_API int vt_diag_render_counted(vt_job* job, int32_t passes, uint64_t* counter
 
 /* Kernel form used by vt_job_render and vt_render_batch when their options
  * do not say: 1 = plain (one thread per pixel, one launch per pass),
- * 2 = persistent (work queue over jobs and tiles). */
+ * 2 = wavefront (path slots over all jobs' work items). */
 VT_API int vt_diag_set_kernel(vt_context* ctx, int32_t kernel);
 
 /* Evaluate a builtin of the renderer on the GPU: fn 0 sin, 1 cos, 2 pow(a, b),

@@ -1396,7 +1396,7 @@ extern "C" int vt_diag_render_counted(vt_job* j, int32_t passes, uint64_t* count
 }
 
 extern "C" int vt_diag_set_kernel(vt_context* ctx, int32_t kernel) {
-  VT_CHECK_ARG(ctx && (kernel == 1 || kernel == 2), "kernel must be 1 (plain) or 2 (persistent)");
+  VT_CHECK_ARG(ctx && (kernel == 1 || kernel == 2), "kernel must be 1 (plain) or 2 (wavefront)");
   ctx->kernel = kernel;
   return VT_OK;
 }

@@ -8,7 +8,7 @@
 
 namespace vt {
 
-// One job as seen by the persistent kernel: its uniforms, device pointers and
+// One job as seen by the wavefront kernels: its uniforms, device pointers and
 // the work it contributes to the launch.
 struct JobEntry {
   Frame F;

@@ -17,7 +17,7 @@ struct vt_context {
   uint64_t budget = 0;          // 0 = unlimited
   uint64_t in_use = 0;          // bytes held through alloc()
   int sm_count = 0;
-  int kernel = 2;               // 1 plain, 2 persistent
+  int kernel = 2;               // 1 plain, 2 wavefront
   vt_log_fn log_fn = nullptr;
   void* log_user = nullptr;
   std::mutex mu;
@@ -99,7 +99,7 @@ namespace vt {
 int fail(int code, const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);
 int build_frame(vt_job* j);
-// passes[i] samples per pixel for jobs[i]; kernel 1 = plain, 2 = persistent.
+// passes[i] samples per pixel for jobs[i]; kernel 1 = plain, 2 = wavefront.
 int render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int kernel,
                 int tile_pixels, int blocks_per_sm, bool count);
 // Wavefront form; `slots` path slots per launch (0 = context default).

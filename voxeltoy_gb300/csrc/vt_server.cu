@@ -4,7 +4,7 @@
 // table).  Each round it admits queued requests while slots and the HBM
 // budget allow (accumulation buffers of the job plus, once per distinct
 // scene, the scene's resident bytes), traces every admitted job together in
-// one persistent launch (passes_per_round samples per pixel each), and
+// one wavefront launch (passes_per_round samples per pixel each), and
 // retires jobs that reached their sample target: their average image is
 // copied to host memory and their device buffers are freed.  Requests that
 // arrive while a round is on the GPU join the next round.  Because the random
