@@ -366,7 +366,7 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
  * frame times, such as an interactive viewer, because cudaMalloc and
  * cudaFree can synchronise the whole device.  Instead, this call takes all
  * of its working memory from one array compiled into the library
- * (VT_FIXED_SCRATCH_BYTES, about 34 MB, not counted against any budget),
+ * (VT_FIXED_SCRATCH_BYTES, about 46 MB, not counted against any budget),
  * reserved on a device when the CUDA runtime loads the library's code for
  * that device.
  *
@@ -380,17 +380,17 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
  * The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress) once, with that device current; make that first
  * call before any stream capture begins on the device.  Each launch clears
- * the words that must start at zero (queue counters, the item counter, the
- * path-slot flags); everything else in the array is written before it is
- * read.  There is one array per device, shared by every call on every
- * context of that device: two calls whose device work overlaps (two host
- * threads, or two contexts driven at the same time) race on it and both
- * results are wrong.  A call returns only after its device work has
- * finished, so calls made one after another are safe. */
+ * the words that must start at zero (queue and hit-list counters, the path
+ * stream's length, the item counter); everything else in the array is
+ * written before it is read.  There is one array per device, shared by
+ * every call on every context of that device: two calls whose device work
+ * overlaps (two host threads, or two contexts driven at the same time) race
+ * on it and both results are wrong.  A call returns only after its device
+ * work has finished, so calls made one after another are safe. */
 #define VT_FIXED_MAX_JOBS 16
 #define VT_FIXED_MAX_PATH_SLOTS 65536
 #define VT_FIXED_MAX_SAMPLES (1 << 20)
-#define VT_FIXED_SCRATCH_BYTES 34352896
+#define VT_FIXED_SCRATCH_BYTES 45625088
 VT_API int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs,
                                  int32_t n_jobs, int32_t passes,
                                  int32_t path_slots, int32_t* results);

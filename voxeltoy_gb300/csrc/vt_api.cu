@@ -1069,11 +1069,8 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     ctx->release(ctx->wf_mem);
     ctx->wf_mem = nullptr;
     ctx->wf_slots = 0;
-    // six float4 of state, two int4 segment ends, two queues of 2 records x 32 B, flags, free list,
-    // hit list
-    const size_t bytes =
-        (size_t)slots * (6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 3 * sizeof(uint32_t));
-    int rc = ctx->alloc(&ctx->wf_mem, bytes);
+    // two path streams, segment ends, hit records, two segment queues (layout of wf_carve)
+    int rc = ctx->alloc(&ctx->wf_mem, (size_t)slots * kWfSlotBytes);
     if (rc != VT_OK) return rc;
     ctx->wf_slots = slots;
   }
@@ -1094,17 +1091,6 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaHostAlloc");
   }
   return VT_OK;
-}
-
-static WfSlots wf_slots_view(vt_context* ctx) {
-  const size_t S = (size_t)ctx->wf_slots;
-  char* b = (char*)ctx->wf_mem;
-  WfSlots st;
-  float4* f = (float4*)b;
-  st.a0 = f; st.a1 = f + S; st.a2 = f + 2 * S; st.a3 = f + 3 * S; st.a4 = f + 4 * S; st.a5 = f + 5 * S;
-  st.hits = (int4*)(f + 6 * S);
-  st.flags = (uint32_t*)((float4*)(st.hits + 2 * S) + 8 * S);   // after the two queues
-  return st;
 }
 
 // One wavefront launch over `entries` (tile_begin = first item of each job).
@@ -1139,15 +1125,10 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   P.jobs = ctx->d_jobs;
   P.n_jobs = (int32_t)entries.size();
   P.grids = ctx->d_grids;
-  P.st = wf_slots_view(ctx);
+  wf_carve(ctx->wf_mem, (size_t)ctx->wf_slots, P);
   P.n_slots = (int32_t)slots;
-  float4* qmem = (float4*)(P.st.hits + 2 * ctx->wf_slots);
-  P.queue[0] = qmem;
-  P.queue[1] = qmem + 4 * ctx->wf_slots;
   P.ctl = ctx->wf_ctl;
   P.next_item = (unsigned long long*)(ctx->wf_ctl + kCtlNextItem);
-  P.free_slots = P.st.flags + ctx->wf_slots;
-  P.hit_slots = P.free_slots + ctx->wf_slots;
   P.n_items = (unsigned long long)items;
   P.sbuf = ctx->sbuf;
   P.counters = count ? ctx->d_counters : nullptr;
@@ -1161,8 +1142,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     }
     T = &table;
   }
-  VT_CUDA(cudaMemsetAsync(P.st.flags, 0, sizeof(uint32_t) * (size_t)slots, st), "slot flags");
-  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, kCtlBytes, st), "wavefront control");
+  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, kCtlBytes, st), "wavefront control");   // first stream: empty
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
   const int bps = blocks_per_sm > 0 ? blocks_per_sm
                                     : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
@@ -1175,9 +1155,9 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     VT_CUDA(launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st, T), "wavefront trace");
     ctx->launches += 4;
     if ((iter & 7) == 7) {
-      VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + ctl_index(par, CTL_LIVE), sizeof(uint32_t),
+      VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + ctl_index(par, CTL_NEXT_N), sizeof(uint32_t),
                               cudaMemcpyDeviceToHost, st),
-              "live count");
+              "stream length");
       VT_CUDA(cudaStreamSynchronize(st), "wavefront round");
       if (*(volatile uint32_t*)ctx->h_live == 0) break;
     }

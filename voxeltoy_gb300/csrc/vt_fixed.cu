@@ -6,10 +6,8 @@
 //               per counter; must start at zero)
 //   job table   VT_FIXED_MAX_JOBS JobEntry records
 //   grid table  VT_FIXED_MAX_JOBS Grid records
-//   path slots  VT_FIXED_MAX_PATH_SLOTS x (six float4 of state, two int4
-//               segment ends, two queues of two 32-byte records, a flag word,
-//               a free-list entry, a hit-list entry); the flags must start at
-//               zero
+//   path slots  VT_FIXED_MAX_PATH_SLOTS x kWfSlotBytes (two path streams,
+//               segment ends, hit records, two segment queues; wf_carve)
 //   samples     VT_FIXED_MAX_SAMPLES float4 per-sample outputs
 // The kernels are the ones vt_render_batch runs; only where their buffers
 // live differs, so results are bit-identical.
@@ -25,7 +23,7 @@ namespace {
 
 constexpr size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-constexpr size_t kSlotBytes = 6 * sizeof(float4) + 2 * sizeof(int4) + 8 * sizeof(float4) + 3 * sizeof(uint32_t);
+constexpr size_t kSlotBytes = kWfSlotBytes;
 constexpr size_t kCtlOff = 0;
 constexpr size_t kJobsOff = kCtlOff + round256(kCtlBytes);
 constexpr size_t kGridsOff = kJobsOff + round256(sizeof(JobEntry) * VT_FIXED_MAX_JOBS);
@@ -83,19 +81,12 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   uint32_t* ctl = (uint32_t*)(base + kCtlOff);
   JobEntry* d_jobs = (JobEntry*)(base + kJobsOff);
   Grid* d_grids = (Grid*)(base + kGridsOff);
-  float4* f = (float4*)(base + kSlotsOff);
   WfParams P;
   memset(&P, 0, sizeof(P));
   P.jobs = d_jobs;
   P.n_jobs = n;
   P.grids = d_grids;
-  P.st.a0 = f; P.st.a1 = f + S; P.st.a2 = f + 2 * S; P.st.a3 = f + 3 * S; P.st.a4 = f + 4 * S; P.st.a5 = f + 5 * S;
-  P.st.hits = (int4*)(f + 6 * S);
-  P.queue[0] = (float4*)(P.st.hits + 2 * S);
-  P.queue[1] = P.queue[0] + 4 * S;
-  P.st.flags = (uint32_t*)(P.queue[1] + 4 * S);
-  P.free_slots = P.st.flags + S;
-  P.hit_slots = P.free_slots + S;
+  wf_carve(base + kSlotsOff, S, P);
   P.n_slots = (int32_t)slots;
   P.ctl = ctl;
   P.next_item = (unsigned long long*)(ctl + kCtlNextItem);
@@ -107,8 +98,6 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   if (e != cudaSuccess) return cuda_fail(e, "fixed job table");
   e = cudaMemcpyAsync(d_grids, grids, sizeof(Grid) * n, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) return cuda_fail(e, "fixed grid table");
-  e = cudaMemsetAsync(P.st.flags, 0, sizeof(uint32_t) * (size_t)slots, st);
-  if (e != cudaSuccess) return cuda_fail(e, "fixed slot flags");
   e = cudaMemsetAsync(ctl, 0, kCtlBytes, st);
   if (e != cudaSuccess) return cuda_fail(e, "fixed control words");
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
@@ -125,7 +114,7 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
     ctx->launches += 4;
     if ((iter & 7) == 7) {
       uint32_t live = 0;   // pageable: the copy has completed when it returns
-      e = cudaMemcpyAsync(&live, ctl + ctl_index(par, CTL_LIVE), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+      e = cudaMemcpyAsync(&live, ctl + ctl_index(par, CTL_NEXT_N), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
       if (e != cudaSuccess) return cuda_fail(e, "fixed live count");
       if (live == 0) break;

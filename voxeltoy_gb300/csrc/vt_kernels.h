@@ -24,25 +24,34 @@ cudaError_t launch_plain(const Frame& F, const JobDev& J, int sample_base, int p
                          unsigned long long* counters, cudaStream_t st);
 cudaError_t launch_diag(const Frame& F, const JobDev& J, int sample, float4* out, HitRecord* hits,
                         unsigned long long* counters, cudaStream_t st);
-// Wavefront path state, structure of arrays over the path slots.
-struct WfSlots {
-  float4* a0;      // ro.xyz, job (uint bits)
+// Wavefront path state: a stream of paths, structure of arrays over the
+// stream positions.  Each round reads one stream and writes the next one
+// compacted: the paths that continue first, then the new paths.
+struct WfState {
+  float4* a0;      // ro.xyz, -
   float4* a1;      // rd.xyz, item (uint bits)
-  float4* a2;      // sd.xyz, light (int bits)
-  float4* a3;      // L.xyz, rng state (uint bits)
+  float4* a2;      // sd.xyz, -
+  float4* a3;      // L.xyz, rng word
   float4* a4;      // T.xyz, bsdf_pdf
-  float4* a5;      // nee_P.xyz, unused
-  uint32_t* flags; // bounces | primary | has_cont | ext | shadow | active | dead
-  int4* hits;      // [2][n_slots] segment ends: extension, shadow
+  float4* a5;      // nee_P.xyz (throughput * light sample), light (int bits)
+  uint32_t* flags; // bounces | primary | has_cont | ext | shadow | active | NEE mask | job
 };
-// Control words of a wavefront launch.  Per parity: entries appended to the
-// queue, entries taken by the tracer, active slots after the round, entries
-// appended to the free list, Lambert and other entries of the hit list; then
-// the 64-bit item counter.  Each
-// word has its own 128-byte line, so atomics on different counters never
-// queue behind each other in one L2 sector.
-enum { CTL_QCOUNT = 0, CTL_QHEAD = 1, CTL_LIVE = 2, CTL_FREE = 3, CTL_HITS_LAMBERT = 4, CTL_HITS_OTHER = 5,
-       CTL_PER_PARITY = 8 };
+// The hits k_wf_shade keeps for k_wf_hit, in hit-list order: Lambert hits
+// from the front, the others from the back.
+struct WfHitRecs {
+  float4* h0;      // ro.xyz, item
+  float4* h1;      // rd.xyz, flags
+  float4* h2;      // L.xyz, rng word
+  float4* h3;      // T.xyz, bsdf_pdf
+  int4* h4;        // hit voxel x, y, z, DDA state
+};
+// Control words of a wavefront launch, per round parity: records appended to
+// the queue, records taken by the tracer, length of the stream the round
+// writes, the item counter when the round started (64-bit), Lambert and other
+// entries of the hit list.  Each word has its own 128-byte line, so atomics
+// on different counters never queue behind each other in one L2 sector.
+enum { CTL_QCOUNT = 0, CTL_QHEAD = 1, CTL_NEXT_N = 2, CTL_ITEM_SNAP = 3, CTL_HITS_LAMBERT = 4,
+       CTL_HITS_OTHER = 5, CTL_PER_PARITY = 8 };
 constexpr int kCtlStride = 32;                                   // words per counter line
 constexpr int kCtlNextItem = 2 * CTL_PER_PARITY * kCtlStride;    // word index of the item counter
 constexpr size_t kCtlBytes = (size_t)(2 * CTL_PER_PARITY + 1) * kCtlStride * sizeof(uint32_t);
@@ -52,18 +61,23 @@ struct WfParams {
   const JobEntry* jobs;            // device array, tile_begin = first item of the job
   int32_t n_jobs;
   const Grid* grids;               // device array, DDA view of each job's volume
-  WfSlots st;
-  int32_t n_slots;
+  WfState x[2];                    // round parity par reads x[par] and writes x[par ^ 1]
+  int4* hits;                      // [2][n_slots] segment ends (extension, shadow) by position
+  WfHitRecs hr;
+  int32_t n_slots;                 // stream capacity (paths in flight)
   float4* queue[2];                // segment records, two float4 each:
-                                   // {origin.xyz, dir.x} {dir.yz, slot << 1 | kind, job}
+                                   // {origin.xyz, dir.x} {dir.yz, position << 1 | kind, job}
   uint32_t* ctl;                   // control words, see ctl_index
-  uint32_t* free_slots;            // slots that need a new path (n_slots entries)
-  uint32_t* hit_slots;             // hits to shade: Lambert from the front, others from the back
   unsigned long long* next_item;
   unsigned long long n_items;
   float4* sbuf;                    // per-item sample outputs
   unsigned long long* counters;    // nullable
 };
+// Device bytes per stream position, and the carving of one allocation of
+// slots * kWfSlotBytes bytes (256-byte aligned) into the buffers of P.
+constexpr size_t kWfSlotBytes = 2 * (6 * sizeof(float4) + sizeof(uint32_t)) + 2 * sizeof(int4) +
+                                (4 * sizeof(float4) + sizeof(int4)) + 8 * sizeof(float4);
+void wf_carve(void* mem, size_t slots, WfParams& P);
 // Launches of at most kWfParamJobs jobs pass their job and grid records as a
 // kernel parameter as well, so the kernels read them through the constant
 // cache instead of global memory.
@@ -79,8 +93,9 @@ struct WfOneJob {
   JobEntry e;
   Grid g;
 };
-// k_wf_shade over every slot, then k_wf_hit over the hit list and
-// k_wf_regen over the free list it leaves (persist_blocks blocks of 128).
+// One round's shading: k_wf_shade over the stream, then k_wf_hit over the
+// hits it keeps and k_wf_regen filling the rest of the next stream with new
+// paths (persist_blocks blocks of 128 each).
 // T (nullable): the launch's job and grid records; a one-job launch uses
 // the WfOneJob form.
 cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool count, cudaStream_t st,

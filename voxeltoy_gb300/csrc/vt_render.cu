@@ -94,8 +94,7 @@ enum : uint32_t {
   SL_HAS_CONT = 1u << 9,
   SL_EXT = 1u << 10,      // an extension segment was traced for this slot
   SL_SHADOW = 1u << 11,   // a shadow segment was traced for this slot
-  SL_ACTIVE = 1u << 12,
-  SL_DEAD = 1u << 13,     // no work left for this slot in this launch
+  SL_ACTIVE = 1u << 12,   // a path (0: an empty position of the stream)
   // bits 14..16: non-finite throughput components of the pending light sample
   // bits 17..31: job of the path
 };
@@ -137,11 +136,12 @@ __device__ __forceinline__ int job_of(const WfParams& P, const Tab& T, unsigned 
   return lo;
 }
 
-// Slot state layout: a0 = (ro, -), a1 = (rd, item), a2 = (sd, -),
+// Path state (WfState): a0 = (ro, -), a1 = (rd, item), a2 = (sd, -),
 // a3 = (L, rng), a4 = (T, bsdf_pdf), a5 = (nee_P, light); the job, bounces
 // and flag bits live in `flags`, and pixel and sample follow from the item.
-// k_wf_shade reads only what ending a segment needs (a1, a3, a4, and a5 for a
-// shadow result); k_wf_hit reads what shading a hit needs (a0, a1, a3, a4).
+// k_wf_shade reads what ending a segment needs (a1, a3, a4, a5 for a shadow
+// result, a0 for a hit it keeps) and copies kept hits into hit records;
+// k_wf_hit reads only the hit records.
 __device__ __forceinline__ void load_flags(uint32_t fl, Path& p) {
   p.bounces = (int)(fl & SL_BOUNCES);
   p.primary = (fl & SL_PRIMARY) ? 1 : 0;
@@ -149,50 +149,40 @@ __device__ __forceinline__ void load_flags(uint32_t fl, Path& p) {
   p.nee_nf = (int)((fl >> 14) & 7u);
 }
 
-__device__ __forceinline__ void load_for_shade(const WfSlots& st, int slot, uint32_t fl, Path& p, uint32_t& item,
+__device__ __forceinline__ void load_for_shade(const WfState& st, int i, uint32_t fl, Path& p, uint32_t& item,
                                                float& rng_word) {
-  const float4 a1 = st.a1[slot], a3 = st.a3[slot], a4 = st.a4[slot];
+  const float4 a1 = st.a1[i], a3 = st.a3[i], a4 = st.a4[i];
   p.rd = xyz4(a1);
   item = __float_as_uint(a1.w);
   p.L = xyz4(a3);
   rng_word = a3.w;
   p.T = xyz4(a4); p.bsdf_pdf = a4.w;
   if (fl & SL_SHADOW) {
-    const float4 a5 = st.a5[slot];
+    const float4 a5 = st.a5[i];
     p.nee_P = xyz4(a5); p.light = __float_as_int(a5.w);
   }
   load_flags(fl, p);
 }
 
-__device__ __forceinline__ void load_for_hit(const WfSlots& st, int slot, uint32_t fl, const JobEntry& E, Path& p,
-                                             uint32_t& item) {
-  const float4 a0 = st.a0[slot], a1 = st.a1[slot], a3 = st.a3[slot], a4 = st.a4[slot];
-  p.ro = xyz4(a0);
-  p.rd = xyz4(a1);
-  item = __float_as_uint(a1.w);
-  p.L = xyz4(a3);
-  p.T = xyz4(a4); p.bsdf_pdf = a4.w;
-  load_flags(fl, p);
+__device__ __forceinline__ void rng_from_item(const JobEntry& E, uint32_t item, uint32_t rng, Path& p) {
   // item - tile_begin = pass * n_pixels + pixel (< 2^32 items per launch)
   const uint32_t r = item - (uint32_t)E.tile_begin;
   const uint32_t np = (uint32_t)E.n_pixels;
   const uint32_t pass = r / np;
-  const uint32_t rng = __float_as_uint(a3.w);
   p.rng.pixel = r - pass * np;
   p.rng.sample = (uint32_t)E.sample_base + pass;
   if (E.F.rng_mode == 1) { p.rng.ox = (int32_t)(rng & 0xffffu); p.rng.oy = (int32_t)(rng >> 16); p.rng.call = 0; }
   else { p.rng.call = rng; p.rng.ox = p.rng.oy = 0; }
 }
 
-__device__ __forceinline__ void store_path(const WfSlots& st, int slot, const Frame& F, const Path& p,
-                                           uint32_t item) {
+__device__ __forceinline__ void store_path(const WfState& st, int i, const Frame& F, const Path& p, uint32_t item) {
   const uint32_t rng = (F.rng_mode == 1) ? ((uint32_t)p.rng.ox | ((uint32_t)p.rng.oy << 16)) : p.rng.call;
-  st.a0[slot] = pack4(p.ro, 0.0f);
-  st.a1[slot] = pack4(p.rd, __uint_as_float(item));
-  st.a2[slot] = pack4(p.sd, 0.0f);
-  st.a3[slot] = pack4(p.L, __uint_as_float(rng));
-  st.a4[slot] = pack4(p.T, p.bsdf_pdf);
-  st.a5[slot] = pack4(p.nee_P, __int_as_float(p.light));
+  st.a0[i] = pack4(p.ro, 0.0f);
+  st.a1[i] = pack4(p.rd, __uint_as_float(item));
+  st.a2[i] = pack4(p.sd, 0.0f);
+  st.a3[i] = pack4(p.L, __uint_as_float(rng));
+  st.a4[i] = pack4(p.T, p.bsdf_pdf);
+  st.a5[i] = pack4(p.nee_P, __int_as_float(p.light));
 }
 
 // Block-wide reservation on N counters with one atomic per counter and
@@ -256,146 +246,171 @@ __device__ __forceinline__ uint32_t slot_flags(const Path& p, uint32_t emit, uin
          (job << kSlotJobShift);
 }
 
-// A round has four kernels:
-//   k_wf_shade  every slot: shadow results, misses (environment), bounce
-//               limit, finished paths -> sample buffer + free list; hits go
-//               to the hit list, Lambert hits from its front, the others
-//               from its back, so that k_wf_hit's warps mostly run one BSDF
-//   k_wf_hit    the hit list: vertex shading, light and BSDF samples, next
-//               segments -> queue
-//   k_wf_regen  the free list: new paths, primary segments -> queue
-//   k_wf_trace  the queue: DDA of every segment
-// k_wf_hit and k_wf_regen keep eight resident blocks per SM (64 registers):
-// the extra warps hide more of the state-load and instruction-fetch latency
-// than the few spills cost; the lighter k_wf_shade fits twelve.
+// A round has four kernels over the stream x[par] (n paths, written by the
+// previous round) and builds the stream x[par ^ 1]:
+//   k_wf_shade  every position: shadow results (NEE added if visible),
+//               extension results (miss -> environment, bounce limit,
+//               selection), finished paths -> sample buffer; surviving hits
+//               -> hit records, Lambert hits from the front of the list, the
+//               others from its back, so that k_wf_hit's warps mostly run one
+//               BSDF
+//   k_wf_hit    the hit records: vertex shading, light and BSDF samples;
+//               writes its paths to positions [0, hits) of the next stream
+//               and their next segments to the queue
+//   k_wf_regen  new paths in positions [hits, capacity) of the next stream,
+//               primary segments to the queue
+//   k_wf_trace  the queue: DDA of every segment, ends stored by position
+// Every state access is to consecutive positions.  k_wf_hit and k_wf_regen
+// keep eight resident blocks per SM (64 registers): the extra warps hide
+// more of the load latency than the few spills cost; the lighter k_wf_shade
+// fits twelve.
 template <bool kCount, class Tab>
 __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool in_range = slot < P.n_slots;
+  if (blockIdx.x == 0 && threadIdx.x == 0)    // items taken before this round, for k_wf_regen
+    *(unsigned long long*)&P.ctl[ctl_index(par, CTL_ITEM_SNAP)] = *(volatile unsigned long long*)P.next_item;
+  const uint32_t n = *(volatile uint32_t*)&P.ctl[ctl_index(par ^ 1, CTL_NEXT_N)];
+  if (blockIdx.x * blockDim.x >= n) return;   // the whole block lies beyond the stream
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const WfState& src = P.x[par];
   Cnt<kCount> cnt;
 #pragma unroll
-  for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
-  const uint32_t fl = in_range ? P.st.flags[slot] : SL_DEAD;
-  const bool active = (fl & SL_ACTIVE) != 0;
-  bool need_new = !active && !(fl & SL_DEAD);
+  for (int k = 0; k < C_NUM; ++k) cnt.c[k] = 0;
+  const uint32_t fl = (uint32_t)i < n ? src.flags[i] : 0u;
   bool hit = false;
   int cls = 0;
   Path p;
-  if (active) {
+  uint32_t item = 0;
+  float rng_word = 0.0f;
+  SegEnd e;
+  e.x = e.y = e.z = e.state = 0;
+  if (fl & SL_ACTIVE) {
     const uint32_t job = fl >> kSlotJobShift;
     const JobEntry& E = job_entry(P, T, job);
-    uint32_t item;
-    float rng_word;
-    load_for_shade(P.st, slot, fl, p, item, rng_word);
+    load_for_shade(src, i, fl, p, item, rng_word);
     if (fl & SL_SHADOW) {
-      const int4 h = P.st.hits[(size_t)P.n_slots + slot];
-      SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
-      shadow_end(E.F, p, e);
+      const int4 h = P.hits[(size_t)P.n_slots + i];
+      SegEnd se; se.x = h.x; se.y = h.y; se.z = h.z; se.state = h.w;
+      shadow_end(E.F, p, se);
     }
     if (fl & SL_EXT) {
-      const int4 h = P.st.hits[slot];
-      SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
+      const int4 h = P.hits[i];
+      e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
       hit = ext_resolve(E.F, E.J, p, e, cnt);
       if (hit) cls = hit_class(E.F, E.J, e);
     }
-    if (hit) {
-      // L and the bounce count for k_wf_hit
-      P.st.a3[slot] = make_float4(p.L.x, p.L.y, p.L.z, rng_word);
-      P.st.flags[slot] = slot_flags(p, 1u, job);
-    } else {
-      P.sbuf[item] = path_output(E.F, p);
-      need_new = true;
-    }
+    if (hit) p.ro = xyz4(src.a0[i]);
+    else P.sbuf[item] = path_output(E.F, p);
   }
-  uint32_t* const ctr[4] = {&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)], &P.ctl[ctl_index(par, CTL_HITS_OTHER)],
-                            &P.ctl[ctl_index(par, CTL_FREE)], &P.ctl[ctl_index(par, CTL_LIVE)]};
-  const uint32_t n[4] = {(hit && cls == 0) ? 1u : 0u, (hit && cls != 0) ? 1u : 0u, need_new ? 1u : 0u, hit ? 1u : 0u};
-  uint32_t base[4];
-  block_reserve<4>(ctr, n, base);
-  const unsigned bl = __ballot_sync(FULL, n[0]), bo = __ballot_sync(FULL, n[1]), bf = __ballot_sync(FULL, n[2]);
-  if (n[0]) P.hit_slots[base[0] + __popc(bl & lt)] = (uint32_t)slot;
-  if (n[1]) P.hit_slots[P.n_slots - 1 - (base[1] + __popc(bo & lt))] = (uint32_t)slot;
-  if (n[2]) P.free_slots[base[2] + __popc(bf & lt)] = (uint32_t)slot;
+  uint32_t* const ctr[2] = {&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)], &P.ctl[ctl_index(par, CTL_HITS_OTHER)]};
+  const uint32_t cnt_l = (hit && cls == 0) ? 1u : 0u, cnt_o = (hit && cls != 0) ? 1u : 0u;
+  const uint32_t nn[2] = {cnt_l, cnt_o};
+  uint32_t base[2];
+  block_reserve<2>(ctr, nn, base);
+  const unsigned bl = __ballot_sync(FULL, cnt_l), bo = __ballot_sync(FULL, cnt_o);
+  if (hit) {
+    const uint32_t j = cnt_l ? base[0] + __popc(bl & lt) : (uint32_t)P.n_slots - 1u - (base[1] + __popc(bo & lt));
+    P.hr.h0[j] = pack4(p.ro, __uint_as_float(item));
+    P.hr.h1[j] = pack4(p.rd, __uint_as_float(slot_flags(p, 1u, fl >> kSlotJobShift)));
+    P.hr.h2[j] = pack4(p.L, rng_word);
+    P.hr.h3[j] = pack4(p.T, p.bsdf_pdf);
+    P.hr.h4[j] = make_int4(e.x, e.y, e.z, e.state);
+  }
   flush_counters(cnt, P.counters);
 }
 
-// Hits kept by k_wf_shade: entries [0, n_lambert) of the hit list, then the
-// other class from the back.  A block-uniform grid-stride loop.
+// The hit records of this round: list entry v (Lambert entries [0, nl), then
+// the others, stored from the back) becomes position v of the next stream.
+// A block-uniform grid-stride loop.
 template <bool kCount, class Tab>
 __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __grid_constant__ Tab T, int par) {
   const uint32_t nl = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)];
   const uint32_t no = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_OTHER)];
   const uint32_t n_hits = nl + no;
+  const WfState& dst = P.x[par ^ 1];
   Cnt<kCount> cnt;
 #pragma unroll
-  for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
+  for (int k = 0; k < C_NUM; ++k) cnt.c[k] = 0;
   const uint32_t stride = gridDim.x * blockDim.x;
   for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n_hits; b0 += stride) {   // block-uniform
     const uint32_t v = b0 + threadIdx.x;
     const bool mine = v < n_hits;
-    const int slot = !mine ? 0 : (int)P.hit_slots[v < nl ? v : P.n_slots - 1 - (v - nl)];
     Path p;
     uint32_t job = 0, item = 0;
     uint32_t emit = 0;
     if (mine) {
-      const uint32_t fl = P.st.flags[slot];
+      const uint32_t j = v < nl ? v : (uint32_t)P.n_slots - 1u - (v - nl);
+      const float4 h0 = P.hr.h0[j], h1 = P.hr.h1[j], h2 = P.hr.h2[j], h3 = P.hr.h3[j];
+      const int4 h4 = P.hr.h4[j];
+      const uint32_t fl = __float_as_uint(h1.w);
       job = fl >> kSlotJobShift;
       const JobEntry& E = job_entry(P, T, job);
-      load_for_hit(P.st, slot, fl, E, p, item);
-      const int4 h = P.st.hits[slot];
-      SegEnd e; e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
+      p.ro = xyz4(h0);
+      item = __float_as_uint(h0.w);
+      p.rd = xyz4(h1);
+      p.L = xyz4(h2);
+      p.T = xyz4(h3); p.bsdf_pdf = h3.w;
+      load_flags(fl, p);
+      rng_from_item(E, item, __float_as_uint(h2.w), p);
+      SegEnd e; e.x = h4.x; e.y = h4.y; e.z = h4.z; e.state = h4.w;
       ext_hit(E.F, E.J, p, e, cnt);
       emit = 2u | (p.has_cont ? 1u : 0u);
     }
     uint32_t* const ctr[1] = {&P.ctl[ctl_index(par, CTL_QCOUNT)]};
-    const uint32_t n[1] = {(emit & 1u) + (emit >> 1)};
+    const uint32_t nn[1] = {(emit & 1u) + (emit >> 1)};
     uint32_t base[1];
-    block_reserve<1>(ctr, n, base);
-    write_segments(P, par, base[0], emit, slot, job, p.ro, p);
+    block_reserve<1>(ctr, nn, base);
+    write_segments(P, par, base[0], emit, (int)v, job, p.ro, p);
     if (mine) {
-      store_path(P.st, slot, job_entry(P, T, job).F, p, item);
-      P.st.flags[slot] = slot_flags(p, emit, job);
+      store_path(dst, (int)v, job_entry(P, T, job).F, p, item);
+      dst.flags[v] = slot_flags(p, emit, job);
     }
   }
   flush_counters(cnt, P.counters);
 }
 
-// New paths for the slots on the free list: each lane takes items until one
-// enters its job's volume or the items run out; a path that misses the
-// volume is finished at once.  The primary segment starts at the volume
-// entry point.  A block-uniform grid-stride loop; the first item of every
-// listed slot is claimed for the whole block with one atomic.
+// New paths at positions [hits, hits + m) of the next stream, m = the free
+// capacity or the items left, whichever is smaller.  Each lane takes items
+// until one enters its job's volume (a path that misses the volume is
+// finished at once) or the items run out (the position stays empty).  The
+// primary segment starts at the volume entry point.  A block-uniform
+// grid-stride loop; the first item of every position is claimed for the
+// whole block with one atomic.
 template <bool kCount, class Tab>
 __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   __shared__ unsigned long long s_item;
-  const uint32_t n_free = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_FREE)];
+  const uint32_t n_hits = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)] +
+                          *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_OTHER)];
+  const unsigned long long taken = *(volatile unsigned long long*)&P.ctl[ctl_index(par, CTL_ITEM_SNAP)];
+  const unsigned long long left = P.n_items > taken ? P.n_items - taken : 0ull;
+  const uint32_t m = (uint32_t)min((unsigned long long)((uint32_t)P.n_slots - n_hits), left);
+  if (blockIdx.x == 0 && threadIdx.x == 0) P.ctl[ctl_index(par, CTL_NEXT_N)] = n_hits + m;
+  const WfState& dst = P.x[par ^ 1];
   Cnt<kCount> cnt;
 #pragma unroll
-  for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
+  for (int k = 0; k < C_NUM; ++k) cnt.c[k] = 0;
   const uint32_t stride = gridDim.x * blockDim.x;
-  for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < n_free; b0 += stride) {   // block-uniform
-    const uint32_t i = b0 + threadIdx.x;
-    const bool mine = i < n_free;
-    const int slot = mine ? (int)P.free_slots[i] : 0;
-    if (threadIdx.x == 0) s_item = atomicAdd(P.next_item, (unsigned long long)min(blockDim.x, n_free - b0));
+  for (uint32_t b0 = blockIdx.x * blockDim.x; b0 < m; b0 += stride) {   // block-uniform
+    const uint32_t k = b0 + threadIdx.x;
+    const bool mine = k < m;
+    const uint32_t pos = n_hits + k;
+    if (threadIdx.x == 0) s_item = atomicAdd(P.next_item, (unsigned long long)min(blockDim.x, m - b0));
     __syncthreads();
     unsigned long long my = s_item + threadIdx.x;
     __syncthreads();
-    bool need_new = mine, active = false, dead = false;
+    bool need_new = mine, active = false;
     Path p;
     uint32_t job = 0, item = 0;
     float t_enter = 0.0f;
     for (;;) {
       if (need_new) {
         if (my >= P.n_items) {
-          need_new = false;
-          dead = true;
+          need_new = false;   // no items left: the position stays empty
         } else {
           item = (uint32_t)my;
           job = (uint32_t)job_of(P, T, my);
@@ -423,16 +438,16 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
       my = base + __popc(want & lt);
     }
     const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
-    uint32_t* const ctr[2] = {&P.ctl[ctl_index(par, CTL_QCOUNT)], &P.ctl[ctl_index(par, CTL_LIVE)]};
-    const uint32_t n[2] = {active ? 1u : 0u, active ? 1u : 0u};
-    uint32_t base[2];
-    block_reserve<2>(ctr, n, base);
-    write_segments(P, par, base[0], active ? 1u : 0u, slot, job, o, p);
+    uint32_t* const ctr[1] = {&P.ctl[ctl_index(par, CTL_QCOUNT)]};
+    const uint32_t nn[1] = {active ? 1u : 0u};
+    uint32_t base[1];
+    block_reserve<1>(ctr, nn, base);
+    write_segments(P, par, base[0], active ? 1u : 0u, (int)pos, job, o, p);
     if (active) {
-      store_path(P.st, slot, job_entry(P, T, job).F, p, item);
-      P.st.flags[slot] = slot_flags(p, 1u, job);
+      store_path(dst, (int)pos, job_entry(P, T, job).F, p, item);
+      dst.flags[pos] = slot_flags(p, 1u, job);
     } else if (mine) {
-      P.st.flags[slot] = dead ? SL_DEAD : 0u;
+      dst.flags[pos] = 0u;
     }
   }
   flush_counters(cnt, P.counters);
@@ -475,7 +490,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
   float4 na = make_float4(0.f, 0.f, 0.f, 0.f), nb = na;
   GridHold<Tab> gh;
   Dda s;
-  uint32_t tag = 0;   // slot << 1 | kind of the current segment
+  uint32_t tag = 0;   // position << 1 | kind of the current segment
   for (;;) {
     if (!have && have_next) {            // start the prefetched segment
       have_next = false;
@@ -483,7 +498,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
       gh.set(P, T, __float_as_uint(nb.w));
       dda_begin(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
       if (s.state == DDA_RUNNING) have = true;
-      else P.st.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
+      else P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
     }
     unsigned need = __ballot_sync(FULL, !have_next);
     while (need && !exhausted) {          // prefetch next records
@@ -509,7 +524,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
     if (have) {
       dda_advance(gh.get(T), s, kTraceSteps, cnt);
       if (s.state != DDA_RUNNING) {
-        P.st.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
+        P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
         have = false;
       }
     }
@@ -580,6 +595,26 @@ cudaError_t launch_wf_accumulate(const JobEntry* jobs, int n_jobs, long long max
   dim3 grid((unsigned)((max_pixels + 255) / 256), (unsigned)n_jobs);
   k_wf_accumulate<<<grid, 256, 0, st>>>(jobs, sbuf);
   return cudaGetLastError();
+}
+
+void wf_carve(void* mem, size_t S, WfParams& P) {
+  float4* f = (float4*)mem;
+  for (int s = 0; s < 2; ++s) {
+    WfState& x = P.x[s];
+    x.a0 = f; x.a1 = f + S; x.a2 = f + 2 * S; x.a3 = f + 3 * S; x.a4 = f + 4 * S; x.a5 = f + 5 * S;
+    f += 6 * S;
+  }
+  P.hr.h0 = f; P.hr.h1 = f + S; P.hr.h2 = f + 2 * S; P.hr.h3 = f + 3 * S;
+  f += 4 * S;
+  P.queue[0] = f;
+  P.queue[1] = f + 4 * S;
+  f += 8 * S;
+  int4* h = (int4*)f;
+  P.hits = h;
+  P.hr.h4 = h + 2 * S;
+  uint32_t* u = (uint32_t*)(h + 3 * S);
+  P.x[0].flags = u;
+  P.x[1].flags = u + S;
 }
 
 int wf_trace_blocks_per_sm() {
