@@ -49,6 +49,10 @@ VT_API int vt_diag_render_counted(vt_job* job, int32_t passes, uint64_t* counter
  * 2 = wavefront (path slots over all jobs' work items). */
 VT_API int vt_diag_set_kernel(vt_context* ctx, int32_t kernel);
 
+/* Wavefront rounds replayed as a captured CUDA graph (enabled = 1, the
+ * default) or launched one by one (0).  Results are identical. */
+VT_API int vt_diag_set_graphs(vt_context* ctx, int32_t enabled);
+
 /* Evaluate a builtin of the renderer on the GPU: fn 0 sin, 1 cos, 2 pow(a, b),
  * 3 acos, 4 atan2(a, b), 5 log2, 6 exp2, 7 float -> half -> float. */
 VT_API int vt_diag_builtins(vt_context* ctx, int32_t fn, const float* a, const float* b,

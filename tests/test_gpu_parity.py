@@ -203,6 +203,25 @@ def test_plain_and_persistent_kernels_agree(ctx):
         close_all(job, scene, env)
 
 
+def test_graph_rounds_equal_direct_launches(ctx):
+    """The wavefront rounds replayed from a captured graph give the same bits
+    as the same rounds launched one by one."""
+    cfg = small_config2(edge=32, w=48, h=40, seed=15)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        out = []
+        for graphs in (True, False, True):
+            ctx.set_graphs(graphs)
+            job.reset()
+            job.render(5)
+            out.append(job.readback().view(np.uint32).copy())
+        np.testing.assert_array_equal(out[0], out[1])
+        np.testing.assert_array_equal(out[0], out[2])
+    finally:
+        ctx.set_graphs(True)
+        close_all(job, scene, env)
+
+
 def test_batch_equals_alone(ctx):
     cfgs = [small_config1(edge=40, w=37, h=23, seed=5), small_config2(edge=32, w=64, h=48, seed=6),
             small_config1(edge=24, w=16, h=70, seed=7)]

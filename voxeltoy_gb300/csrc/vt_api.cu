@@ -153,6 +153,7 @@ extern "C" int vt_destroy(vt_context* ctx) {
   ctx->release(ctx->sbuf);
   ctx->release(ctx->wf_ctl);
   if (ctx->h_live) cudaFreeHost(ctx->h_live);
+  if (ctx->rounds_exec) cudaGraphExecDestroy(ctx->rounds_exec);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -1147,20 +1148,59 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   const int bps = blocks_per_sm > 0 ? blocks_per_sm
                                     : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
   const int trace_blocks = ctx->sm_count * bps;
-  for (int64_t iter = 0;; ++iter) {
-    const int par = (int)(iter & 1);
-    VT_CUDA(cudaMemsetAsync(ctx->wf_ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t), st),
-            "round counters");
-    VT_CUDA(launch_wf_shade(P, par, ctx->sm_count * 8, count, st, T), "wavefront shade");
-    VT_CUDA(launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st, T), "wavefront trace");
-    ctx->launches += 4;
-    if ((iter & 7) == 7) {
-      VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + ctl_index(par, CTL_NEXT_N), sizeof(uint32_t),
-                              cudaMemcpyDeviceToHost, st),
-              "stream length");
-      VT_CUDA(cudaStreamSynchronize(st), "wavefront round");
-      if (*(volatile uint32_t*)ctx->h_live == 0) break;
+  // one round: its counters cleared, shade + hit + regen, trace
+  auto round = [&](int par) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(ctx->wf_ctl + ctl_index(par, 0), 0,
+                                    CTL_PER_PARITY * kCtlStride * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = launch_wf_shade(P, par, ctx->sm_count * 8, count, st, T);
+    if (e == cudaSuccess) e = launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st, T);
+    return e;
+  };
+  // Rounds go in groups of eight (a CUDA graph captured once per launch and
+  // replayed), then the length of the next stream is read back; an empty
+  // stream means every item is done.
+  if (ctx->use_graphs) {
+    cudaGraph_t graph = nullptr;
+    VT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "capture rounds");
+    cudaError_t ce = cudaSuccess;
+    for (int r = 0; r < 8 && ce == cudaSuccess; ++r) ce = round(r & 1);
+    const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return cuda_fail(ce != cudaSuccess ? ce : ee, "capture rounds");
     }
+    bool updated = false;
+    if (ctx->rounds_exec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(ctx->rounds_exec, graph, &info) == cudaSuccess;
+      if (!updated) {
+        cudaGetLastError();
+        cudaGraphExecDestroy(ctx->rounds_exec);
+        ctx->rounds_exec = nullptr;
+      }
+    }
+    if (!updated) {
+      const cudaError_t ie = cudaGraphInstantiate(&ctx->rounds_exec, graph, 0);
+      if (ie != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        ctx->rounds_exec = nullptr;
+        return cuda_fail(ie, "instantiate rounds");
+      }
+    }
+    cudaGraphDestroy(graph);
+  }
+  for (;;) {
+    if (ctx->use_graphs) {
+      VT_CUDA(cudaGraphLaunch(ctx->rounds_exec, st), "wavefront rounds");
+    } else {
+      for (int r = 0; r < 8; ++r) VT_CUDA(round(r & 1), "wavefront round");
+    }
+    ctx->launches += 8 * 4;
+    VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + ctl_index(1, CTL_NEXT_N), sizeof(uint32_t),
+                            cudaMemcpyDeviceToHost, st),
+            "stream length");
+    VT_CUDA(cudaStreamSynchronize(st), "wavefront rounds");
+    if (*(volatile uint32_t*)ctx->h_live == 0) break;
   }
   long long max_pixels = 0;
   for (const JobEntry& e : entries) max_pixels = std::max<long long>(max_pixels, e.n_pixels);
@@ -1372,6 +1412,12 @@ extern "C" int vt_diag_render_counted(vt_job* j, int32_t passes, uint64_t* count
                           j->ctx->stream), "counters");
   VT_CUDA(cudaStreamSynchronize(j->ctx->stream), "counters");
   if (result) *result = j->samples >= j->set.max_samples ? VT_FINISHED_RENDERING : VT_SAMPLES_PENDING;
+  return VT_OK;
+}
+
+extern "C" int vt_diag_set_graphs(vt_context* ctx, int32_t enabled) {
+  VT_CHECK_ARG(ctx, "context is null");
+  ctx->use_graphs = enabled != 0;
   return VT_OK;
 }
 

@@ -42,6 +42,8 @@ struct vt_context {
   int trace_occupancy = 0;       // occupancy limit of the DDA kernel (cached)
   int trace_steps = 16;          // DDA steps between refills of the trace kernel
   uint64_t launches = 0;         // render kernels launched by this context
+  cudaGraphExec_t rounds_exec = nullptr;   // eight wavefront rounds, replayed until the stream empties
+  bool use_graphs = true;
   unsigned long long* d_counters = nullptr;
   unsigned long long* d_queue = nullptr;
   int32_t* d_error = nullptr;

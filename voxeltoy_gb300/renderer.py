@@ -86,6 +86,10 @@ class Context:
     def set_kernel(self, kernel: int):
         L.call("vt_diag_set_kernel", self.h, kernel)
 
+    def set_graphs(self, enabled: bool):
+        """Replay wavefront rounds as a CUDA graph (default) or launch them one by one."""
+        L.call("vt_diag_set_graphs", self.h, 1 if enabled else 0)
+
     def builtins(self, fn: int, a: np.ndarray, b: np.ndarray | None = None) -> np.ndarray:
         a = np.ascontiguousarray(a, dtype=np.float32)
         b = None if b is None else np.ascontiguousarray(b, dtype=np.float32)
