@@ -100,6 +100,21 @@ typedef struct vt_material {
   float roughness;
 } vt_material;
 
+/* ---------------------------------------------------------------- images -- */
+/* Float images for environment maps and saved frames (the reference reads
+ * and writes them with OpenImageIO: image.cpp:28-59, renderer.cpp:1108-1140).
+ * vt_image_decode reads PFM ("PF" colour, "Pf" grey) and Radiance RGBE
+ * (.hdr, flat or run-length scanlines) into RGB floats, rows top first as
+ * vt_env_create_image takes them; with rgb NULL it returns only the size.
+ * vt_image_encode_pfm writes a colour PFM from RGB or RGBA floats whose rows
+ * are bottom first (vt_job_readback's order, which PFM also uses); with out
+ * NULL it returns only the size.  Neither needs a GPU. */
+VT_API int vt_image_decode(const uint8_t* data, size_t size, float* rgb,
+                           size_t rgb_bytes, int32_t* width, int32_t* height);
+VT_API int vt_image_encode_pfm(const float* pixels, int32_t width, int32_t height,
+                               int32_t channels, uint8_t* out, size_t out_bytes,
+                               size_t* written);
+
 /* ---------------------------------------------------------------- scenes -- */
 enum {
   VT_SCENE_PRUNE_EMISSIVE = 1u << 0, /* drop emissive voxels with no empty 6-neighbour
@@ -151,6 +166,40 @@ VT_API int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices,
                                   int32_t rz, int32_t mode, int32_t placement,
                                   const vt_material* palette, int32_t n_palette,
                                   vt_scene** out);
+
+/* ---------------------------------------------------------- file ingest -- */
+/* MagicaVoxel .vox bytes (Renderer::loadVoxFile, src/renderer/renderer.h:62;
+ * MagicaVoxelLoader::load, src/renderer/loaders/magicaVoxel.cpp:122-321).
+ * As the reference: file versions 150 (and 200, which only adds chunks that
+ * are skipped), axes converted so that the file's z is up (res = {x, z, y}),
+ * colour index 254 left empty, one Lambert material per colour used, albedo
+ * = palette RGB / 255, in order of first use, from the file's RGBA chunk or
+ * MagicaVoxel's default palette.  Voxels outside the model are an error (the
+ * reference writes past its grid).
+ * vt_vox_decode needs no GPU: with voxels and palette NULL it returns the
+ * resolution and palette size; then voxels (res[0]*res[1]*res[2] bytes,
+ * 0 empty, k = palette[k-1]) and palette (n_palette entries) are filled. */
+VT_API int vt_vox_decode(const uint8_t* data, size_t size, int32_t res[3],
+                         uint8_t* voxels, size_t voxels_bytes,
+                         vt_material* palette, int32_t* n_palette);
+VT_API int vt_scene_create_from_vox(vt_context* ctx, const uint8_t* data,
+                                    size_t size, uint32_t flags, vt_scene** out);
+
+/* Wavefront OBJ text (MeshLoader::loadFromOBJ, src/mesh/meshLoader.cpp:11-74,
+ * which merges every shape into one vertex and index list): `v` positions
+ * and `f` faces (v, v/vt, v//vn, v/vt/vn references, negative = relative),
+ * polygons fan-triangulated; other records are ignored.  vt_obj_decode needs
+ * no GPU and follows the same two-call pattern as vt_vox_decode;
+ * vt_scene_voxelize_obj decodes and calls vt_scene_voxelize_mesh
+ * (Renderer::loadMesh, src/renderer/import.cpp:66-131). */
+VT_API int vt_obj_decode(const char* text, size_t size, float* vertices,
+                         int64_t vertex_capacity, uint32_t* indices,
+                         int64_t triangle_capacity, int64_t* n_vertices,
+                         int64_t* n_triangles);
+VT_API int vt_scene_voxelize_obj(vt_context* ctx, const char* text, size_t size,
+                                 int32_t rx, int32_t ry, int32_t rz, int32_t mode,
+                                 int32_t placement, const vt_material* palette,
+                                 int32_t n_palette, vt_scene** out);
 
 typedef struct vt_scene_info {
   int32_t resolution[3];

@@ -200,3 +200,43 @@ def test_emissive_scene_renders_light(ctx):
         job.close()
     finally:
         sc.close()
+
+
+def test_vox_scene_matches_decoded_volume(ctx):
+    """vt_scene_create_from_vox == vt_scene_create of what vt_vox_decode returns."""
+    from test_formats import vox_file
+    from voxeltoy_gb300 import formats as F
+    rng = np.random.default_rng(3)
+    size = (20, 16, 12)
+    pts = {tuple(rng.integers(0, s) for s in size) for _ in range(600)}
+    vox = [(x, y, z, int(rng.choice([3, 17, 40, 254]))) for x, y, z in sorted(pts)]
+    data = vox_file(size, vox)
+    grid, pal = F.vox_decode(data)
+    a = Scene.from_vox(ctx, data)
+    b = Scene.dense(ctx, grid, pal)
+    try:
+        np.testing.assert_array_equal(a.voxels(), grid)
+        cfg = small_config1(edge=8, w=16, h=16)
+        ja = Job(ctx, a, None, cfg.camera, cfg.settings, 16, 16)
+        jb = Job(ctx, b, None, cfg.camera, cfg.settings, 16, 16)
+        ja.render(2); jb.render(2)
+        np.testing.assert_array_equal(ja.readback().view(np.uint32), jb.readback().view(np.uint32))
+        ja.close(); jb.close()
+    finally:
+        a.close(); b.close()
+
+
+def test_obj_scene_matches_mesh_voxelization(ctx):
+    """vt_scene_voxelize_obj == vt_scene_voxelize_mesh on the same triangles."""
+    v, f = S.icosphere(2)
+    v = np.ascontiguousarray(v, np.float32)
+    text = "".join(f"v {x:.9g} {y:.9g} {z:.9g}\n" for x, y, z in v)
+    text += "".join(f"f {a + 1} {b + 1} {c + 1}\n" for a, b, c in f)
+    for mode in (L.VT_VOXELIZE_THIN, L.VT_VOXELIZE_FAT):
+        a = Scene.voxelize_obj(ctx, text, (40, 40, 40), mode=mode)
+        b = Scene.voxelize(ctx, v, f, (40, 40, 40), mode=mode, placement=L.VT_MESH_FIT_UNIT_CUBE)
+        try:
+            np.testing.assert_array_equal(a.voxels(), b.voxels())
+            assert np.count_nonzero(a.voxels()) > 0
+        finally:
+            a.close(); b.close()

@@ -142,6 +142,13 @@ SIGNATURES = {
     "vt_job_destroy": [P],
     "vt_render_batch": [P, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(BatchOpts), C.POINTER(C.c_int32)],
     "vt_render_batch_fixed": [P, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)],
+    "vt_vox_decode": [P, C.c_size_t, C.POINTER(C.c_int32), P, C.c_size_t, P, C.POINTER(C.c_int32)],
+    "vt_scene_create_from_vox": [P, P, C.c_size_t, C.c_uint32, PP],
+    "vt_obj_decode": [P, C.c_size_t, P, C.c_int64, P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
+    "vt_scene_voxelize_obj": [P, P, C.c_size_t, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, C.c_int32,
+                              PP],
+    "vt_image_decode": [P, C.c_size_t, P, C.c_size_t, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
+    "vt_image_encode_pfm": [P, C.c_int32, C.c_int32, C.c_int32, P, C.c_size_t, C.POINTER(C.c_size_t)],
     "vt_server_create": [P, C.POINTER(ServerOpts), PP],
     "vt_server_submit": [P, P, P, C.POINTER(Camera), C.POINTER(RenderSettings), C.c_int32, C.c_int32, C.c_int32,
                          C.POINTER(C.c_uint64)],

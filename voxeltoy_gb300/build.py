@@ -20,7 +20,7 @@ OUT_DIR = PKG / "_lib"
 BUILD_DIR = PKG / "_lib" / "obj"
 LIB = OUT_DIR / "libvoxeltoy.so"
 
-SOURCES = ["vt_api.cu", "vt_render.cu", "vt_scene.cu", "vt_server.cu", "vt_fixed.cu"]
+SOURCES = ["vt_api.cu", "vt_render.cu", "vt_scene.cu", "vt_server.cu", "vt_fixed.cu", "vt_io.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false",

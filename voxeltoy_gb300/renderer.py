@@ -171,6 +171,28 @@ class Scene:
                placement, L.materials(pal), len(pal), C.byref(h))
         return cls(ctx, h)
 
+    @classmethod
+    def from_vox(cls, ctx: Context, data, flags: int = 0) -> "Scene":
+        """MagicaVoxel .vox bytes or path (Renderer::loadVoxFile)."""
+        from .formats import _bytes
+        b = _bytes(data)
+        h = C.c_void_p()
+        L.call("vt_scene_create_from_vox", ctx.h, b, len(b), flags, C.byref(h))
+        return cls(ctx, h)
+
+    @classmethod
+    def voxelize_obj(cls, ctx: Context, text, resolution=(64, 64, 64), mode: int = 0,
+                     placement: int = L.VT_MESH_FIT_UNIT_CUBE, palette=None) -> "Scene":
+        """Wavefront OBJ text or path, voxelized on the GPU (Renderer::loadMesh)."""
+        from .formats import _bytes
+        b = text.encode() if isinstance(text, str) and "\n" in text else _bytes(text)
+        pal = palette or [(0, (0, 0, 0), (0.7, 0.7, 0.7), 0.0)]
+        rx, ry, rz = resolution
+        h = C.c_void_p()
+        L.call("vt_scene_voxelize_obj", ctx.h, b, len(b), rx, ry, rz, mode, placement, L.materials(pal), len(pal),
+               C.byref(h))
+        return cls(ctx, h)
+
     def info(self) -> L.SceneInfo:
         inf = L.SceneInfo()
         L.call("vt_scene_get_info", self.h, C.byref(inf))
@@ -377,6 +399,19 @@ class Renderer:
     def load_mesh(self, vertices: np.ndarray, indices: np.ndarray, resolution=(64, 64, 64), mode: int = 0):
         self._replace_scene(Scene.voxelize(self.ctx, vertices, indices, resolution, mode))
 
+    # Renderer::loadMesh from an OBJ file (import.cpp:66-131)
+    def load_mesh_file(self, path: str, resolution=(64, 64, 64), mode: int = 0):
+        self._replace_scene(Scene.voxelize_obj(self.ctx, path, resolution, mode))
+
+    # Renderer::loadVoxFile (renderer.h:62)
+    def load_vox_file(self, path: str, flags: int = L.VT_SCENE_PRUNE_EMISSIVE):
+        self._replace_scene(Scene.from_vox(self.ctx, path, flags))
+
+    # Renderer::loadBackgroundImage (renderer.cpp:947-1055) from a PFM or Radiance HDR file
+    def load_background_image(self, path: str):
+        from .formats import image_decode
+        self.set_background_image(image_decode(path))
+
     def set_background_image(self, rgb: np.ndarray | None):
         old = self.env
         self.env = Env(self.ctx, rgb) if rgb is not None else None
@@ -427,13 +462,9 @@ class Renderer:
 
     # Renderer::saveImage (renderer.h:72): float RGB written as a PFM file
     def save_image(self, path: str):
-        img = self.job.readback(L.VT_READBACK_FLIP_Y)
-        rgb = img[..., :3]
-        h, w = rgb.shape[:2]
+        from .formats import encode_pfm
         with open(path, "wb") as f:
-            f.write(f"PF\n{w} {h}\n-1.0\n".encode())
-            # PFM stores the bottom row first
-            f.write(np.ascontiguousarray(rgb[::-1], dtype="<f4").tobytes())
+            f.write(encode_pfm(self.job.readback()))   # PFM, like the readback, stores the bottom row first
 
     # Renderer::requestAction with the focal-distance service
     def pick_focal_distance(self, x: float, y: float):
