@@ -385,6 +385,39 @@ VT_API int vt_job_pick(vt_job* job, float x, float y, float* distance,
                        int32_t voxel[3]);
 VT_API int vt_job_destroy(vt_job* job);
 
+/* ---------------------------------------------------------- voxel edits -- */
+/* Set one voxel of a scene: entry 0 empties it, k (1..n_palette) gives it
+ * palette[k-1].  The grid, its occupancy bricks and the emissive list follow:
+ * scenes made with VT_SCENE_AUTO_EMISSIVE rediscover (and, with
+ * VT_SCENE_PRUNE_EMISSIVE, prune) their list; otherwise an emptied voxel
+ * leaves the caller's list.  Jobs on the scene see the edit at their next
+ * render or pick; reset them to drop samples of the old volume.  Do not edit
+ * a scene that a vt_server is rendering.  No counterpart as a function in
+ * the reference, whose edits run as the shaders below. */
+VT_API int vt_scene_set_voxel(vt_scene* scene, int32_t x, int32_t y, int32_t z,
+                              int32_t entry);
+/* RendererServiceSelectActiveVoxel (src/shaders/editVoxels/selectVoxel.vs:
+ * 35-69): the voxel under window point (x, y) (pixels, origin bottom-left)
+ * and the normal of its voxelSpaceToWorldSpace basis; voxel (-1,-1,-1) and
+ * normal 0 when the ray hits nothing (the reference leaves index 0 there). */
+VT_API int vt_job_select_voxel(vt_job* job, float x, float y, int32_t voxel[3],
+                               float normal[3]);
+/* RendererServiceAddVoxel (addVoxel.vs:16-41): select at (x, y); the new
+ * voxel is the selected one plus the hit normal or, when the screen-space
+ * motion (dx, dy) (pixels, y up) is not zero, plus the camera right / up
+ * axis of its dominant component; it copies the selected voxel's material
+ * (the ground's when the ground was hit).  voxel receives the new voxel, or
+ * -1s when nothing was hit or the new voxel lies outside the volume (no
+ * edit).  restart != 0 resets the job's accumulation (requestAction's
+ * restartAccumulation, src/renderer/actions.cpp:5-52). */
+VT_API int vt_job_add_voxel(vt_job* job, float x, float y, float dx, float dy,
+                            int32_t restart, int32_t voxel[3]);
+/* RendererServiceRemoveVoxel (removeVoxel.vs:8-11): select at (x, y) and
+ * empty that voxel; voxel receives it, or -1s when nothing (or only the
+ * implicit ground) was hit. */
+VT_API int vt_job_remove_voxel(vt_job* job, float x, float y, int32_t restart,
+                               int32_t voxel[3]);
+
 /* ------------------------------------------------------------- batching -- */
 /* Trace `passes` samples per pixel for every job in one wavefront launch:
  * path slots pull (job, pass, pixel) work items from a device counter and

@@ -240,3 +240,94 @@ def test_obj_scene_matches_mesh_voxelization(ctx):
             assert np.count_nonzero(a.voxels()) > 0
         finally:
             a.close(); b.close()
+
+
+def test_voxel_edits_match_a_rebuilt_scene(ctx):
+    """set_voxel keeps grid, bricks and the emissive list equal to a scene
+    built from the edited volume: same voxels, same emissive list, same image."""
+    rng = np.random.default_rng(4)
+    g = (rng.random((20, 24, 28)) < 0.3).astype(np.uint8) * rng.integers(1, 3, (20, 24, 28), dtype=np.uint8)
+    pal = [S.lambert(0.6), S.lambert(0.4, emission=(3.0, 3.0, 3.0))]
+    flags = L.VT_SCENE_AUTO_EMISSIVE | L.VT_SCENE_PRUNE_EMISSIVE
+    a = Scene.dense(ctx, g, pal, flags=flags)
+    edits = [(0, 0, 0, 2), (27, 23, 19, 1), (3, 4, 5, 0), (4, 4, 4, 2), (7, 8, 3, 0), (8, 8, 4, 2), (11, 12, 13, 0)]
+    want = g.copy()
+    for x, y, z, e in edits:
+        a.set_voxel(x, y, z, e)
+        want[z, y, x] = e
+    b = Scene.dense(ctx, want, pal, flags=flags)
+    try:
+        np.testing.assert_array_equal(a.voxels(), want)
+        assert sorted(a.emissive().tolist()) == sorted(b.emissive().tolist())
+        cfg = small_config1(edge=8, w=24, h=20)
+        ja = Job(ctx, a, None, cfg.camera, cfg.settings, 24, 20)
+        jb = Job(ctx, b, None, cfg.camera, cfg.settings, 24, 20)
+        ja.render(3); jb.render(3)
+        np.testing.assert_array_equal(ja.readback().view(np.uint32), jb.readback().view(np.uint32))
+        a.set_voxel(1, 1, 1, 2)                 # an edit after the job was built reaches it
+        want[1, 1, 1] = 2
+        c = Scene.dense(ctx, want, pal, flags=flags)
+        jc = Job(ctx, c, None, cfg.camera, cfg.settings, 24, 20)
+        ja.reset(); ja.render(2); jc.render(2)
+        np.testing.assert_array_equal(ja.readback().view(np.uint32), jc.readback().view(np.uint32))
+        for j in (ja, jb, jc):
+            j.close()
+        c.close()
+        with pytest.raises(L.VtError):
+            a.set_voxel(28, 0, 0, 1)
+        with pytest.raises(L.VtError):
+            a.set_voxel(0, 0, 0, 3)
+    finally:
+        a.close(); b.close()
+
+
+def test_caller_emissive_list_drops_removed_voxels(ctx):
+    g = np.ones((8, 8, 8), np.uint8)
+    em = np.array([0, 9, 100], np.int32)
+    sc = Scene.dense(ctx, g, [S.lambert(0.5, emission=(1, 1, 1))], emissive=em)
+    try:
+        sc.set_voxel(1, 1, 0, 0)                # linear index 9
+        assert sorted(sc.emissive().tolist()) == [0, 100]
+    finally:
+        sc.close()
+
+
+def test_select_add_remove_services(ctx):
+    cfg = small_config1(edge=32, w=32, h=32)
+    scene = Scene.dense(ctx, cfg.voxels, cfg.palette)
+    job = Job(ctx, scene, None, cfg.camera, cfg.settings, 32, 32)
+    try:
+        x, y = 16.0, 16.0
+        d0, v0 = job.pick(x, y)
+        assert v0[0] >= 0
+        sel, n = job.select_voxel(x, y)
+        assert sel == v0 and sorted(abs(c) for c in n) in ([0.0, 0.0, 1.0], [0.0, 1.0, 1.0], [1.0, 1.0, 1.0])
+        before = scene.voxels()
+        # remove the voxel under the cursor: the pick now lands behind it
+        job.render(2)
+        assert job.remove_voxel(x, y) == v0 and job.samples() == 0
+        vox = scene.voxels()
+        assert vox[v0[2], v0[1], v0[0]] == 0
+        assert np.count_nonzero(vox != before) == 1
+        d1, v1 = job.pick(x, y)
+        assert v1 != v0 and d1 >= d0
+        # add on the new hit along its normal: the pick lands on the new voxel
+        sel, n = job.select_voxel(x, y)
+        new = job.add_voxel(x, y)
+        assert new == tuple(s + int(c) for s, c in zip(sel, n))
+        vox = scene.voxels()
+        src = vox[sel[2], sel[1], sel[0]] if sel[1] >= 0 else cfg.settings.ground_material + 1
+        assert vox[new[2], new[1], new[0]] == src
+        assert job.pick(x, y)[1] == new
+        # with screen-space motion the new voxel is offset along the camera right
+        # axis's dominant components (several on ties, as the reference's step masks)
+        sel, _ = job.select_voxel(x, y)
+        moved = job.add_voxel(x, y, 5.0, 0.5)
+        if moved[0] >= 0:
+            off = [m - s for m, s in zip(moved, sel)]
+            assert all(abs(o) <= 1 for o in off) and any(off)
+        # nothing under the cursor: no edit
+        vox = scene.voxels()
+        assert job.remove_voxel(0.0, 0.0) == (-1, -1, -1) or job.pick(0.0, 0.0)[1][0] >= 0
+    finally:
+        job.close(); scene.close()

@@ -143,6 +143,10 @@ SIGNATURES = {
     "vt_render_batch": [P, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(BatchOpts), C.POINTER(C.c_int32)],
     "vt_render_batch_fixed": [P, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)],
     "vt_vox_decode": [P, C.c_size_t, C.POINTER(C.c_int32), P, C.c_size_t, P, C.POINTER(C.c_int32)],
+    "vt_scene_set_voxel": [P, C.c_int32, C.c_int32, C.c_int32, C.c_int32],
+    "vt_job_select_voxel": [P, C.c_float, C.c_float, C.POINTER(C.c_int32), fp],
+    "vt_job_add_voxel": [P, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32, C.POINTER(C.c_int32)],
+    "vt_job_remove_voxel": [P, C.c_float, C.c_float, C.c_int32, C.POINTER(C.c_int32)],
     "vt_scene_create_from_vox": [P, P, C.c_size_t, C.c_uint32, PP],
     "vt_obj_decode": [P, C.c_size_t, P, C.c_int64, P, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)],
     "vt_scene_voxelize_obj": [P, P, C.c_size_t, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, C.c_int32,

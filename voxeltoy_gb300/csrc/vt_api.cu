@@ -248,28 +248,15 @@ static int prune_emissive(vt_context* ctx, vt_scene* s, std::vector<int32_t>& li
   return VT_OK;
 }
 
-static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette, int32_t n_palette,
-                        const int32_t* emissive, int64_t n_emissive, uint32_t flags) {
+// The scene's emissive list: discovered from the palette
+// (VT_SCENE_AUTO_EMISSIVE, in voxel order) or the caller's indices, pruned
+// when VT_SCENE_PRUNE_EMISSIVE asks, uploaded in place of the previous list.
+static int scene_emissive(vt_context* ctx, vt_scene* s, const int32_t* emissive, int64_t n_emissive,
+                          uint32_t flags) {
   const int64_t nvox = (int64_t)s->res[0] * s->res[1] * s->res[2];
-  // palette
-  std::vector<uint4> pal(std::max(n_palette, 1));
-  for (int i = 0; i < n_palette; ++i) {
-    int rc = pack_material(palette[i], &pal[i]);
-    if (rc != VT_OK) return rc;
-  }
-  s->n_palette = n_palette;
-  s->host_palette.assign(palette, palette + n_palette);
-  int rc = ctx->alloc((void**)&s->palette, sizeof(uint4) * pal.size());
-  if (rc != VT_OK) return rc;
-  VT_CUDA(cudaMemcpyAsync(s->palette, pal.data(), sizeof(uint4) * pal.size(), cudaMemcpyHostToDevice, ctx->stream),
-          "palette upload");
-  // bit-bricks
-  const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
-  rc = ctx->alloc((void**)&s->bricks, sizeof(unsigned long long) * nb);
-  if (rc != VT_OK) return rc;
-  VT_CUDA(launch_build_bricks(s->grid, s->res[0], s->res[1], s->res[2], s->bricks, s->bdim[0], s->bdim[1],
-                              s->bdim[2], ctx->stream), "brick build");
-  // emissive list
+  const int32_t n_palette = s->n_palette;
+  const vt_material* palette = s->host_palette.data();
+  int rc = VT_OK;
   std::vector<int32_t> list;
   if (flags & VT_SCENE_AUTO_EMISSIVE) {
     uint8_t em[256] = {0};
@@ -310,15 +297,44 @@ static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette
     rc = prune_emissive(ctx, s, list);
     if (rc != VT_OK) return rc;
   }
+  ctx->release(s->emissive);
+  s->emissive = nullptr;
   s->n_emissive = (int64_t)list.size();
   rc = ctx->alloc((void**)&s->emissive, sizeof(int32_t) * std::max<size_t>(list.size(), 1));
   if (rc != VT_OK) return rc;
   if (!list.empty())
     VT_CUDA(cudaMemcpyAsync(s->emissive, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice,
                             ctx->stream), "emissive upload");
+  return VT_OK;
+}
+
+static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette, int32_t n_palette,
+                        const int32_t* emissive, int64_t n_emissive, uint32_t flags) {
+  const int64_t nvox = (int64_t)s->res[0] * s->res[1] * s->res[2];
+  // palette
+  std::vector<uint4> pal(std::max(n_palette, 1));
+  for (int i = 0; i < n_palette; ++i) {
+    int rc = pack_material(palette[i], &pal[i]);
+    if (rc != VT_OK) return rc;
+  }
+  s->n_palette = n_palette;
+  s->host_palette.assign(palette, palette + n_palette);
+  int rc = ctx->alloc((void**)&s->palette, sizeof(uint4) * pal.size());
+  if (rc != VT_OK) return rc;
+  VT_CUDA(cudaMemcpyAsync(s->palette, pal.data(), sizeof(uint4) * pal.size(), cudaMemcpyHostToDevice, ctx->stream),
+          "palette upload");
+  // bit-bricks
+  const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
+  rc = ctx->alloc((void**)&s->bricks, sizeof(unsigned long long) * nb);
+  if (rc != VT_OK) return rc;
+  VT_CUDA(launch_build_bricks(s->grid, s->res[0], s->res[1], s->res[2], s->bricks, s->bdim[0], s->bdim[1],
+                              s->bdim[2], ctx->stream), "brick build");
+  s->flags = flags;
+  rc = scene_emissive(ctx, s, emissive, n_emissive, flags);
+  if (rc != VT_OK) return rc;
   VT_CUDA(cudaStreamSynchronize(ctx->stream), "scene upload");
   s->bytes = (uint64_t)nvox + sizeof(unsigned long long) * nb + sizeof(uint4) * pal.size() +
-             sizeof(int32_t) * std::max<size_t>(list.size(), 1);
+             sizeof(int32_t) * std::max<int64_t>(s->n_emissive, 1);
   return VT_OK;
 }
 
@@ -942,6 +958,7 @@ int vt::build_frame(vt_job* j) {
   F.seed = S.seed;
   F.width = j->w;
   F.height = j->h;
+  j->scene_generation = s->generation;
   JobDev& D = j->dev;
   D.grid = s->grid;
   D.bricks = s->bricks;
@@ -1047,9 +1064,18 @@ extern "C" int vt_job_reset(vt_job* j) {
 }
 
 // Launch `passes` samples per pixel for a set of jobs with the selected kernel.
+int vt::refresh_job(vt_job* j) {
+  if (j->scene && j->scene_generation != j->scene->generation) return build_frame(j);
+  return VT_OK;
+}
+
 int vt::render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int kernel,
                     int path_slots, int blocks_per_sm, bool count) {
   cudaSetDevice(ctx->device);
+  for (int32_t i = 0; i < n; ++i) {
+    const int rc = refresh_job(jobs[i]);
+    if (rc != VT_OK) return rc;
+  }
   if (count) VT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * C_NUM, ctx->stream), "counters");
   if (kernel == 1) {
     for (int i = 0; i < n; ++i) {
@@ -1318,6 +1344,10 @@ extern "C" int vt_job_device_buffer(vt_job* j, void** sums, int32_t* samples) {
 
 extern "C" int vt_job_pick(vt_job* j, float x, float y, float* distance, int32_t voxel[3]) {
   VT_CHECK_ARG(j && distance, "null argument");
+  {
+    const int rc0 = refresh_job(j);
+    if (rc0 != VT_OK) return rc0;
+  }
   cudaSetDevice(j->ctx->device);
   int rc = j->ctx->ensure_scratch(64);
   if (rc != VT_OK) return rc;
@@ -1330,6 +1360,132 @@ extern "C" int vt_job_pick(vt_job* j, float x, float y, float* distance, int32_t
   VT_CUDA(cudaStreamSynchronize(j->ctx->stream), "pick");
   if (voxel) { voxel[0] = v[0]; voxel[1] = v[1]; voxel[2] = v[2]; }
   return VT_OK;
+}
+
+// ------------------------------------------------------------- voxel edits
+extern "C" int vt_scene_set_voxel(vt_scene* s, int32_t x, int32_t y, int32_t z, int32_t entry) {
+  VT_CHECK_ARG(s, "scene is null");
+  VT_CHECK_ARG(x >= 0 && y >= 0 && z >= 0 && x < s->res[0] && y < s->res[1] && z < s->res[2],
+               "voxel outside the volume");
+  VT_CHECK_ARG(entry >= 0 && entry <= s->n_palette, "entry outside the palette");
+  vt_context* ctx = s->ctx;
+  cudaSetDevice(ctx->device);
+  const int64_t idx = (int64_t)x + (int64_t)s->res[0] * ((int64_t)y + (int64_t)s->res[1] * z);
+  VT_CUDA(launch_set_voxel(s->grid, s->bricks, s->res[0], s->res[1], s->bdim[0], s->bdim[1], x, y, z,
+                           (uint8_t)entry, ctx->stream), "voxel edit");
+  int rc = VT_OK;
+  if (s->flags & VT_SCENE_AUTO_EMISSIVE) {
+    rc = scene_emissive(ctx, s, nullptr, 0, s->flags);          // rediscover from the palette
+  } else if (s->n_emissive > 0 && entry == 0) {
+    std::vector<int32_t> list((size_t)s->n_emissive);           // an emptied voxel leaves the caller's list
+    VT_CUDA(cudaMemcpyAsync(list.data(), s->emissive, sizeof(int32_t) * list.size(), cudaMemcpyDeviceToHost,
+                            ctx->stream), "emissive list");
+    VT_CUDA(cudaStreamSynchronize(ctx->stream), "emissive list");
+    list.erase(std::remove(list.begin(), list.end(), (int32_t)idx), list.end());
+    if ((int64_t)list.size() != s->n_emissive) rc = scene_emissive(ctx, s, list.data(), (int64_t)list.size(), 0);
+  }
+  if (rc != VT_OK) return rc;
+  VT_CUDA(cudaStreamSynchronize(ctx->stream), "voxel edit");
+  s->generation += 1;
+  return VT_OK;
+}
+
+// RendererServiceSelectActiveVoxel (selectVoxel.vs:35-69).
+static int select_voxel(vt_job* j, float x, float y, int32_t voxel[3], float normal[3], bool* hit) {
+  vt_context* ctx = j->ctx;
+  cudaSetDevice(ctx->device);
+  int rc = refresh_job(j);
+  if (rc != VT_OK) return rc;
+  rc = ctx->ensure_scratch(64);
+  if (rc != VT_OK) return rc;
+  int32_t* d = (int32_t*)ctx->scratch;
+  VT_CUDA(launch_select(j->frame, j->dev, x, y, j->cam.near_distance, d, ctx->stream), "select voxel");
+  int32_t out[8];
+  VT_CUDA(cudaMemcpyAsync(out, d, sizeof(out), cudaMemcpyDeviceToHost, ctx->stream), "select voxel");
+  VT_CUDA(cudaStreamSynchronize(ctx->stream), "select voxel");
+  for (int i = 0; i < 3; ++i) {
+    voxel[i] = out[i];
+    memcpy(&normal[i], &out[4 + i], sizeof(float));
+  }
+  *hit = out[3] != 0;
+  return VT_OK;
+}
+
+extern "C" int vt_job_select_voxel(vt_job* j, float x, float y, int32_t voxel[3], float normal[3]) {
+  VT_CHECK_ARG(j && voxel && normal, "null argument");
+  bool hit = false;
+  return select_voxel(j, x, y, voxel, normal, &hit);
+}
+
+static bool inside(const vt_scene* s, const int32_t v[3]) {
+  return v[0] >= 0 && v[1] >= 0 && v[2] >= 0 && v[0] < s->res[0] && v[1] < s->res[1] && v[2] < s->res[2];
+}
+
+// GLSL step(a, b) * step(c, b) * sign(b) per component: the dominant axes of v.
+static void axis_mask(const float v[3], float out[3]) {
+  const float a[3] = {std::fabs(v[0]), std::fabs(v[1]), std::fabs(v[2])};
+  const float mx = (!(a[0] < a[1]) && !(a[0] < a[2])) ? 1.0f : 0.0f;
+  const float my = (!(a[1] < a[0]) && !(a[1] < a[2])) ? 1.0f : 0.0f;
+  const float mz = (!(a[2] < a[0]) && !(a[2] < a[1])) ? 1.0f : 0.0f;
+  out[0] = mx * vtb::gsign(v[0]); out[1] = my * vtb::gsign(v[1]); out[2] = mz * vtb::gsign(v[2]);
+}
+
+extern "C" int vt_job_add_voxel(vt_job* j, float x, float y, float dx, float dy, int32_t restart,
+                                int32_t voxel[3]) {
+  VT_CHECK_ARG(j && voxel, "null argument");
+  int32_t sel[3];
+  float n[3];
+  bool hit = false;
+  int rc = select_voxel(j, x, y, sel, n, &hit);
+  if (rc != VT_OK) return rc;
+  voxel[0] = voxel[1] = voxel[2] = -1;
+  if (!hit) return VT_OK;
+  // addVoxel.vs:16-41: with screen-space motion, the axis of the camera's
+  // right / up vector nearest the dominant motion; otherwise the hit normal
+  if (dx != 0.0f || dy != 0.0f) {
+    const float* M = j->frame.inv_mv;   // row-major: columns are the camera axes
+    const float right[3] = {M[0], M[4], M[8]}, up[3] = {M[1], M[5], M[9]};
+    float ar[3], au[3];
+    axis_mask(right, ar);
+    axis_mask(up, au);
+    const float ax = std::fabs(dx), ay = std::fabs(dy);
+    const float mdx = (!(ax < ay) ? 1.0f : 0.0f) * vtb::gsign(dx);
+    const float mdy = (!(ay < ax) ? 1.0f : 0.0f) * vtb::gsign(dy);
+    for (int i = 0; i < 3; ++i) n[i] = ar[i] * mdx + au[i] * mdy;
+  }
+  int32_t c[3];
+  for (int i = 0; i < 3; ++i) c[i] = sel[i] + (int32_t)n[i];
+  if (!inside(j->scene, c)) return VT_OK;       // imageStore outside the image writes nothing
+  // the new voxel copies the selected voxel's material (the ground's below the volume)
+  int32_t entry = j->set.ground_material + 1;
+  if (inside(j->scene, sel)) {
+    const int64_t idx = (int64_t)sel[0] + (int64_t)j->scene->res[0] * ((int64_t)sel[1] + (int64_t)j->scene->res[1] * sel[2]);
+    uint8_t e = 0;
+    VT_CUDA(cudaMemcpyAsync(&e, j->scene->grid + idx, 1, cudaMemcpyDeviceToHost, j->ctx->stream), "selected voxel");
+    VT_CUDA(cudaStreamSynchronize(j->ctx->stream), "selected voxel");
+    if (e) entry = e;
+  }
+  rc = vt_scene_set_voxel(const_cast<vt_scene*>(j->scene), c[0], c[1], c[2], entry);
+  if (rc != VT_OK) return rc;
+  for (int i = 0; i < 3; ++i) voxel[i] = c[i];
+  if (restart) rc = vt_job_reset(j);
+  return rc;
+}
+
+extern "C" int vt_job_remove_voxel(vt_job* j, float x, float y, int32_t restart, int32_t voxel[3]) {
+  VT_CHECK_ARG(j && voxel, "null argument");
+  int32_t sel[3];
+  float n[3];
+  bool hit = false;
+  int rc = select_voxel(j, x, y, sel, n, &hit);
+  if (rc != VT_OK) return rc;
+  voxel[0] = voxel[1] = voxel[2] = -1;
+  if (!hit || !inside(j->scene, sel)) return VT_OK;   // nothing, or the implicit ground
+  rc = vt_scene_set_voxel(const_cast<vt_scene*>(j->scene), sel[0], sel[1], sel[2], 0);
+  if (rc != VT_OK) return rc;
+  for (int i = 0; i < 3; ++i) voxel[i] = sel[i];
+  if (restart) rc = vt_job_reset(j);
+  return rc;
 }
 
 extern "C" int vt_job_destroy(vt_job* j) {
@@ -1363,6 +1519,10 @@ extern "C" int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_j
 // ------------------------------------------------------------- diagnostics
 extern "C" int vt_diag_trace_rays(vt_job* j, const float* origins, const float* dirs, int64_t n, int32_t* out) {
   VT_CHECK_ARG(j && (n == 0 || (origins && dirs && out)) && n >= 0, "bad argument");
+  {
+    const int rc0 = refresh_job(j);
+    if (rc0 != VT_OK) return rc0;
+  }
   if (n == 0) return VT_OK;
   vt_context* ctx = j->ctx;
   cudaSetDevice(ctx->device);
@@ -1383,6 +1543,10 @@ extern "C" int vt_diag_trace_rays(vt_job* j, const float* origins, const float* 
 
 extern "C" int vt_diag_samples(vt_job* j, int32_t sample, float* rgba, int32_t* hits, uint64_t* counters) {
   VT_CHECK_ARG(j && rgba && sample >= 0, "bad argument");
+  {
+    const int rc0 = refresh_job(j);
+    if (rc0 != VT_OK) return rc0;
+  }
   vt_context* ctx = j->ctx;
   cudaSetDevice(ctx->device);
   const size_t n = (size_t)j->w * j->h;

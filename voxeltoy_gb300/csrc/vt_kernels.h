@@ -109,12 +109,17 @@ cudaError_t launch_trace_rays(const Frame& F, const JobDev& J, const float* orig
                               int64_t n, int32_t* out, cudaStream_t st);
 cudaError_t launch_pick(const Frame& F, const JobDev& J, float x, float y, float* out_dist,
                         int32_t* out_voxel, cudaStream_t st);
+// out: voxel x, y, z, hit (1) as int32 then the face normal as 3 floats.
+cudaError_t launch_select(const Frame& F, const JobDev& J, float x, float y, float frag_z, int32_t* out,
+                          cudaStream_t st);
 cudaError_t launch_resolve(const float4* sum, int32_t w, int32_t h, int32_t samples, float exposure,
                            float inv_gamma, uint32_t flags, float4* out, cudaStream_t st);
 cudaError_t launch_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n,
                             cudaStream_t st);
 
 // ---- scene (vt_scene.cu)
+cudaError_t launch_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t rx, int32_t ry, int32_t bx, int32_t by,
+                             int32_t x, int32_t y, int32_t z, uint8_t entry, cudaStream_t st);
 cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
                                 unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
                                 cudaStream_t st);

@@ -678,6 +678,38 @@ __global__ void k_pick(const Frame F, const JobDev J, float x, float y, float* o
   out_voxel[0] = s.x; out_voxel[1] = s.y; out_voxel[2] = s.z;
 }
 
+// selectVoxel.vs:35-69: generateRay at window depth frag_z (the shader
+// passes cameraNear), AABB clip, traverse, and the basis normal of the hit
+// (voxelSpaceToWorldSpace).  Nothing hit: out[3] = 0.
+__global__ void k_select(const Frame F, const JobDev J, float x, float y, float frag_z, int32_t* out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  Cnt<false> cnt;
+  Rng rng;
+  rng.pixel = 0; rng.sample = 0; rng.call = 0; rng.ox = 0; rng.oy = 0;
+  v3 o, d;
+  generate_ray(F, J, mk3(x, y, frag_z), rng, o, d);
+  out[0] = out[1] = out[2] = -1;
+  out[3] = 0;
+  float* nrm = (float*)(out + 4);
+  nrm[0] = nrm[1] = nrm[2] = 0.0f;
+  const float t = ray_aabb(o, d, ld3(F.bmin), ld3(F.bmax));
+  if (t < 0.0f) return;
+  Dda s;
+  const Grid g = grid_of(F, J);
+  dda_begin(g, s, o + t * d, d);
+  if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
+  if (!dda_hit(F, s)) return;
+  const Basis b = voxel_basis(F, s.x, s.y, s.z, o, d);
+  out[0] = s.x; out[1] = s.y; out[2] = s.z; out[3] = 1;
+  nrm[0] = b.normal.x; nrm[1] = b.normal.y; nrm[2] = b.normal.z;
+}
+
+cudaError_t launch_select(const Frame& F, const JobDev& J, float x, float y, float frag_z, int32_t* out,
+                          cudaStream_t st) {
+  k_select<<<1, 32, 0, st>>>(F, J, x, y, frag_z, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pick(const Frame& F, const JobDev& J, float x, float y, float* out_dist,
                         int32_t* out_voxel, cudaStream_t st) {
   k_pick<<<1, 32, 0, st>>>(F, J, x, y, out_dist, out_voxel);

@@ -67,6 +67,8 @@ struct vt_scene {
   int32_t* emissive = nullptr;
   int64_t n_emissive = 0;
   uint64_t bytes = 0;
+  uint32_t flags = 0;            // creation flags (emissive list policy for edits)
+  uint64_t generation = 0;       // bumped by edits that move device buffers
   std::vector<vt_material> host_palette;
   ~vt_scene();
 };
@@ -92,6 +94,7 @@ struct vt_job {
   float4* comp = nullptr;
   float4* staging = nullptr;
   int32_t samples = 0;
+  uint64_t scene_generation = 0; // scene->generation when frame/dev were built
   vt::Frame frame;
   vt::JobDev dev;
   ~vt_job();
@@ -101,6 +104,8 @@ namespace vt {
 int fail(int code, const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);
 int build_frame(vt_job* j);
+// Rebuilds a job's frame when its scene was edited since (scene->generation).
+int refresh_job(vt_job* j);
 // passes[i] samples per pixel for jobs[i]; kernel 1 = plain, 2 = wavefront.
 int render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int kernel,
                 int tile_pixels, int blocks_per_sm, bool count);

@@ -36,6 +36,24 @@ __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int
   bricks[b] = w;
 }
 
+// One voxel edit: its grid entry and its bit in the padded brick grid.
+__global__ void k_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t rx, int32_t ry, int32_t bx, int32_t by,
+                            int32_t x, int32_t y, int32_t z, uint8_t entry) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)] = entry;
+  const int64_t px = bx + 2, py = by + 2;
+  const int64_t b = (int64_t)((x >> 2) + 1) + px * ((int64_t)((y >> 2) + 1) + py * (int64_t)((z >> 2) + 1));
+  const unsigned long long bit = 1ull << ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4));
+  if (entry) atomicOr(&bricks[b], bit);
+  else atomicAnd(&bricks[b], ~bit);
+}
+
+cudaError_t launch_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t rx, int32_t ry, int32_t bx, int32_t by,
+                             int32_t x, int32_t y, int32_t z, uint8_t entry, cudaStream_t st) {
+  k_set_voxel<<<1, 32, 0, st>>>(grid, bricks, rx, ry, bx, by, x, y, z, entry);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
                                 unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
                                 cudaStream_t st) {

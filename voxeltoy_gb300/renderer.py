@@ -193,6 +193,10 @@ class Scene:
                C.byref(h))
         return cls(ctx, h)
 
+    def set_voxel(self, x: int, y: int, z: int, entry: int):
+        """Edit one voxel: entry 0 empties it, k uses palette[k-1]."""
+        L.call("vt_scene_set_voxel", self.h, x, y, z, entry)
+
     def info(self) -> L.SceneInfo:
         inf = L.SceneInfo()
         L.call("vt_scene_get_info", self.h, C.byref(inf))
@@ -297,6 +301,23 @@ class Job:
         v = (C.c_int32 * 3)()
         L.call("vt_job_pick", self.h, x, y, C.byref(d), v)
         return d.value, tuple(v)
+
+    def select_voxel(self, x: float, y: float):
+        """(voxel, normal) under window point (x, y); voxel (-1, -1, -1) on a miss."""
+        v = (C.c_int32 * 3)()
+        n = (C.c_float * 3)()
+        L.call("vt_job_select_voxel", self.h, x, y, v, n)
+        return tuple(v), tuple(n)
+
+    def add_voxel(self, x: float, y: float, dx: float = 0.0, dy: float = 0.0, restart: bool = True):
+        v = (C.c_int32 * 3)()
+        L.call("vt_job_add_voxel", self.h, x, y, dx, dy, 1 if restart else 0, v)
+        return tuple(v)
+
+    def remove_voxel(self, x: float, y: float, restart: bool = True):
+        v = (C.c_int32 * 3)()
+        L.call("vt_job_remove_voxel", self.h, x, y, 1 if restart else 0, v)
+        return tuple(v)
 
     def samples_diag(self, sample: int):
         n = self.width * self.height
@@ -465,6 +486,30 @@ class Renderer:
         from .formats import encode_pfm
         with open(path, "wb") as f:
             f.write(encode_pfm(self.job.readback()))   # PFM, like the readback, stores the bottom row first
+
+    # Renderer::requestAction (renderer.h:106, actions.cpp:5-52): x, y and dx, dy
+    # are normalised window coordinates with the origin at the top left, as
+    # the reference's UI passes them.
+    PA_SELECT_FOCAL_POINT, PA_SELECT_ACTIVE_VOXEL, PA_ADD_VOXEL, PA_REMOVE_VOXEL = range(4)
+
+    def request_action(self, x: float, y: float, dx: float, dy: float, action: int, restart: bool = True):
+        px, py = x * self.width, (1.0 - y) * self.height
+        vx, vy = dx * self.width, -(dy * self.height)     # the add service flips the motion's y
+        if action == self.PA_SELECT_FOCAL_POINT:
+            if restart:
+                self.job.reset()
+            return self.pick_focal_distance(px, py)
+        if action == self.PA_SELECT_ACTIVE_VOXEL:
+            voxel, normal = self.job.select_voxel(px, py)
+            if voxel[0] >= 0:
+                self._settings.selected_voxel[:] = list(voxel)
+                self.update_render_settings()
+            return voxel, normal
+        if action == self.PA_ADD_VOXEL:
+            return self.job.add_voxel(px, py, vx, vy, restart)
+        if action == self.PA_REMOVE_VOXEL:
+            return self.job.remove_voxel(px, py, restart)
+        raise ValueError(f"unknown action {action}")
 
     # Renderer::requestAction with the focal-distance service
     def pick_focal_distance(self, x: float, y: float):
