@@ -432,3 +432,65 @@ def test_samples_bitexact_ablation(ctx, orc, kind):
         assert not report, "\n".join(report)
     finally:
         close_all(job, scene, env)
+
+
+def _feature_configs():
+    ref = reference_config(seed=6)                         # every quirk, noise-table RNG, thin lens, ground
+    ref_img = reference_config(seed=7)
+    ref_img.env_rgb = S.sky_sun_env(48, 24, peak=200.0)    # + image environment
+    ortho = small_config1(edge=32, w=33, h=29, seed=8)     # orthographic, wireframe, selection
+    ortho.camera.lens_model = L.VT_LENS_ORTHOGRAPHIC
+    ortho.settings.wireframe_opacity = 0.6
+    ortho.settings.wireframe_thickness = 0.05
+    z, y, x = np.argwhere(ortho.voxels > 0)[len(np.argwhere(ortho.voxels > 0)) // 2]
+    ortho.settings.selected_voxel[:] = [int(x), int(y), int(z)]
+    ortho.settings.select_enabled = 1
+    pin = small_config2(edge=40, w=31, h=17, seed=9)        # pinhole, RR, emissive NEE
+    pin.camera.lens_model = L.VT_LENS_PINHOLE
+    return {"reference": ref, "reference_image_env": ref_img, "ortho_wire_select": ortho, "pinhole": pin}
+
+
+@pytest.mark.parametrize("name", ["reference", "reference_image_env", "ortho_wire_select", "pinhole"])
+def test_wavefront_equals_plain_features(ctx, name):
+    """Every camera model, quirk set and RNG through the wavefront kernels
+    gives the same accumulation as the per-pixel kernel (itself bit-exact
+    with the oracle per sample)."""
+    cfg = _feature_configs()[name]
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        ctx.set_kernel(1)
+        job.render(4)
+        a = job.readback().copy()
+        job.reset()
+        ctx.set_kernel(2)
+        job.render(4)
+        np.testing.assert_array_equal(a.view(np.uint32), job.readback().view(np.uint32))
+    finally:
+        ctx.set_kernel(2)
+        close_all(job, scene, env)
+
+
+def test_batch_of_many_jobs_equals_alone(ctx):
+    """More jobs than fit in the kernels' parameter block (the global job
+    table), uneven sizes and different features, rendered alone and in one
+    batch, and an empty batch."""
+    cfgs = [small_config1(edge=16 + 4 * i, w=9 + 5 * i, h=7 + 3 * i, seed=20 + i) for i in range(7)]
+    cfgs += list(_feature_configs().values())
+    made = [gpu_setup(ctx, c) for c in cfgs]
+    try:
+        alone = []
+        for _s, _e, j in made:
+            j.render(3)
+            alone.append(j.readback().copy())
+            j.reset()
+        assert len(made) > 8
+        ctx.render_batch([j for _s, _e, j in made], 3)
+        for (_s, _e, j), want in zip(made, alone):
+            np.testing.assert_array_equal(j.readback().view(np.uint32), want.view(np.uint32))
+        assert ctx.render_batch([], 3) == []
+        before = [j.samples() for _s, _e, j in made]
+        ctx.render_batch([j for _s, _e, j in made], 0)
+        assert [j.samples() for _s, _e, j in made] == before
+    finally:
+        for s, e, j in made:
+            close_all(j, s, e)
