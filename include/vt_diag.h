@@ -53,6 +53,11 @@ VT_API int vt_diag_set_kernel(vt_context* ctx, int32_t kernel);
  * default) or launched one by one (0).  Results are identical. */
 VT_API int vt_diag_set_graphs(vt_context* ctx, int32_t enabled);
 
+/* Wavefront lanes: 2 (the default) runs two independent wavefronts over the
+ * two halves of a launch's samples on two streams, so that one's shading
+ * overlaps the other's DDA; 1 runs one.  Results are identical. */
+VT_API int vt_diag_set_lanes(vt_context* ctx, int32_t lanes);
+
 /* Evaluate a builtin of the renderer on the GPU: fn 0 sin, 1 cos, 2 pow(a, b),
  * 3 acos, 4 atan2(a, b), 5 log2, 6 exp2, 7 float -> half -> float. */
 VT_API int vt_diag_builtins(vt_context* ctx, int32_t fn, const float* a, const float* b,

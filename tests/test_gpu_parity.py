@@ -203,6 +203,23 @@ def test_plain_and_persistent_kernels_agree(ctx):
         close_all(job, scene, env)
 
 
+def test_one_and_two_lanes_agree(ctx):
+    """Two wavefront lanes on two streams give the same bits as one."""
+    cfg = small_config2(edge=40, w=96, h=80, seed=16)     # enough samples for two lanes
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        out = []
+        for lanes in (1, 2):
+            ctx.set_lanes(lanes)
+            job.reset()
+            job.render(3)
+            out.append(job.readback().view(np.uint32).copy())
+        np.testing.assert_array_equal(out[0], out[1])
+    finally:
+        ctx.set_lanes(2)
+        close_all(job, scene, env)
+
+
 def test_graph_rounds_equal_direct_launches(ctx):
     """The wavefront rounds replayed from a captured graph give the same bits
     as the same rounds launched one by one."""

@@ -167,6 +167,7 @@ SIGNATURES = {
     "vt_diag_render_counted": [P, C.c_int32, P, C.POINTER(C.c_int32)],
     "vt_diag_set_kernel": [P, C.c_int32],
     "vt_diag_set_graphs": [P, C.c_int32],
+    "vt_diag_set_lanes": [P, C.c_int32],
     "vt_diag_builtins": [P, C.c_int32, P, P, P, C.c_int64],
     "vt_diag_cdf_from_function": [P, P, C.c_int32, C.c_int32, P, P, fp],
     "vt_diag_env_texels": [P, P, C.c_size_t],

@@ -153,7 +153,11 @@ extern "C" int vt_destroy(vt_context* ctx) {
   ctx->release(ctx->sbuf);
   ctx->release(ctx->wf_ctl);
   if (ctx->h_live) cudaFreeHost(ctx->h_live);
-  if (ctx->rounds_exec) cudaGraphExecDestroy(ctx->rounds_exec);
+  for (cudaGraphExec_t& g : ctx->rounds_exec)
+    if (g) cudaGraphExecDestroy(g);
+  if (ctx->lane_ready) cudaEventDestroy(ctx->lane_ready);
+  if (ctx->lane_done) cudaEventDestroy(ctx->lane_done);
+  if (ctx->lane_stream) cudaStreamDestroy(ctx->lane_stream);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -1110,8 +1114,14 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     ctx->sbuf_items = items;
   }
   if (!ctx->wf_ctl) {
-    int rc = ctx->alloc((void**)&ctx->wf_ctl, kCtlBytes);
+    int rc = ctx->alloc((void**)&ctx->wf_ctl, 2 * kCtlBytes);
     if (rc != VT_OK) return rc;
+  }
+  if (!ctx->lane_stream) {
+    cudaError_t e = cudaStreamCreateWithFlags(&ctx->lane_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_done, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "lane stream");
   }
   if (!ctx->h_live) {
     cudaError_t e = cudaHostAlloc((void**)&ctx->h_live, 64, cudaHostAllocDefault);
@@ -1147,18 +1157,6 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   cudaStream_t st = ctx->stream;
   VT_CUDA(cudaMemcpyAsync(ctx->d_jobs, entries.data(), jbytes, cudaMemcpyHostToDevice, st), "job table");
   VT_CUDA(cudaMemcpyAsync(ctx->d_grids, grids.data(), gbytes, cudaMemcpyHostToDevice, st), "grid table");
-  WfParams P;
-  memset(&P, 0, sizeof(P));
-  P.jobs = ctx->d_jobs;
-  P.n_jobs = (int32_t)entries.size();
-  P.grids = ctx->d_grids;
-  wf_carve(ctx->wf_mem, (size_t)ctx->wf_slots, P);
-  P.n_slots = (int32_t)slots;
-  P.ctl = ctx->wf_ctl;
-  P.next_item = (unsigned long long*)(ctx->wf_ctl + kCtlNextItem);
-  P.n_items = (unsigned long long)items;
-  P.sbuf = ctx->sbuf;
-  P.counters = count ? ctx->d_counters : nullptr;
   WfJobTable table;
   const WfJobTable* T = nullptr;
   if (entries.size() <= (size_t)kWfParamJobs) {
@@ -1169,64 +1167,108 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     }
     T = &table;
   }
-  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, kCtlBytes, st), "wavefront control");   // first stream: empty
+  // Lanes: independent wavefronts over halves of the items, each with half
+  // the path slots, on their own streams, so that one lane's memory-bound
+  // shading overlaps the other's ALU-bound DDA.
+  const int lanes = (ctx->lanes == 2 && items >= 8192 && slots >= 2048) ? 2 : 1;
+  const size_t lane_slots = lanes == 2 ? ((size_t)slots / 2) & ~(size_t)31 : (size_t)slots;   // 256-byte lane bases
+  cudaStream_t lane_st[2] = {st, ctx->lane_stream};
+  WfParams P[2];
+  for (int l = 0; l < lanes; ++l) {
+    memset(&P[l], 0, sizeof(P[l]));
+    P[l].jobs = ctx->d_jobs;
+    P[l].n_jobs = (int32_t)entries.size();
+    P[l].grids = ctx->d_grids;
+    wf_carve((char*)ctx->wf_mem + (size_t)l * lane_slots * kWfSlotBytes, lane_slots, P[l]);
+    P[l].n_slots = (int32_t)lane_slots;
+    P[l].ctl = ctx->wf_ctl + (size_t)l * (kCtlBytes / sizeof(uint32_t));
+    P[l].next_item = (unsigned long long*)(P[l].ctl + kCtlNextItem);
+    P[l].n_items = (unsigned long long)(l + 1 == lanes ? items : items / lanes * (l + 1));
+    P[l].sbuf = ctx->sbuf;
+    P[l].counters = count ? ctx->d_counters : nullptr;
+  }
+  // control words zero (first stream empty), item counters at each lane's first item
+  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, 2 * kCtlBytes, st), "wavefront control");
+  unsigned long long begins[2] = {0ull, (unsigned long long)(items / lanes)};
+  if (lanes == 2)
+    VT_CUDA(cudaMemcpyAsync(P[1].next_item, &begins[1], sizeof(unsigned long long), cudaMemcpyHostToDevice, st),
+            "lane items");   // pageable source: read when the call returns
+  if (lanes == 2) {
+    VT_CUDA(cudaEventRecord(ctx->lane_ready, st), "lane start");
+    VT_CUDA(cudaStreamWaitEvent(ctx->lane_stream, ctx->lane_ready, 0), "lane start");
+  }
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
-  const int bps = blocks_per_sm > 0 ? blocks_per_sm
-                                    : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
+  int bps = blocks_per_sm > 0 ? blocks_per_sm
+                              : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
+  if (lanes == 2 && blocks_per_sm <= 0 && ctx->trace_blocks_per_sm <= 0) bps = std::max(1, bps * 2 / 3);
   const int trace_blocks = ctx->sm_count * bps;
-  // one round: its counters cleared, shade + hit + regen, trace
-  auto round = [&](int par) -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(ctx->wf_ctl + ctl_index(par, 0), 0,
-                                    CTL_PER_PARITY * kCtlStride * sizeof(uint32_t), st);
-    if (e == cudaSuccess) e = launch_wf_shade(P, par, ctx->sm_count * 8, count, st, T);
-    if (e == cudaSuccess) e = launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, count, st, T);
+  // one round of a lane: its counters cleared, shade + hit + regen, trace
+  auto round = [&](int l, int par) -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(P[l].ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t),
+                                    lane_st[l]);
+    if (e == cudaSuccess) e = launch_wf_shade(P[l], par, ctx->sm_count * 8, count, lane_st[l], T);
+    if (e == cudaSuccess) e = launch_wf_trace(P[l], par, trace_blocks, ctx->trace_steps, count, lane_st[l], T);
     return e;
   };
-  // Rounds go in groups of eight (a CUDA graph captured once per launch and
-  // replayed), then the length of the next stream is read back; an empty
-  // stream means every item is done.
+  // Rounds go in groups of eight (a CUDA graph per lane, captured once per
+  // launch and replayed), then the length of each lane's next stream is read
+  // back; an empty stream means the lane's items are done.
   if (ctx->use_graphs) {
-    cudaGraph_t graph = nullptr;
-    VT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "capture rounds");
-    cudaError_t ce = cudaSuccess;
-    for (int r = 0; r < 8 && ce == cudaSuccess; ++r) ce = round(r & 1);
-    const cudaError_t ee = cudaStreamEndCapture(st, &graph);
-    if (ce != cudaSuccess || ee != cudaSuccess) {
-      if (graph) cudaGraphDestroy(graph);
-      return cuda_fail(ce != cudaSuccess ? ce : ee, "capture rounds");
-    }
-    bool updated = false;
-    if (ctx->rounds_exec) {
-      cudaGraphExecUpdateResultInfo info;
-      updated = cudaGraphExecUpdate(ctx->rounds_exec, graph, &info) == cudaSuccess;
+    for (int l = 0; l < lanes; ++l) {
+      cudaGraph_t graph = nullptr;
+      VT_CUDA(cudaStreamBeginCapture(lane_st[l], cudaStreamCaptureModeThreadLocal), "capture rounds");
+      cudaError_t ce = cudaSuccess;
+      for (int r = 0; r < 8 && ce == cudaSuccess; ++r) ce = round(l, r & 1);
+      const cudaError_t ee = cudaStreamEndCapture(lane_st[l], &graph);
+      if (ce != cudaSuccess || ee != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(ce != cudaSuccess ? ce : ee, "capture rounds");
+      }
+      cudaGraphExec_t& exec = ctx->rounds_exec[l];
+      bool updated = false;
+      if (exec) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(exec, graph, &info) == cudaSuccess;
+        if (!updated) {
+          cudaGetLastError();
+          cudaGraphExecDestroy(exec);
+          exec = nullptr;
+        }
+      }
       if (!updated) {
-        cudaGetLastError();
-        cudaGraphExecDestroy(ctx->rounds_exec);
-        ctx->rounds_exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        if (ie != cudaSuccess) {
+          cudaGraphDestroy(graph);
+          exec = nullptr;
+          return cuda_fail(ie, "instantiate rounds");
+        }
       }
+      cudaGraphDestroy(graph);
     }
-    if (!updated) {
-      const cudaError_t ie = cudaGraphInstantiate(&ctx->rounds_exec, graph, 0);
-      if (ie != cudaSuccess) {
-        cudaGraphDestroy(graph);
-        ctx->rounds_exec = nullptr;
-        return cuda_fail(ie, "instantiate rounds");
-      }
-    }
-    cudaGraphDestroy(graph);
   }
-  for (;;) {
-    if (ctx->use_graphs) {
-      VT_CUDA(cudaGraphLaunch(ctx->rounds_exec, st), "wavefront rounds");
-    } else {
-      for (int r = 0; r < 8; ++r) VT_CUDA(round(r & 1), "wavefront round");
+  bool live[2] = {true, lanes == 2};
+  while (live[0] || live[1]) {
+    for (int l = 0; l < lanes; ++l) {
+      if (!live[l]) continue;
+      if (ctx->use_graphs) {
+        VT_CUDA(cudaGraphLaunch(ctx->rounds_exec[l], lane_st[l]), "wavefront rounds");
+      } else {
+        for (int r = 0; r < 8; ++r) VT_CUDA(round(l, r & 1), "wavefront round");
+      }
+      ctx->launches += 8 * 4;
+      VT_CUDA(cudaMemcpyAsync(ctx->h_live + l, P[l].ctl + ctl_index(1, CTL_NEXT_N), sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, lane_st[l]),
+              "stream length");
     }
-    ctx->launches += 8 * 4;
-    VT_CUDA(cudaMemcpyAsync(ctx->h_live, ctx->wf_ctl + ctl_index(1, CTL_NEXT_N), sizeof(uint32_t),
-                            cudaMemcpyDeviceToHost, st),
-            "stream length");
-    VT_CUDA(cudaStreamSynchronize(st), "wavefront rounds");
-    if (*(volatile uint32_t*)ctx->h_live == 0) break;
+    for (int l = 0; l < lanes; ++l) {
+      if (!live[l]) continue;
+      VT_CUDA(cudaStreamSynchronize(lane_st[l]), "wavefront rounds");
+      if (((volatile uint32_t*)ctx->h_live)[l] == 0) live[l] = false;
+    }
+  }
+  if (lanes == 2) {                   // the accumulation waits for both lanes
+    VT_CUDA(cudaEventRecord(ctx->lane_done, ctx->lane_stream), "lane join");
+    VT_CUDA(cudaStreamWaitEvent(st, ctx->lane_done, 0), "lane join");
   }
   long long max_pixels = 0;
   for (const JobEntry& e : entries) max_pixels = std::max<long long>(max_pixels, e.n_pixels);
@@ -1576,6 +1618,12 @@ extern "C" int vt_diag_render_counted(vt_job* j, int32_t passes, uint64_t* count
                           j->ctx->stream), "counters");
   VT_CUDA(cudaStreamSynchronize(j->ctx->stream), "counters");
   if (result) *result = j->samples >= j->set.max_samples ? VT_FINISHED_RENDERING : VT_SAMPLES_PENDING;
+  return VT_OK;
+}
+
+extern "C" int vt_diag_set_lanes(vt_context* ctx, int32_t lanes) {
+  VT_CHECK_ARG(ctx && (lanes == 1 || lanes == 2), "lanes must be 1 or 2");
+  ctx->lanes = lanes;
   return VT_OK;
 }
 

@@ -34,7 +34,7 @@ struct vt_context {
   int64_t wf_slots = 0;
   float4* sbuf = nullptr;        // per-sample outputs of one launch
   int64_t sbuf_items = 0;
-  uint32_t* wf_ctl = nullptr;    // control words (kCtlBytes, layout of ctl_index)
+  uint32_t* wf_ctl = nullptr;    // control words, one kCtlBytes block per lane (layout of ctl_index)
   uint32_t* h_live = nullptr;    // pinned host copy of a live counter
   int64_t max_slots = 1 << 23;   // path slots per launch
   int64_t max_items = 1 << 28;   // samples per launch (sample buffer entries)
@@ -42,8 +42,11 @@ struct vt_context {
   int trace_occupancy = 0;       // occupancy limit of the DDA kernel (cached)
   int trace_steps = 16;          // DDA steps between refills of the trace kernel
   uint64_t launches = 0;         // render kernels launched by this context
-  cudaGraphExec_t rounds_exec = nullptr;   // eight wavefront rounds, replayed until the stream empties
+  cudaGraphExec_t rounds_exec[2] = {nullptr, nullptr};   // per lane: eight rounds, replayed
   bool use_graphs = true;
+  cudaStream_t lane_stream = nullptr;   // the second lane of a wavefront launch
+  cudaEvent_t lane_ready = nullptr, lane_done = nullptr;
+  int lanes = 2;                 // wavefront lanes run side by side (1 or 2)
   unsigned long long* d_counters = nullptr;
   unsigned long long* d_queue = nullptr;
   int32_t* d_error = nullptr;

@@ -86,6 +86,10 @@ class Context:
     def set_kernel(self, kernel: int):
         L.call("vt_diag_set_kernel", self.h, kernel)
 
+    def set_lanes(self, lanes: int):
+        """Wavefront lanes side by side on two streams (2, default) or one."""
+        L.call("vt_diag_set_lanes", self.h, lanes)
+
     def set_graphs(self, enabled: bool):
         """Replay wavefront rounds as a CUDA graph (default) or launch them one by one."""
         L.call("vt_diag_set_graphs", self.h, 1 if enabled else 0)
