@@ -19,8 +19,8 @@ import time
 from pathlib import Path
 
 DEFAULT_GRID = {
-    "path_slots": [1 << 21, 1 << 22, 1 << 23, 1 << 24],
-    "trace_blocks_per_sm": [0],
+    "path_slots": [1 << 22, 1 << 23, 1 << 24, 1 << 25],
+    "trace_blocks_per_sm": [0, 3, 5],
     "trace_steps": [8, 16, 32],
 }
 
