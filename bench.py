@@ -131,6 +131,8 @@ def all_max(world, x: float) -> float:
 
 def workload_config(args):
     from voxeltoy_gb300 import scenes as S
+    if args.workload == "config1":
+        return S.config1(edge=args.edge, width=args.res, height=args.res, spp=args.spp, seed=1)
     return S.config2(edge=args.edge, width=args.res, height=args.res, spp=args.spp, seed=2)
 
 
@@ -201,13 +203,20 @@ def run_reference(args, world, rank):
         "config": config_dict(args, cfg),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "ms_per_step extrapolates the sampled rate to the full 256-spp frame",
+        "note": f"ms_per_step extrapolates the sampled rate to the full {args.spp}-spp frame",
     }
     print(json.dumps(line), flush=True)
     return 0
 
 
 def config_dict(args, cfg) -> dict:
+    if args.workload == "config1":
+        return {"workload": f"config1 plain method, small: {args.edge}^3 union of 8 spheres + ground slab, one "
+                            f"Lambert material (albedo 0.7), constant white sky, {args.res}^2 pinhole, 4 bounces, "
+                            f"no Russian roulette, {args.spp} spp",
+                "grid": args.edge, "width": args.res, "height": args.res, "spp": args.spp, "max_bounces": 4,
+                "paths_per_step": cfg.width * cfg.height * cfg.spp,
+                "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas"}
     return {"workload": f"config2 full shading: {args.edge}^3 fBm 35% occupancy, 17-entry palette "
                         f"(8 Lambert, 8 Torrance-Sparrow, 1 emissive on 2% of voxels), {args.res}^2 thin lens, "
                         f"1024x512 sky+sun env (importance sampled), 8 bounces, RR after 3, {args.spp} spp",
@@ -474,9 +483,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--edge", type=int, default=256)
-    ap.add_argument("--res", type=int, default=1024)
-    ap.add_argument("--spp", type=int, default=256)
+    ap.add_argument("--edge", type=int, default=None, help="grid edge (256; 64 for config1)")
+    ap.add_argument("--res", type=int, default=None, help="image edge (1024; 256 for config1)")
+    ap.add_argument("--spp", type=int, default=None, help="samples per pixel (256; 16 for config1)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 wavefront")
@@ -484,8 +493,9 @@ def main():
     ap.add_argument("--slots", type=int, default=0, help="path slots per launch (skips the autotuner)")
     ap.add_argument("--trace-steps", type=int, default=0, help="DDA steps between refills (with --slots)")
     ap.add_argument("--trace-bps", type=int, default=-1, help="trace blocks per SM, 0 = occupancy (with --slots)")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batching", "serving", "voxelize"],
-                    help="config2 (default, the headline line); batching = 64 uneven scenes in one launch vs "
+    ap.add_argument("--workload", default="config2",
+                    choices=["config2", "config1", "batching", "serving", "voxelize"],
+                    help="config2 (default, the headline line); config1 = the small plain case; batching = 64 uneven scenes in one launch vs "
                          "a loop of plain per-scene launches; serving = Poisson request stream through the "
                          "server; voxelize = 1.3M-triangle mesh into 1024^3, then a 2048^2 render")
     ap.add_argument("--scenes", type=int, default=64, help="batching: number of scenes")
@@ -495,6 +505,10 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up and timed renders of the resident frame (for ncu captures)")
     args = ap.parse_args()
+    small = args.workload == "config1"
+    args.edge = args.edge or (64 if small else 256)
+    args.res = args.res or (256 if small else 1024)
+    args.spp = args.spp or (16 if small else 256)
     if args.impl == "gb300" and not args.profile:
         args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
@@ -506,7 +520,7 @@ def main():
     from voxeltoy_gb300 import _lib as L
 
     torch.cuda.set_device(local)
-    if args.workload != "config2":
+    if args.workload not in ("config2", "config1"):
         runner = {"batching": run_batching, "serving": run_serving, "voxelize": run_voxelize}[args.workload]
         line = runner(args, world, rank, local)
         if rank == 0:
@@ -520,7 +534,7 @@ def main():
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=f"cuda:{local}")
 
     scene = Scene.dense(ctx, cfg.voxels, cfg.palette, flags=cfg.scene_flags)
-    env = Env(ctx, cfg.env_rgb)
+    env = Env(ctx, cfg.env_rgb) if cfg.env_rgb is not None else None
     job = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
     paths = cfg.width * cfg.height * cfg.spp
     tuning = {"path_slots": "default"}
@@ -543,7 +557,9 @@ def main():
             if k >= args.warmup:
                 print(json.dumps({"profile_step_ms": 1e3 * (time.perf_counter() - t0), "paths": paths,
                                   "launches": ctx.launch_count(), "tuning": tuning}), flush=True)
-        job.close(); env.close(); scene.close(); ctx.close()
+        for o in (job, env, scene, ctx):
+            if o is not None:
+                o.close()
         return 0
 
     # event counts of one full frame: the algorithmic bytes of a launch
@@ -583,21 +599,24 @@ def main():
 
     # end to end through the C ABI from pinned host memory
     vox_h = torch.from_numpy(np.ascontiguousarray(cfg.voxels)).pin_memory().numpy()
-    env_h = torch.from_numpy(np.ascontiguousarray(cfg.env_rgb)).pin_memory().numpy()
+    env_h = (torch.from_numpy(np.ascontiguousarray(cfg.env_rgb)).pin_memory().numpy()
+             if cfg.env_rgb is not None else None)
     out_h = torch.empty((cfg.height, cfg.width, 4), dtype=torch.float32).pin_memory().numpy()
-    h2d = vox_h.nbytes + env_h.nbytes + 32 * len(cfg.palette)
+    h2d = vox_h.nbytes + (env_h.nbytes if env_h is not None else 0) + 32 * len(cfg.palette)
     d2h = out_h.nbytes
 
     def e2e_step():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sc = Scene.dense(ctx, vox_h, cfg.palette, flags=cfg.scene_flags)
-        ev = Env(ctx, env_h)
+        ev = Env(ctx, env_h) if env_h is not None else None
         jb = Job(ctx, sc, ev, cfg.camera, cfg.settings, cfg.width, cfg.height)
         jb.render(cfg.spp)
         jb.readback(out=out_h)
         dt = time.perf_counter() - t0
-        jb.close(); ev.close(); sc.close()
+        jb.close(); sc.close()
+        if ev is not None:
+            ev.close()
         return dt
 
     e2e_step()
@@ -615,7 +634,7 @@ def main():
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         t = json.loads(tf.read_text())
-        if (t.get("workload") == "config2" and t.get("grid") == args.edge and t.get("res") == args.res
+        if (t.get("workload") == args.workload and t.get("grid") == args.edge and t.get("res") == args.res
                 and t.get("spp") == args.spp):
             traffic = t["dram_bytes_per_launch"]
     line = {
@@ -641,7 +660,9 @@ def main():
         "clocks": clk.summary(),
         "tuning": tuning,
     }
-    job.close(); env.close(); scene.close(); ctx.close()
+    for o in (job, env, scene, ctx):
+        if o is not None:
+            o.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
