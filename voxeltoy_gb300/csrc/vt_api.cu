@@ -153,8 +153,7 @@ extern "C" int vt_destroy(vt_context* ctx) {
   ctx->release(ctx->sbuf);
   ctx->release(ctx->wf_ctl);
   if (ctx->h_live) cudaFreeHost(ctx->h_live);
-  for (cudaGraphExec_t& g : ctx->rounds_exec)
-    if (g) cudaGraphExecDestroy(g);
+  if (ctx->rounds_exec) cudaGraphExecDestroy(ctx->rounds_exec);
   if (ctx->lane_ready) cudaEventDestroy(ctx->lane_ready);
   if (ctx->lane_done) cudaEventDestroy(ctx->lane_done);
   if (ctx->lane_stream) cudaStreamDestroy(ctx->lane_stream);
@@ -1168,7 +1167,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     T = &table;
   }
   // Lanes: independent wavefronts over halves of the items, each with half
-  // the path slots, on their own streams, so that one lane's memory-bound
+  // the path slots and its own stream, so that one lane's memory-bound
   // shading overlaps the other's ALU-bound DDA.
   const int lanes = (ctx->lanes == 2 && items >= 8192 && slots >= 2048) ? 2 : 1;
   const size_t lane_slots = lanes == 2 ? ((size_t)slots / 2) & ~(size_t)31 : (size_t)slots;   // 256-byte lane bases
@@ -1193,82 +1192,84 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   if (lanes == 2)
     VT_CUDA(cudaMemcpyAsync(P[1].next_item, &begins[1], sizeof(unsigned long long), cudaMemcpyHostToDevice, st),
             "lane items");   // pageable source: read when the call returns
-  if (lanes == 2) {
-    VT_CUDA(cudaEventRecord(ctx->lane_ready, st), "lane start");
-    VT_CUDA(cudaStreamWaitEvent(ctx->lane_stream, ctx->lane_ready, 0), "lane start");
-  }
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
   int bps = blocks_per_sm > 0 ? blocks_per_sm
                               : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
   if (lanes == 2 && blocks_per_sm <= 0 && ctx->trace_blocks_per_sm <= 0) bps = std::max(1, bps * 2 / 3);
   const int trace_blocks = ctx->sm_count * bps;
-  // one round of a lane: its counters cleared, shade + hit + regen, trace
-  auto round = [&](int l, int par) -> cudaError_t {
-    cudaError_t e = cudaMemsetAsync(P[l].ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t),
-                                    lane_st[l]);
-    if (e == cudaSuccess) e = launch_wf_shade(P[l], par, ctx->sm_count * 8, count, lane_st[l], T);
-    if (e == cudaSuccess) e = launch_wf_trace(P[l], par, trace_blocks, ctx->trace_steps, count, lane_st[l], T);
+  // Eight rounds of every lane: per round and lane its counters cleared,
+  // shade + hit + regen, trace.  The second lane's stream forks from the
+  // first and joins it again, so the group is one unit of work on `st` (one
+  // CUDA graph when graphs are on); within it the lanes run free of each
+  // other.
+  auto group = [&]() -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    if (lanes == 2) {
+      e = cudaEventRecord(ctx->lane_ready, st);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->lane_stream, ctx->lane_ready, 0);
+    }
+    for (int r = 0; r < 8 && e == cudaSuccess; ++r) {
+      const int par = r & 1;
+      for (int l = 0; l < lanes && e == cudaSuccess; ++l) {
+        e = cudaMemsetAsync(P[l].ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t),
+                            lane_st[l]);
+        if (e == cudaSuccess) e = launch_wf_shade(P[l], par, ctx->sm_count * 8, count, lane_st[l], T);
+        if (e == cudaSuccess) e = launch_wf_trace(P[l], par, trace_blocks, ctx->trace_steps, count, lane_st[l], T);
+      }
+    }
+    if (e == cudaSuccess && lanes == 2) {
+      e = cudaEventRecord(ctx->lane_done, ctx->lane_stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->lane_done, 0);
+    }
     return e;
   };
-  // Rounds go in groups of eight (a CUDA graph per lane, captured once per
-  // launch and replayed), then the length of each lane's next stream is read
-  // back; an empty stream means the lane's items are done.
   if (ctx->use_graphs) {
-    for (int l = 0; l < lanes; ++l) {
-      cudaGraph_t graph = nullptr;
-      VT_CUDA(cudaStreamBeginCapture(lane_st[l], cudaStreamCaptureModeThreadLocal), "capture rounds");
-      cudaError_t ce = cudaSuccess;
-      for (int r = 0; r < 8 && ce == cudaSuccess; ++r) ce = round(l, r & 1);
-      const cudaError_t ee = cudaStreamEndCapture(lane_st[l], &graph);
-      if (ce != cudaSuccess || ee != cudaSuccess) {
-        if (graph) cudaGraphDestroy(graph);
-        return cuda_fail(ce != cudaSuccess ? ce : ee, "capture rounds");
-      }
-      cudaGraphExec_t& exec = ctx->rounds_exec[l];
-      bool updated = false;
-      if (exec) {
-        cudaGraphExecUpdateResultInfo info;
-        updated = cudaGraphExecUpdate(exec, graph, &info) == cudaSuccess;
-        if (!updated) {
-          cudaGetLastError();
-          cudaGraphExecDestroy(exec);
-          exec = nullptr;
-        }
-      }
+    cudaGraph_t graph = nullptr;
+    VT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "capture rounds");
+    const cudaError_t ce = group();
+    const cudaError_t ee = cudaStreamEndCapture(st, &graph);
+    if (ce != cudaSuccess || ee != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      return cuda_fail(ce != cudaSuccess ? ce : ee, "capture rounds");
+    }
+    cudaGraphExec_t& exec = ctx->rounds_exec;
+    bool updated = false;
+    if (exec) {
+      cudaGraphExecUpdateResultInfo info;
+      updated = cudaGraphExecUpdate(exec, graph, &info) == cudaSuccess;
       if (!updated) {
-        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-        if (ie != cudaSuccess) {
-          cudaGraphDestroy(graph);
-          exec = nullptr;
-          return cuda_fail(ie, "instantiate rounds");
-        }
+        cudaGetLastError();
+        cudaGraphExecDestroy(exec);
+        exec = nullptr;
       }
-      cudaGraphDestroy(graph);
     }
-  }
-  bool live[2] = {true, lanes == 2};
-  while (live[0] || live[1]) {
-    for (int l = 0; l < lanes; ++l) {
-      if (!live[l]) continue;
-      if (ctx->use_graphs) {
-        VT_CUDA(cudaGraphLaunch(ctx->rounds_exec[l], lane_st[l]), "wavefront rounds");
-      } else {
-        for (int r = 0; r < 8; ++r) VT_CUDA(round(l, r & 1), "wavefront round");
+    if (!updated) {
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      if (ie != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        exec = nullptr;
+        return cuda_fail(ie, "instantiate rounds");
       }
-      ctx->launches += 8 * 4;
+    }
+    cudaGraphDestroy(graph);
+  }
+  // Groups run until every lane's next stream is empty (its items are done;
+  // a finished lane's rounds find nothing to do).
+  for (;;) {
+    if (ctx->use_graphs) {
+      VT_CUDA(cudaGraphLaunch(ctx->rounds_exec, st), "wavefront rounds");
+    } else {
+      VT_CUDA(group(), "wavefront rounds");
+    }
+    ctx->launches += (uint64_t)lanes * 8 * 4;
+    for (int l = 0; l < lanes; ++l)
       VT_CUDA(cudaMemcpyAsync(ctx->h_live + l, P[l].ctl + ctl_index(1, CTL_NEXT_N), sizeof(uint32_t),
-                              cudaMemcpyDeviceToHost, lane_st[l]),
+                              cudaMemcpyDeviceToHost, st),
               "stream length");
-    }
-    for (int l = 0; l < lanes; ++l) {
-      if (!live[l]) continue;
-      VT_CUDA(cudaStreamSynchronize(lane_st[l]), "wavefront rounds");
-      if (((volatile uint32_t*)ctx->h_live)[l] == 0) live[l] = false;
-    }
-  }
-  if (lanes == 2) {                   // the accumulation waits for both lanes
-    VT_CUDA(cudaEventRecord(ctx->lane_done, ctx->lane_stream), "lane join");
-    VT_CUDA(cudaStreamWaitEvent(st, ctx->lane_done, 0), "lane join");
+    VT_CUDA(cudaStreamSynchronize(st), "wavefront rounds");
+    bool any = false;
+    for (int l = 0; l < lanes; ++l) any = any || ((volatile uint32_t*)ctx->h_live)[l] != 0;
+    if (!any) break;
   }
   long long max_pixels = 0;
   for (const JobEntry& e : entries) max_pixels = std::max<long long>(max_pixels, e.n_pixels);

@@ -42,7 +42,7 @@ struct vt_context {
   int trace_occupancy = 0;       // occupancy limit of the DDA kernel (cached)
   int trace_steps = 16;          // DDA steps between refills of the trace kernel
   uint64_t launches = 0;         // render kernels launched by this context
-  cudaGraphExec_t rounds_exec[2] = {nullptr, nullptr};   // per lane: eight rounds, replayed
+  cudaGraphExec_t rounds_exec = nullptr;   // eight rounds of every lane, replayed
   bool use_graphs = true;
   cudaStream_t lane_stream = nullptr;   // the second lane of a wavefront launch
   cudaEvent_t lane_ready = nullptr, lane_done = nullptr;
