@@ -658,6 +658,8 @@ def main():
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "bytes_model": "1 B/DDA cell + 16 B/palette record + 8 B/env texel eval + 4 B/CDF probe + "
                                     "4 B/emissive read + 64 B/path framebuffer"},
+        "rates": {"gsegments_per_s": world * float(cnt[6]) / (ms * 1e-3) / 1e9,
+                  "gdda_cells_per_s": world * float(cnt[1]) / (ms * 1e-3) / 1e9},
         "counters_per_frame": {"paths": int(cnt[0]), "dda_cells": int(cnt[1]), "palette": int(cnt[2]),
                                "env_evals": int(cnt[3]), "cdf_probes": int(cnt[4]), "emissive_reads": int(cnt[5]),
                                "segments": int(cnt[6]), "empty_brick_cells": int(cnt[7])},
