@@ -326,6 +326,23 @@ def test_voxelize_bitexact_icosphere(ctx, orc, mode):
         sc.close()
 
 
+def test_emissive_discovery_in_voxel_order(ctx):
+    """Discovery without pruning is exactly the emissive voxels in index
+    order: a ragged volume of many discovery chunks, and one without lights."""
+    rng = np.random.default_rng(31)
+    g = rng.integers(0, 3, size=(61, 97, 150), dtype=np.uint8)          # 887,550 voxels
+    g[rng.random(g.shape) < 0.03] = 3
+    pal = [S.lambert(0.5), S.lambert(0.3), S.lambert(0.8, emission=(2.0, 1.0, 0.5))]
+    sc = Scene.dense(ctx, g, pal, flags=L.VT_SCENE_AUTO_EMISSIVE)
+    dark = Scene.dense(ctx, g, pal[:2] + [S.lambert(0.8)], flags=L.VT_SCENE_AUTO_EMISSIVE)
+    try:
+        np.testing.assert_array_equal(sc.emissive(), np.flatnonzero(g.ravel() == 3).astype(np.int32))
+        assert dark.emissive().size == 0
+    finally:
+        sc.close()
+        dark.close()
+
+
 def test_emissive_pruning_matches_oracle(ctx, orc):
     cfg = small_config2(edge=48)
     sc = Scene.dense(ctx, cfg.voxels, cfg.palette, flags=L.VT_SCENE_AUTO_EMISSIVE | L.VT_SCENE_PRUNE_EMISSIVE)

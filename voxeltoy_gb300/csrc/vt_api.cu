@@ -215,18 +215,26 @@ static void scene_bounds(vt_scene* s) {
 // Emissive-list pruning with the reference's swap-with-last removal order
 // (Renderer::pruneInteriorEmissiveVoxels, src/renderer/import.cpp:180-203);
 // the neighbour tests run on the GPU.
-static int prune_emissive(vt_context* ctx, vt_scene* s, std::vector<int32_t>& list) {
+// `on_device` (nullable): the same list already in device memory.
+static int prune_emissive(vt_context* ctx, vt_scene* s, std::vector<int32_t>& list,
+                          const int32_t* on_device = nullptr) {
   if (list.empty()) return VT_OK;
   const int64_t n = (int64_t)list.size();
   int32_t* d_list = nullptr;
   uint8_t* d_keep = nullptr;
-  int rc = ctx->alloc((void**)&d_list, sizeof(int32_t) * n);
-  if (rc != VT_OK) return rc;
+  int rc = VT_OK;
+  if (!on_device) {
+    rc = ctx->alloc((void**)&d_list, sizeof(int32_t) * n);
+    if (rc != VT_OK) return rc;
+  }
   rc = ctx->alloc((void**)&d_keep, (size_t)n);
   if (rc != VT_OK) { ctx->release(d_list); return rc; }
   std::vector<uint8_t> keep(n);
-  cudaError_t e = cudaMemcpyAsync(d_list, list.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = launch_emissive_flags(s->grid, s->res[0], s->res[1], s->res[2], d_list, n, d_keep, ctx->stream);
+  cudaError_t e = cudaSuccess;
+  if (!on_device)
+    e = cudaMemcpyAsync(d_list, list.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, ctx->stream);
+  const int32_t* dl = on_device ? on_device : d_list;
+  if (e == cudaSuccess) e = launch_emissive_flags(s->grid, s->res[0], s->res[1], s->res[2], dl, n, d_keep, ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(keep.data(), d_keep, (size_t)n, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   ctx->release(d_list);
@@ -270,35 +278,42 @@ static int scene_emissive(vt_context* ctx, vt_scene* s, const int32_t* emissive,
                       vtb::h2f(vtb::f2h(m.emission[2]));
       em[i + 1] = e > 0.0f ? 1 : 0;
     }
-    uint8_t* d_em = nullptr;
-    int32_t* d_out = nullptr;
-    rc = ctx->alloc((void**)&d_em, 256);
+    // voxel order, found on the device (two passes over the grid)
+    const int64_t chunks = emissive_chunks(nvox);
+    void* tmp = nullptr;
+    rc = ctx->alloc(&tmp, 256 + sizeof(uint32_t) * (size_t)(chunks + 1));
     if (rc != VT_OK) return rc;
-    rc = ctx->alloc((void**)&d_out, sizeof(int32_t) * std::max<int64_t>(nvox, 1));
-    if (rc != VT_OK) { ctx->release(d_em); return rc; }
-    unsigned long long cnt = 0;
+    uint8_t* d_em = (uint8_t*)tmp;
+    uint32_t* d_counts = (uint32_t*)((char*)tmp + 256);
+    uint32_t total = 0;   // pageable: the read has completed when the copy returns
     cudaError_t e = cudaMemcpyAsync(d_em, em, 256, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_queue, 0, sizeof(unsigned long long), ctx->stream);
-    if (e == cudaSuccess) e = launch_find_emissive(s->grid, nvox, d_em, d_out, ctx->d_queue, nvox, ctx->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&cnt, ctx->d_queue, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    if (e == cudaSuccess) {
-      list.resize(cnt);
-      if (cnt) e = cudaMemcpy(list.data(), d_out, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = launch_emissive_count(s->grid, nvox, d_em, d_counts, ctx->stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&total, d_counts + chunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    int32_t* d_out = nullptr;
+    if (e == cudaSuccess && total > 0) {
+      rc = ctx->alloc((void**)&d_out, sizeof(int32_t) * (size_t)total);
+      if (rc != VT_OK) { ctx->release(tmp); return rc; }
+      list.resize(total);
+      e = launch_emissive_write(s->grid, nvox, d_em, d_counts, d_out, ctx->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(list.data(), d_out, sizeof(int32_t) * (size_t)total, cudaMemcpyDeviceToHost, ctx->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     }
-    ctx->release(d_em);
+    if (e == cudaSuccess && (flags & VT_SCENE_PRUNE_EMISSIVE)) rc = prune_emissive(ctx, s, list, d_out);
     ctx->release(d_out);
+    ctx->release(tmp);
     if (e != cudaSuccess) return cuda_fail(e, "emissive discovery");
-    std::sort(list.begin(), list.end());
+    if (rc != VT_OK) return rc;
   } else if (n_emissive > 0) {
     VT_CHECK_ARG(emissive, "emissive_indices is null");
     list.assign(emissive, emissive + n_emissive);
     for (int32_t v : list)
       if (v < 0 || (int64_t)v >= nvox) return fail(VT_EINVAL, "emissive index %d out of range", v);
-  }
-  if (flags & VT_SCENE_PRUNE_EMISSIVE) {
-    rc = prune_emissive(ctx, s, list);
-    if (rc != VT_OK) return rc;
+    if (flags & VT_SCENE_PRUNE_EMISSIVE) {
+      rc = prune_emissive(ctx, s, list);
+      if (rc != VT_OK) return rc;
+    }
   }
   ctx->release(s->emissive);
   s->emissive = nullptr;
@@ -330,8 +345,15 @@ static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette
   const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
   rc = ctx->alloc((void**)&s->bricks, sizeof(unsigned long long) * nb);
   if (rc != VT_OK) return rc;
+  // the bricks pass also finds the largest palette entry the volume uses
+  unsigned long long* d_top = ctx->d_queue + 1;
+  VT_CUDA(cudaMemsetAsync(d_top, 0, sizeof(unsigned long long), ctx->stream), "brick build");
   VT_CUDA(launch_build_bricks(s->grid, s->res[0], s->res[1], s->res[2], s->bricks, s->bdim[0], s->bdim[1],
-                              s->bdim[2], ctx->stream), "brick build");
+                              s->bdim[2], d_top, ctx->stream), "brick build");
+  unsigned long long top = 0;   // pageable: the read has completed when the copy returns
+  VT_CUDA(cudaMemcpyAsync(&top, d_top, sizeof(top), cudaMemcpyDeviceToHost, ctx->stream), "brick build");
+  if (top > (unsigned long long)n_palette)
+    return fail(VT_EINVAL, "voxel uses palette entry %d of %d", (int)top, n_palette);
   s->flags = flags;
   rc = scene_emissive(ctx, s, emissive, n_emissive, flags);
   if (rc != VT_OK) return rc;
@@ -367,9 +389,6 @@ extern "C" int vt_scene_create(vt_context* ctx, int32_t rx, int32_t ry, int32_t 
   int rc = scene_alloc(ctx, rx, ry, rz, out, &s);
   if (rc != VT_OK) return rc;
   const int64_t nvox = (int64_t)rx * ry * rz;
-  uint8_t mx = 0;
-  for (int64_t i = 0; i < nvox; ++i) mx = voxels[i] > mx ? voxels[i] : mx;
-  if ((int)mx > n_palette) { delete s; return fail(VT_EINVAL, "voxel uses palette entry %d of %d", mx, n_palette); }
   cudaError_t e = cudaMemcpyAsync(s->grid, voxels, (size_t)nvox, cudaMemcpyHostToDevice, ctx->stream);
   if (e != cudaSuccess) { delete s; return cuda_fail(e, "grid upload"); }
   rc = scene_finish(ctx, s, palette, n_palette, emissive_indices, n_emissive, flags);

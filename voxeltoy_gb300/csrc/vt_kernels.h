@@ -120,14 +120,22 @@ cudaError_t launch_builtins(int32_t fn, const float* a, const float* b, float* o
 // ---- scene (vt_scene.cu)
 cudaError_t launch_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t rx, int32_t ry, int32_t bx, int32_t by,
                              int32_t x, int32_t y, int32_t z, uint8_t entry, cudaStream_t st);
+// max_entry (nullable): receives the largest palette entry of the volume.
 cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
                                 unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
-                                cudaStream_t st);
+                                unsigned long long* max_entry, cudaStream_t st);
 cudaError_t launch_emissive_flags(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
                                   const int32_t* emissive, int64_t n, uint8_t* keep, cudaStream_t st);
-cudaError_t launch_find_emissive(const uint8_t* grid, int64_t n_voxels, const uint8_t* emissive_entry,
-                                 int32_t* out, unsigned long long* count, int64_t capacity,
-                                 cudaStream_t st);
+// Emissive voxels in increasing index order, in two launches:
+// launch_emissive_count leaves in counts[0..chunks) each chunk's first output
+// position and in counts[chunks] the total (counts holds chunks + 1 words,
+// chunks = emissive_chunks(n_voxels)); launch_emissive_write then writes the
+// total indices into out.
+int64_t emissive_chunks(int64_t n_voxels);
+cudaError_t launch_emissive_count(const uint8_t* grid, int64_t n_voxels, const uint8_t* emissive_entry,
+                                  uint32_t* counts, cudaStream_t st);
+cudaError_t launch_emissive_write(const uint8_t* grid, int64_t n_voxels, const uint8_t* emissive_entry,
+                                  const uint32_t* offsets, int32_t* out, cudaStream_t st);
 // Scratch buffers of the environment build (device memory, caller-owned).
 struct EnvScratch {
   float* lum;        // w*h luminance of the FP16 texels

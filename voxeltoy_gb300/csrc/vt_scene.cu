@@ -12,28 +12,37 @@ namespace vt {
 // One thread per brick of the padded brick grid (one border brick on every
 // side).  Voxels outside the volume read as occupied, so the DDA stops on
 // the first voxel beyond the volume without a separate bounds test.
+//
+// With `max_entry`, the largest palette entry of the volume is atomically
+// max-ed into *max_entry (the host checks it against the palette size).
 __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int32_t ry, int32_t rz,
-                               unsigned long long* __restrict__ bricks, int32_t bx, int32_t by, int32_t bz) {
+                               unsigned long long* __restrict__ bricks, int32_t bx, int32_t by, int32_t bz,
+                               unsigned long long* max_entry) {
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t px = bx + 2, py = by + 2, pz = bz + 2;
-  if (b >= px * py * pz) return;
-  const int x0 = ((int)(b % px) - 1) * 4;
-  const int y0 = ((int)((b / px) % py) - 1) * 4;
-  const int z0 = ((int)(b / (px * py)) - 1) * 4;
-  unsigned long long w = 0ull;
-  for (int dz = 0; dz < 4; ++dz) {
-    const int z = z0 + dz;
-    for (int dy = 0; dy < 4; ++dy) {
-      const int y = y0 + dy;
-      for (int dx = 0; dx < 4; ++dx) {
-        const int x = x0 + dx;
-        const bool outside = x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz;
-        const bool set = outside || grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)] != 0;
-        if (set) w |= 1ull << (dx | (dy << 2) | (dz << 4));
+  unsigned top = 0;
+  if (b < px * py * pz) {
+    const int x0 = ((int)(b % px) - 1) * 4;
+    const int y0 = ((int)((b / px) % py) - 1) * 4;
+    const int z0 = ((int)(b / (px * py)) - 1) * 4;
+    unsigned long long w = 0ull;
+    for (int dz = 0; dz < 4; ++dz) {
+      const int z = z0 + dz;
+      for (int dy = 0; dy < 4; ++dy) {
+        const int y = y0 + dy;
+        for (int dx = 0; dx < 4; ++dx) {
+          const int x = x0 + dx;
+          const bool outside = x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz;
+          const unsigned v = outside ? 0u : grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)];
+          top = v > top ? v : top;
+          if (outside || v != 0) w |= 1ull << (dx | (dy << 2) | (dz << 4));
+        }
       }
     }
+    bricks[b] = w;
   }
-  bricks[b] = w;
+  top = __reduce_max_sync(0xffffffffu, top);
+  if (max_entry && (threadIdx.x & 31) == 0 && top) atomicMax(max_entry, (unsigned long long)top);
 }
 
 // One voxel edit: its grid entry and its bit in the padded brick grid.
@@ -56,9 +65,9 @@ cudaError_t launch_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t 
 
 cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
                                 unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
-                                cudaStream_t st) {
+                                unsigned long long* max_entry, cudaStream_t st) {
   const int64_t nb = (int64_t)(bx + 2) * (by + 2) * (bz + 2);
-  k_build_bricks<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(grid, rx, ry, rz, bricks, bx, by, bz);
+  k_build_bricks<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(grid, rx, ry, rz, bricks, bx, by, bz, max_entry);
   return cudaGetLastError();
 }
 
@@ -93,37 +102,104 @@ cudaError_t launch_emissive_flags(const uint8_t* grid, int32_t rx, int32_t ry, i
 }
 
 // Linear indices of voxels whose palette entry emits (emissive_entry[g] != 0),
-// appended in arbitrary order; the host sorts them.
-__global__ void k_find_emissive(const uint8_t* __restrict__ grid, int64_t n_voxels,
-                                const uint8_t* __restrict__ emissive_entry, int32_t* out,
-                                unsigned long long* count, int64_t capacity) {
+// in increasing order: the volume is cut into chunks of kEmChunk voxels; one
+// kernel counts each chunk's emissive voxels, one block turns the counts into
+// chunk offsets, and a second pass over the chunks writes each chunk's
+// indices from its offset, rows of 256 voxels at a time in voxel order.
+constexpr int kEmThreads = 256;
+constexpr int kEmRows = 16;
+constexpr int64_t kEmChunk = (int64_t)kEmThreads * kEmRows;
+
+// Exclusive prefix of `v` over the block (kEmThreads threads); *total gets the sum.
+__device__ __forceinline__ uint32_t block_prefix(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+  for (int w = 0; w < kEmThreads / 32; ++w) {
+    before += w < warp ? warp_sums[w] : 0u;
+    all += warp_sums[w];
+  }
+  __syncthreads();   // warp_sums is reused by the next call
+  *total = all;
+  return before + x - v;
+}
+
+__global__ void k_emissive_count(const uint8_t* __restrict__ grid, int64_t n_voxels,
+                                 const uint8_t* __restrict__ emissive_entry, uint32_t* __restrict__ counts) {
   __shared__ uint8_t s_em[256];
+  __shared__ uint32_t s_warp[kEmThreads / 32];
   for (int i = threadIdx.x; i < 256; i += blockDim.x) s_em[i] = emissive_entry[i];
   __syncthreads();
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_voxels;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    const uint8_t g = grid[i];
-    const bool e = s_em[g] != 0;
-    const unsigned mask = __ballot_sync(__activemask(), e);
-    if (e) {
-      const int lane = threadIdx.x & 31;
-      const int leader = __ffs(mask) - 1;
-      unsigned long long base = 0;
-      if (lane == leader) base = atomicAdd(count, (unsigned long long)__popc(mask));
-      base = __shfl_sync(mask, base, leader);
-      const unsigned long long slot = base + __popc(mask & ((1u << lane) - 1u));
-      if ((int64_t)slot < capacity) out[slot] = (int32_t)i;
-    }
+  const int64_t base = (int64_t)blockIdx.x * kEmChunk;
+  uint32_t c = 0;
+  for (int r = 0; r < kEmRows; ++r) {
+    const int64_t i = base + (int64_t)r * kEmThreads + threadIdx.x;
+    if (i < n_voxels && s_em[grid[i]]) ++c;
+  }
+  uint32_t total;
+  block_prefix(c, s_warp, &total);
+  if (threadIdx.x == 0) counts[blockIdx.x] = total;
+}
+
+// In place: counts[0..n) -> exclusive offsets, counts[n] = total.  One block.
+__global__ void k_emissive_offsets(uint32_t* counts, int64_t n) {
+  __shared__ uint32_t s_warp[kEmThreads / 32];
+  const int64_t per = (n + kEmThreads - 1) / kEmThreads;
+  const int64_t b = (int64_t)threadIdx.x * per, e = b + per < n ? b + per : n;
+  uint32_t sum = 0;
+  for (int64_t i = b; i < e; ++i) sum += counts[i];
+  uint32_t total;
+  uint32_t run = block_prefix(sum, s_warp, &total);
+  for (int64_t i = b; i < e; ++i) {
+    const uint32_t c = counts[i];
+    counts[i] = run;
+    run += c;
+  }
+  if (threadIdx.x == 0) counts[n] = total;
+}
+
+__global__ void k_emissive_write(const uint8_t* __restrict__ grid, int64_t n_voxels,
+                                 const uint8_t* __restrict__ emissive_entry, const uint32_t* __restrict__ offsets,
+                                 int32_t* __restrict__ out) {
+  __shared__ uint8_t s_em[256];
+  __shared__ uint32_t s_warp[kEmThreads / 32];
+  for (int i = threadIdx.x; i < 256; i += blockDim.x) s_em[i] = emissive_entry[i];
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kEmChunk;
+  uint32_t at = offsets[blockIdx.x];
+  for (int r = 0; r < kEmRows; ++r) {
+    const int64_t i = base + (int64_t)r * kEmThreads + threadIdx.x;
+    const bool e = i < n_voxels && s_em[grid[i]];
+    uint32_t total;
+    const uint32_t pre = block_prefix(e ? 1u : 0u, s_warp, &total);
+    if (e) out[at + pre] = (int32_t)i;
+    at += total;
   }
 }
 
-cudaError_t launch_find_emissive(const uint8_t* grid, int64_t n_voxels, const uint8_t* emissive_entry,
-                                 int32_t* out, unsigned long long* count, int64_t capacity,
-                                 cudaStream_t st) {
-  if (n_voxels <= 0) return cudaSuccess;
-  int64_t blocks = (n_voxels + 255) / 256;
-  if (blocks > 152 * 32) blocks = 152 * 32;
-  k_find_emissive<<<(unsigned)blocks, 256, 0, st>>>(grid, n_voxels, emissive_entry, out, count, capacity);
+int64_t emissive_chunks(int64_t n_voxels) { return (n_voxels + kEmChunk - 1) / kEmChunk; }
+
+cudaError_t launch_emissive_count(const uint8_t* grid, int64_t n_voxels, const uint8_t* emissive_entry,
+                                  uint32_t* counts, cudaStream_t st) {
+  const int64_t chunks = emissive_chunks(n_voxels);
+  if (chunks <= 0) return cudaSuccess;
+  k_emissive_count<<<(unsigned)chunks, kEmThreads, 0, st>>>(grid, n_voxels, emissive_entry, counts);
+  k_emissive_offsets<<<1, kEmThreads, 0, st>>>(counts, chunks);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_emissive_write(const uint8_t* grid, int64_t n_voxels, const uint8_t* emissive_entry,
+                                  const uint32_t* offsets, int32_t* out, cudaStream_t st) {
+  const int64_t chunks = emissive_chunks(n_voxels);
+  if (chunks <= 0) return cudaSuccess;
+  k_emissive_write<<<(unsigned)chunks, kEmThreads, 0, st>>>(grid, n_voxels, emissive_entry, offsets, out);
   return cudaGetLastError();
 }
 
