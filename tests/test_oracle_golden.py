@@ -5,14 +5,21 @@ Pins the oracle on the only golden vectors the reference itself documents
 search example of src/shaders/envLight/envMapSample.h:10-21), on the
 published Philox-4x32-10 known-answer vectors, and on analytic answers.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 
+# the examples as tests/golden/reference_examples.json holds them
+with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_examples.json")) as _f:
+    GOLDEN = json.load(_f)
 # image.cpp:107-124 -- one row of intensities and its normalised CDF
-ROW0 = [1, 1, 0, 2, 1, 0, 5]
-ROW0_CDF = [0.0, 0.1, 0.2, 0.2, 0.4, 0.5, 0.5, 1.0]
+ROW0 = GOLDEN["cdf_rows"]["rows"][0]
+ROW0_CDF = GOLDEN["cdf_rows"]["row0_cdf"]
 # image.cpp:144-154 -- second row (sum 12) and a last row taking the total to 150
-ROW1 = [2, 1, 5, 0, 0, 1, 3]
+ROW1 = GOLDEN["cdf_rows"]["rows"][1]
+LAST = GOLDEN["cdf_rows"]["rows"][2]
 
 
 def test_cdf_row_example_reference_float(orc):
@@ -28,8 +35,7 @@ def test_cdf_row_example_fp64(orc, chunk):
 
 
 def test_cdf_marginal_example(orc):
-    last = [128, 0, 0, 0, 0, 0, 0]
-    func = np.array([ROW0, ROW1, last], np.float32)
+    func = np.array([ROW0, ROW1, LAST], np.float32)
     _, cv, _ = orc.cdf_from_function(func)
     np.testing.assert_array_equal(cv, np.float32([0.0, 10 / 150, 22 / 150, 1.0]))
     assert f"{cv[1]:.2f}"[:3] == "0.0" and int(cv[1] * 100) == 6      # the comment's 0.06
@@ -51,22 +57,16 @@ def test_cdf_black_rows_are_uniform(orc):
 
 def test_binary_search_example(orc):
     # envMapSample.h:10-21: u = 0.7 lands in the bracket starting at index 3
-    assert orc.binary_search([0, 0.1, 0.5, 0.6, 0.75, 0.9, 1.0], 0.7) == 3
-    cdf = [0, 0.1, 0.5, 0.6, 0.75, 0.9, 1.0]
-    for u, k in [(0.0, 0), (0.09, 0), (0.1, 1), (0.5999, 2), (0.6, 3), (0.95, 5), (0.99999, 5)]:
-        assert orc.binary_search(cdf, u) == k
+    ex = GOLDEN["binary_search"]
+    assert ex["queries"][0] == [0.7, 3]
+    for u, k in ex["queries"]:
+        assert orc.binary_search(ex["cdf"], u) == k
 
 
 def test_philox_known_answers(orc):
     # Philox-4x32-10 known-answer vectors published with the algorithm (Salmon et al. 2011)
-    cases = [
-        ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
-        ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
-        ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
-         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
-    ]
-    for ctr, key, want in cases:
-        assert orc.philox(ctr, key).tolist() == want
+    for c in GOLDEN["philox4x32_10"]["cases"]:
+        assert orc.philox(c["ctr"], c["key"]).tolist() == c["out"]
 
 
 def test_constant_env_integral(orc):
