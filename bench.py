@@ -361,7 +361,9 @@ def run_serving(args, world, rank, local):
         edge = int(rng.integers(64, 513))
         pool.append(S.sphere_union(edge, None, 300 + i, occupancy=float(rng.uniform(0.1, 0.5))))
     ctx = Context(local)
-    srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4)
+    from voxeltoy_gb300 import _lib as L
+    order = L.VT_SERVE_LEAST_WORK if args.order == "least-work" else L.VT_SERVE_ARRIVAL
+    srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4, order=order)
     resident = []
     reqs = []
     for k in range(n):
@@ -407,7 +409,8 @@ def run_serving(args, world, rank, local):
             "dtype": "f32", "data": "synthetic (seeded request stream)",
             "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s ({n} requests), "
                                    f"sphere-union scenes edge 64-512 (pool of {pool_n}), reuse 0.5, resolution "
-                                   f"256^2-1024^2, 16-1024 spp log-uniform, 4 bounces, 60 GB admission budget",
+                                   f"256^2-1024^2, 16-1024 spp log-uniform, 4 bounces, 60 GB admission budget, "
+                                   f"admission order {args.order}",
                        "requests": n, "offered_mpaths_s": paths / args.duration / 1e6},
             "time_to_spp_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
                                "max": float(lat.max() * 1e3)},
@@ -505,6 +508,8 @@ def main():
     ap.add_argument("--scenes", type=int, default=64, help="batching: number of scenes")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: requests per second")
     ap.add_argument("--duration", type=float, default=5.0, help="serving: seconds of arrivals")
+    ap.add_argument("--order", default="arrival", choices=["arrival", "least-work"],
+                    help="serving: admission order of queued requests")
     ap.add_argument("--check", action="store_true", help="voxelize: compare the occupancy with the oracle")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up and timed renders of the resident frame (for ncu captures)")

@@ -483,7 +483,14 @@ typedef struct vt_server_opts {
   int32_t max_active_jobs;     /* slots traced concurrently                     */
   int32_t passes_per_round;    /* samples per pixel each active job gets per round */
   int32_t path_slots;          /* paths in flight per round, 0 = auto            */
+  int32_t order;               /* which queued request is admitted next:
+                                  VT_SERVE_ARRIVAL (0, first come first served) or
+                                  VT_SERVE_LEAST_WORK (fewest paths w*h*spp first,
+                                  arrival order among equals; under sustained
+                                  overload large requests can wait indefinitely) */
 } vt_server_opts;
+
+enum { VT_SERVE_ARRIVAL = 0, VT_SERVE_LEAST_WORK = 1 };
 
 enum {
   VT_REQ_QUEUED = 0, VT_REQ_RUNNING = 1, VT_REQ_DONE = 2,

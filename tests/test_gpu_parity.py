@@ -6,6 +6,7 @@ same IEEE single-precision operations, for per-sample radiance too.  The
 converged image is compared with the FP64 oracle by relative RMSE <= 1e-3.
 """
 import math
+import time
 
 import numpy as np
 import pytest
@@ -283,6 +284,40 @@ def test_server_results_equal_alone(ctx):
         srv.close()
         for m in made:
             close_all(m[2], m[0], m[1])
+
+
+def test_server_admission_order(ctx):
+    """One slot, a long request holding it, then a large and a small request
+    queued behind it: arrival order finishes the large one first, least-work
+    order the small one; the images do not depend on the order."""
+    cfg = small_config1(edge=24, w=16, h=16, seed=11)
+    scene, _env, job = gpu_setup(ctx, cfg)
+    finished = {}
+    images = {}
+    try:
+        for order in (L.VT_SERVE_ARRIVAL, L.VT_SERVE_LEAST_WORK):
+            srv = Server(ctx, max_active_jobs=1, passes_per_round=4, order=order)
+            try:
+                t0 = time.perf_counter()
+                sub = {}
+                for name, res, spp in (("hold", 256, 256), ("large", 96, 64), ("small", 16, 4)):
+                    sub[name] = (srv.submit(scene, None, cfg.camera, cfg.settings, res, res, spp),
+                                 time.perf_counter() - t0, res)
+                done = {}
+                for name, (t, at, res) in sub.items():
+                    assert srv.wait(t, 120.0) == L.VT_OK
+                    img, secs = srv.result(t, res, res)
+                    done[name] = at + secs
+                    images[(order, name)] = img.view(np.uint32).copy()
+                finished[order] = done
+            finally:
+                srv.close()
+        assert finished[L.VT_SERVE_ARRIVAL]["large"] < finished[L.VT_SERVE_ARRIVAL]["small"]
+        assert finished[L.VT_SERVE_LEAST_WORK]["small"] < finished[L.VT_SERVE_LEAST_WORK]["large"]
+        for name in ("hold", "large", "small"):
+            np.testing.assert_array_equal(images[(L.VT_SERVE_ARRIVAL, name)], images[(L.VT_SERVE_LEAST_WORK, name)])
+    finally:
+        close_all(job, scene)
 
 
 def _tri_soup(seed, n_small=3000, n_large=40, res=(96, 80, 64)):

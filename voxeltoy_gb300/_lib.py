@@ -22,6 +22,7 @@ VT_SCENE_PRUNE_EMISSIVE, VT_SCENE_AUTO_EMISSIVE = 1, 2
 VT_VOXELIZE_THIN, VT_VOXELIZE_FAT = 0, 1
 VT_MESH_VOXEL_SPACE, VT_MESH_FIT_UNIT_CUBE = 0, 1
 VT_LENS_PINHOLE, VT_LENS_THIN_LENS, VT_LENS_ORTHOGRAPHIC = 0, 1, 2
+VT_SERVE_ARRIVAL, VT_SERVE_LEAST_WORK = 0, 1
 VT_BUTTON_ROTATE, VT_BUTTON_PAN = 1, 2
 VT_KEY_FORWARD, VT_KEY_BACK, VT_KEY_RIGHT, VT_KEY_LEFT = 0, 1, 2, 3
 VT_QUIRK_GAMMA_BEFORE_AVERAGE = 1 << 0
@@ -82,7 +83,7 @@ class BatchOpts(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_int32), ("passes_per_round", C.c_int32),
-                ("path_slots", C.c_int32)]
+                ("path_slots", C.c_int32), ("order", C.c_int32)]
 
 
 class ServerStats(C.Structure):

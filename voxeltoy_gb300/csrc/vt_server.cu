@@ -45,6 +45,7 @@ struct Request {
   double t_submit = 0.0, t_done = 0.0;
   int error = VT_OK;
   uint64_t job_bytes() const { return (uint64_t)w * h * sizeof(float4) * 3; }
+  uint64_t paths() const { return (uint64_t)w * h * (uint64_t)spp; }
 };
 
 }  // namespace
@@ -124,25 +125,29 @@ void vt_server::run() {
           ++i;
         }
       }
-      // admission in arrival order
+      // admission: in arrival order, or the request with the fewest paths first
       while (!queue.empty() && (int)active.size() < opts.max_active_jobs) {
-        Request* r = queue.front();
+        size_t at = 0;
+        if (opts.order == VT_SERVE_LEAST_WORK)
+          for (size_t i = 1; i < queue.size(); ++i)
+            if (queue[i]->paths() < queue[at]->paths()) at = i;
+        Request* r = queue[at];
         if (r->cancel) {
-          queue.pop_front();
+          queue.erase(queue.begin() + at);
           r->state = VT_REQ_CANCELLED;
           stats.cancelled++;
           continue;
         }
         const uint64_t alone = r->job_bytes() + r->scene->bytes;
         if (opts.hbm_budget_bytes && alone > opts.hbm_budget_bytes) {
-          queue.pop_front();
+          queue.erase(queue.begin() + at);
           r->state = VT_REQ_FAILED;
           r->error = VT_EBUDGET;
           stats.failed++;
           continue;
         }
         if (!admit_locked(r)) break;   // wait for memory to free up
-        queue.pop_front();
+        queue.erase(queue.begin() + at);
       }
       stats.active = (int32_t)active.size();
       stats.queued = (int32_t)queue.size();
@@ -202,6 +207,7 @@ extern "C" int vt_server_create(vt_context* ctx, const vt_server_opts* opts, vt_
   if (opts) s->opts = *opts;
   if (s->opts.max_active_jobs <= 0) s->opts.max_active_jobs = 64;
   if (s->opts.passes_per_round <= 0) s->opts.passes_per_round = 4;
+  if (s->opts.order != VT_SERVE_LEAST_WORK) s->opts.order = VT_SERVE_ARRIVAL;
   memset(&s->stats, 0, sizeof(s->stats));
   vt_context& L = s->lane;
   L.device = ctx->device;
