@@ -47,6 +47,27 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def l2_copy_gbs(device: int) -> float:
+    """Bandwidth of an L2-resident copy (32 MiB to 32 MiB, read + write bytes,
+    best of 5 runs of 200 copies), the denominator of the L2 fraction."""
+    import torch
+    a = torch.ones(8 << 20, dtype=torch.float32, device=f"cuda:{device}")
+    b = torch.empty_like(a)
+    for _ in range(20):
+        b.copy_(a)
+    best = float("inf")
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(200):
+            b.copy_(a)
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) * 1e-3)
+    return 2 * a.numel() * 4 * 200 / best / 1e9
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region."""
 
@@ -606,6 +627,7 @@ def main():
     value = world * paths / (ms * 1e-3) / 1e6
     launch_ms = float(np.mean(times))
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
+    l2_gbs = l2_copy_gbs(local)
 
     # end to end through the C ABI from pinned host memory
     vox_h = torch.from_numpy(np.ascontiguousarray(cfg.voxels)).pin_memory().numpy()
@@ -662,7 +684,9 @@ def main():
                      "kernel": "k_wf_shade + k_wf_hit + k_wf_regen + k_wf_trace + k_wf_accumulate (one frame = one launch)",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "bytes_model": "1 B/DDA cell + 16 B/palette record + 8 B/env texel eval + 4 B/CDF probe + "
-                                    "4 B/emissive read + 64 B/path framebuffer"},
+                                    "4 B/emissive read + 64 B/path framebuffer",
+                     "l2": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
+                            "peak_source": "L2-resident 32 MiB copy measured in this run (torch copy_)"}},
         "rates": {"gsegments_per_s": world * float(cnt[6]) / (ms * 1e-3) / 1e9,
                   "gdda_cells_per_s": world * float(cnt[1]) / (ms * 1e-3) / 1e9},
         "counters_per_frame": {"paths": int(cnt[0]), "dda_cells": int(cnt[1]), "palette": int(cnt[2]),
