@@ -331,3 +331,23 @@ def test_select_add_remove_services(ctx):
         assert job.remove_voxel(0.0, 0.0) == (-1, -1, -1) or job.pick(0.0, 0.0)[1][0] >= 0
     finally:
         job.close(); scene.close()
+
+
+def test_zero_work_calls(ctx):
+    """Zero passes, an empty batch and a job whose sample cap is reached leave
+    the accumulation untouched; a job without samples reads back zeros."""
+    cfg = small_config1(edge=16, w=8, h=6)
+    cfg.settings.max_samples = 2
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        assert job.render(0) == L.VT_SAMPLES_PENDING and job.samples() == 0
+        assert ctx.render_batch([], 3) == []
+        assert ctx.render_batch([job], 0) == [L.VT_SAMPLES_PENDING] and job.samples() == 0
+        np.testing.assert_array_equal(job.readback(), 0.0)
+        assert job.render(5) == L.VT_FINISHED_RENDERING and job.samples() == 2
+        done = job.readback().copy()
+        assert job.render(3) == L.VT_FINISHED_RENDERING and job.samples() == 2
+        np.testing.assert_array_equal(job.readback(), done)
+    finally:
+        close_all(job, scene, env)
+

@@ -172,6 +172,43 @@ def test_samples_bitexact_ortho_wireframe_selection(ctx, orc):
     _compare_samples(ctx, orc, cfg, samples=(0, 1))
 
 
+def _plain_equals_wavefront(ctx, cfg, passes=3):
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        ctx.set_kernel(1)
+        job.render(passes)
+        a = job.readback().copy()
+        job.reset()
+        ctx.set_kernel(2)
+        job.render(passes)
+        np.testing.assert_array_equal(a.view(np.uint32), job.readback().view(np.uint32))
+    finally:
+        ctx.set_kernel(2)
+        close_all(job, scene, env)
+
+
+@pytest.mark.parametrize("shape", [(23, 37, 50), (5, 64, 9), (61, 7, 30)])
+def test_ragged_volume_bitexact(ctx, orc, shape):
+    """Volumes whose sides differ and are not multiples of the 4-voxel brick:
+    the partial border bricks, the world bounds on the major axis and the
+    emissive list of a cropped grid."""
+    cfg = small_config2(edge=64, w=36, h=28, seed=17)
+    z, y, x = shape
+    cfg.voxels = np.ascontiguousarray(cfg.voxels[:z, :y, :x])
+    _compare_samples(ctx, orc, cfg, samples=(0, 2))
+    _plain_equals_wavefront(ctx, cfg)
+
+
+@pytest.mark.parametrize("fill", [0, 1])
+def test_empty_and_full_volumes(ctx, orc, fill):
+    """Every ray misses (sky only), or every ray stops on the first voxel."""
+    cfg = small_config1(edge=16, w=20, h=16, seed=18)
+    cfg.voxels = np.full((13, 10, 17), fill, np.uint8)
+    img = _compare_samples(ctx, orc, cfg, samples=(0, 1))
+    assert np.isfinite(img).all()
+    _plain_equals_wavefront(ctx, cfg)
+
+
 def test_accumulation_matches_oracle_average(ctx, orc):
     cfg = small_config1(edge=48, w=40, h=32)
     scene, env, job = gpu_setup(ctx, cfg)
