@@ -48,24 +48,27 @@ def peaks() -> dict:
 
 
 def l2_copy_gbs(device: int) -> float:
-    """Bandwidth of an L2-resident copy (32 MiB to 32 MiB, read + write bytes,
-    best of 5 runs of 200 copies), the denominator of the L2 fraction."""
+    """Bandwidth of an L2-resident copy (read + write bytes; the best over
+    8, 16 and 32 MiB buffers and 5 runs of 200 copies each), the denominator
+    of the L2 fraction."""
     import torch
-    a = torch.ones(8 << 20, dtype=torch.float32, device=f"cuda:{device}")
-    b = torch.empty_like(a)
-    for _ in range(20):
-        b.copy_(a)
-    best = float("inf")
-    for _ in range(5):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(200):
+    best_gbs = 0.0
+    for mib in (8, 16, 32):
+        a = torch.ones(mib << 18, dtype=torch.float32, device=f"cuda:{device}")
+        b = torch.empty_like(a)
+        for _ in range(20):
             b.copy_(a)
-        e1.record()
-        e1.synchronize()
-        best = min(best, e0.elapsed_time(e1) * 1e-3)
-    return 2 * a.numel() * 4 * 200 / best / 1e9
+        for _ in range(5):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(200):
+                b.copy_(a)
+            e1.record()
+            e1.synchronize()
+            best_gbs = max(best_gbs, 2 * a.numel() * 4 * 200 / (e0.elapsed_time(e1) * 1e-3) / 1e9)
+        del a, b
+    return best_gbs
 
 
 class ClockSampler:
@@ -686,7 +689,7 @@ def main():
                      "bytes_model": "1 B/DDA cell + 16 B/palette record + 8 B/env texel eval + 4 B/CDF probe + "
                                     "4 B/emissive read + 64 B/path framebuffer",
                      "l2": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
-                            "peak_source": "L2-resident 32 MiB copy measured in this run (torch copy_)"}},
+                            "peak_source": "L2-resident copy (8-32 MiB buffers) measured in this run (torch copy_)"}},
         "rates": {"gsegments_per_s": world * float(cnt[6]) / (ms * 1e-3) / 1e9,
                   "gdda_cells_per_s": world * float(cnt[1]) / (ms * 1e-3) / 1e9},
         "counters_per_frame": {"paths": int(cnt[0]), "dda_cells": int(cnt[1]), "palette": int(cnt[2]),
