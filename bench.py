@@ -517,7 +517,7 @@ def main():
     ap.add_argument("--edge", type=int, default=None, help="grid edge (256; 64 for config1)")
     ap.add_argument("--res", type=int, default=None, help="image edge (1024; 256 for config1)")
     ap.add_argument("--spp", type=int, default=None, help="samples per pixel (256; 16 for config1)")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=16.0)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 wavefront")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
