@@ -522,6 +522,7 @@ def main():
     ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 wavefront")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     ap.add_argument("--slots", type=int, default=0, help="path slots per launch (skips the autotuner)")
+    ap.add_argument("--lanes", type=int, default=2, choices=[1, 2], help="wavefront lanes with --slots")
     ap.add_argument("--trace-steps", type=int, default=0, help="DDA steps between refills (with --slots)")
     ap.add_argument("--trace-bps", type=int, default=-1, help="trace blocks per SM, 0 = occupancy (with --slots)")
     ap.add_argument("--workload", default="config2",
@@ -573,13 +574,14 @@ def main():
     paths = cfg.width * cfg.height * cfg.spp
     tuning = {"path_slots": "default"}
     if args.slots > 0:
+        ctx.set_lanes(args.lanes)
         ctx.set_tuning(args.slots, args.trace_bps, args.trace_steps)
         tuning = {"path_slots": args.slots, "trace_blocks_per_sm": args.trace_bps, "trace_steps": args.trace_steps,
-                  "source": "command line"}
+                  "lanes": args.lanes, "source": "command line"}
     elif not args.no_tune and args.kernel == 2:
         from voxeltoy_gb300 import autotune
         best = autotune.tune(ctx, [job], passes=cfg.spp, repeats=1, use_cache=False)
-        tuning = {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps")}
+        tuning = {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps", "lanes")}
         for r in best.get("sweep", [])[:12]:
             print("tune", json.dumps(r), file=sys.stderr)
     if args.profile:

@@ -4,7 +4,10 @@ Times short renders of the caller's own jobs over a grid of
   path_slots            paths in flight per launch (state + queues per slot)
   trace_blocks_per_sm   resident blocks of the DDA kernel
   trace_steps           DDA steps between ray-pool refills
-and applies the fastest setting to the context.  Results are cached in a JSON
+  lanes                 wavefronts side by side on two streams (2) or one
+and applies the fastest setting to the context.  Path-slot counts above the
+workload's samples collapse to one setting; frames shorter than a few
+milliseconds are timed several times per setting.  Results are cached in a JSON
 file keyed by a workload class (log2 of the largest grid edge, log2 of the
 pixels per pass, number of jobs) so later runs with a similar workload skip
 the sweep.
@@ -22,6 +25,7 @@ DEFAULT_GRID = {
     "path_slots": [1 << 22, 1 << 23, 1 << 24, 1 << 25],
     "trace_blocks_per_sm": [0, 3, 5],
     "trace_steps": [8, 16, 32],
+    "lanes": [2, 1],
 }
 
 
@@ -36,6 +40,11 @@ def workload_key(jobs) -> str:
     edge = max(max(j.scene.info().resolution) for j in jobs)
     pixels = sum(j.width * j.height for j in jobs)
     return f"edge{int(round(math.log2(max(edge, 1))))}_px{int(round(math.log2(max(pixels, 1))))}_jobs{len(jobs)}"
+
+
+def _apply(ctx, setting: dict):
+    ctx.set_lanes(setting.get("lanes", 2))
+    ctx.set_tuning(setting["path_slots"], setting["trace_blocks_per_sm"], setting["trace_steps"])
 
 
 def _time_render(ctx, jobs, passes: int, repeats: int) -> float:
@@ -59,7 +68,8 @@ def _time_render(ctx, jobs, passes: int, repeats: int) -> float:
 def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None, use_cache: bool = True) -> dict:
     """Sweep the grid on `passes` samples per pixel of `jobs`, apply and return
     the best setting ({"path_slots", "trace_blocks_per_sm", "trace_steps",
-    "seconds", "key", "cached"})."""
+    "lanes", "seconds", "key", "cached"}).  `grid` overrides entries of
+    DEFAULT_GRID."""
     key = workload_key(jobs)
     path = cache_path()
     cache = {}
@@ -70,19 +80,26 @@ def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None
             cache = {}
     if use_cache and key in cache:
         best = dict(cache[key])
-        ctx.set_tuning(best["path_slots"], best["trace_blocks_per_sm"], best["trace_steps"])
+        _apply(ctx, best)
         best.update(key=key, cached=True)
         return best
-    grid = grid or DEFAULT_GRID
+    grid = dict(DEFAULT_GRID, **(grid or {}))
+    items = passes * sum(j.width * j.height for j in jobs)
+    slot_list = sorted({min(s, max(items, 32)) for s in grid["path_slots"]})
+    _apply(ctx, {"path_slots": slot_list[-1], "trace_blocks_per_sm": 0, "trace_steps": 16})
+    _time_render(ctx, jobs, passes, 1)                                   # warm: buffers, graphs
+    once = _time_render(ctx, jobs, passes, 1)
+    reps = max(repeats, min(50, math.ceil(0.03 / max(once, 1e-6))))
     results = []
-    for slots, bps, steps in itertools.product(grid["path_slots"], grid["trace_blocks_per_sm"], grid["trace_steps"]):
-        ctx.set_tuning(slots, bps, steps)
-        t = _time_render(ctx, jobs, passes, repeats)
-        results.append((t, slots, bps, steps))
-    results.sort()
-    t, slots, bps, steps = results[0]
-    ctx.set_tuning(slots, bps, steps)
-    best = {"path_slots": slots, "trace_blocks_per_sm": bps, "trace_steps": steps, "seconds": t}
+    for lanes, slots, bps, steps in itertools.product(grid["lanes"], slot_list, grid["trace_blocks_per_sm"],
+                                                      grid["trace_steps"]):
+        setting = {"path_slots": slots, "trace_blocks_per_sm": bps, "trace_steps": steps, "lanes": lanes}
+        _apply(ctx, setting)
+        results.append((_time_render(ctx, jobs, passes, reps), setting))
+    results.sort(key=lambda r: r[0])
+    t, best = results[0]
+    _apply(ctx, best)
+    best = dict(best, seconds=t)
     for j in jobs:
         j.reset()
     if use_cache:
@@ -92,6 +109,5 @@ def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None
             path.write_text(json.dumps(cache, indent=1))
         except OSError:
             pass
-    best.update(key=key, cached=False, sweep=[{"seconds": r[0], "path_slots": r[1], "trace_blocks_per_sm": r[2],
-                                               "trace_steps": r[3]} for r in results])
+    best.update(key=key, cached=False, repeats=reps, sweep=[dict(r[1], seconds=r[0]) for r in results])
     return best
