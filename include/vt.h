@@ -216,6 +216,25 @@ VT_API int vt_scene_read_voxels(const vt_scene* scene, uint8_t* out, size_t byte
 /* Copy the (pruned) emissive list back; *n receives its length. */
 VT_API int vt_scene_read_emissive(const vt_scene* scene, int32_t* out,
                                   int64_t capacity, int64_t* n);
+/* Renderer::getMaterials (src/renderer/renderer.h:120, renderer.cpp:1142-1203):
+ * the scene's materials as the reference's flat float table, each record its
+ * type followed by LambertMaterialData (6 floats) or MetalMaterialData /
+ * PlasticMaterialData (7 floats) (src/renderer/material/material.h:15-33).
+ * A scene made by vt_scene_create_from_offsets returns the caller's table as
+ * given, so its offsets stay valid; any other scene lays its palette out
+ * entry after entry.  *size receives the table's length in floats; with out
+ * NULL nothing else is written. */
+VT_API int vt_scene_read_material_table(const vt_scene* scene, float* out,
+                                        int64_t capacity, int64_t* size);
+/* Renderer::updateMaterialColor / updateMaterialValue (renderer.h:121-122,
+ * renderer.cpp:1205-1235): overwrite n floats of that table from data_offset
+ * on (3 for a colour, 1 for a value).  The range must lie inside the data of
+ * one record, after its type.  Materials of the volume change in place for
+ * later passes; with VT_SCENE_AUTO_EMISSIVE the emissive list follows the
+ * new emissions.  Accumulated samples are kept: vt_job_reset restarts them,
+ * as the reference's material editor does after each change. */
+VT_API int vt_scene_write_material_table(vt_scene* scene, int64_t data_offset,
+                                         const float* values, int32_t n);
 VT_API int vt_scene_destroy(vt_scene* scene);
 
 /* ------------------------------------------------------------ environment -- */

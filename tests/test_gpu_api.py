@@ -351,3 +351,82 @@ def test_zero_work_calls(ctx):
     finally:
         close_all(job, scene, env)
 
+
+def _offsets_scene_inputs():
+    # records: Lambert at 0, metal at 7, an unused Lambert at 15, an emitting Lambert at 22
+    table = np.array([0, 0, 0, 0, 0.8, 0.2, 0.2,
+                      1, 0, 0, 0, 0.9, 0.9, 0.9, 30.0,
+                      0, 0, 0, 0, 0.1, 0.6, 0.3,
+                      0, 2.0, 2.0, 2.0, 0.5, 0.5, 0.5], np.float32)
+    occ = S.sphere_union(24, 5, 41) > 0
+    rng = np.random.default_rng(41)
+    offsets = np.where(occ, rng.choice([0, 7, 22], size=occ.shape, p=[0.6, 0.35, 0.05]), -1).astype(np.int32)
+    return offsets, table
+
+
+def _image(ctx, scene, cfg, passes=2):
+    job = Job(ctx, scene, None, cfg.camera, cfg.settings, cfg.width, cfg.height)
+    try:
+        job.render(passes)
+        return job.readback().view(np.uint32).copy()
+    finally:
+        job.close()
+
+
+def test_material_table_read_and_write(ctx):
+    """Renderer::getMaterials / updateMaterialColor / updateMaterialValue:
+    the caller's table comes back as given, and a scene whose table was
+    written renders like a scene built from the written table."""
+    cfg = small_config1(edge=24, w=24, h=20, seed=41)
+    offsets, table = _offsets_scene_inputs()
+    flags = L.VT_SCENE_AUTO_EMISSIVE
+    sc = Scene.from_offsets(ctx, offsets, table, flags=flags)
+    made = []
+    try:
+        np.testing.assert_array_equal(sc.material_table(), table)
+        sc.write_material_table(4, [0.1, 0.9, 0.1])        # updateMaterialColor: albedo of record 0
+        sc.write_material_table(14, 5.0)                    # updateMaterialValue: roughness of the metal
+        sc.write_material_table(23, [0.0, 0.0, 0.0])        # the emitter goes dark
+        sc.write_material_table(16, [3.0, 3.0, 3.0])        # emission of the unused record: table only
+        want = table.copy()
+        want[4:7] = [0.1, 0.9, 0.1]
+        want[14] = 5.0
+        want[23:26] = 0.0
+        want[16:19] = 3.0
+        np.testing.assert_array_equal(sc.material_table(), want)
+        assert sc.emissive().size == 0
+        ref = Scene.from_offsets(ctx, offsets, want, flags=flags)
+        made.append(ref)
+        np.testing.assert_array_equal(_image(ctx, sc, cfg), _image(ctx, ref, cfg))
+        sc.write_material_table(23, [2.0, 2.0, 2.0])        # and lights up again
+        lit = Scene.from_offsets(ctx, offsets, table, flags=flags)
+        made.append(lit)
+        assert lit.emissive().size > 0
+        np.testing.assert_array_equal(sc.emissive(), lit.emissive())
+        for off, n in ((0, 1), (5, 3), (15, 1), (29, 1), (-1, 1)):   # a type, across records, beyond the table
+            with pytest.raises(L.VtError) as e:
+                sc.write_material_table(off, np.zeros(n))
+            assert e.value.code == L.VT_EINVAL
+    finally:
+        close_all(*made, sc)
+
+
+def test_renderer_material_records(ctx):
+    r = Renderer()
+    r.ctx = ctx
+    try:
+        g = np.zeros((8, 8, 8), np.uint8)
+        g[2:6, 2:6, 2:6] = 1
+        g[0, 0, 0] = 2
+        r.load_volume(g, [S.lambert((0.5, 0.4, 0.3)), S.metal((0.9, 0.8, 0.7), 12.0)], flags=0)
+        recs = r.get_materials()
+        assert [(o, t) for o, t, _ in recs] == [(0, L.VT_MATERIAL_LAMBERT), (7, L.VT_MATERIAL_METAL)]
+        np.testing.assert_allclose(recs[1][2], [0, 0, 0, 0.9, 0.8, 0.7, 12.0], rtol=1e-6)
+        r.update_material_color(4, (0.2, 0.2, 0.2))
+        r.update_material_value(14, 40.0)
+        recs = r.get_materials()
+        np.testing.assert_allclose(recs[0][2][3:], [0.2, 0.2, 0.2], rtol=1e-6)
+        assert recs[1][2][6] == 40.0
+    finally:
+        close_all(r.job, r.scene)
+

@@ -112,6 +112,8 @@ SIGNATURES = {
     "vt_scene_get_info": [P, C.POINTER(SceneInfo)],
     "vt_scene_read_voxels": [P, P, C.c_size_t],
     "vt_scene_read_emissive": [P, P, C.c_int64, C.POINTER(C.c_int64)],
+    "vt_scene_read_material_table": [P, P, C.c_int64, C.POINTER(C.c_int64)],
+    "vt_scene_write_material_table": [P, C.c_int64, P, C.c_int32],
     "vt_scene_destroy": [P],
     "vt_env_create_image": [P, P, C.c_int32, C.c_int32, PP],
     "vt_env_read_cdf": [P, P, C.c_size_t, P, C.c_size_t, fp],

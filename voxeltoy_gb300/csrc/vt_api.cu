@@ -337,6 +337,17 @@ static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette
   }
   s->n_palette = n_palette;
   s->host_palette.assign(palette, palette + n_palette);
+  // the palette as the reference's flat material table, entry after entry
+  s->mat_table.clear();
+  s->mat_offset.assign(n_palette, -1);
+  for (int i = 0; i < n_palette; ++i) {
+    const vt_material& m = palette[i];
+    s->mat_offset[i] = (int64_t)s->mat_table.size();
+    s->mat_table.push_back((float)m.type);
+    s->mat_table.insert(s->mat_table.end(), m.emission, m.emission + 3);
+    s->mat_table.insert(s->mat_table.end(), m.albedo, m.albedo + 3);
+    if (m.type != VT_MATERIAL_LAMBERT) s->mat_table.push_back(m.roughness);
+  }
   int rc = ctx->alloc((void**)&s->palette, sizeof(uint4) * pal.size());
   if (rc != VT_OK) return rc;
   VT_CUDA(cudaMemcpyAsync(s->palette, pal.data(), sizeof(uint4) * pal.size(), cudaMemcpyHostToDevice, ctx->stream),
@@ -435,8 +446,15 @@ extern "C" int vt_scene_create_from_offsets(vt_context* ctx, int32_t rx, int32_t
   }
   std::vector<uint8_t> vox((size_t)nvox);
   for (int64_t i = 0; i < nvox; ++i) vox[i] = offsets[i] >= 0 ? entry[offsets[i]] : 0;
-  return vt_scene_create(ctx, rx, ry, rz, vox.data(), pal.data(), (int32_t)pal.size(), emissive_indices,
-                         n_emissive, flags, out);
+  const int rc = vt_scene_create(ctx, rx, ry, rz, vox.data(), pal.data(), (int32_t)pal.size(), emissive_indices,
+                                 n_emissive, flags, out);
+  if (rc == VT_OK) {   // the caller's table and offsets stay the material table
+    vt_scene* s = *out;
+    s->mat_table.assign(table, table + table_size);
+    s->mat_offset.assign(s->n_palette, -1);
+    for (size_t k = 0; k < used.size(); ++k) s->mat_offset[k] = used[k];
+  }
+  return rc;
 }
 
 // computeMeshTransform (src/renderer/import.cpp:46-64) followed by the vertex
@@ -540,6 +558,76 @@ extern "C" int vt_scene_read_emissive(const vt_scene* s, int32_t* out, int64_t c
     cudaSetDevice(s->ctx->device);
     VT_CUDA(cudaMemcpy(out, s->emissive, sizeof(int32_t) * std::min(capacity, s->n_emissive), cudaMemcpyDeviceToHost),
             "emissive readback");
+  }
+  return VT_OK;
+}
+
+extern "C" int vt_scene_read_material_table(const vt_scene* s, float* out, int64_t capacity, int64_t* size) {
+  VT_CHECK_ARG(s && size, "null argument");
+  *size = (int64_t)s->mat_table.size();
+  if (!out) return VT_OK;
+  if (capacity < *size)
+    return fail(VT_EINVAL, "capacity %lld < %lld floats", (long long)capacity, (long long)*size);
+  std::copy(s->mat_table.begin(), s->mat_table.end(), out);
+  return VT_OK;
+}
+
+// Floats of the record at `at` (type + data), 0 for an unknown type.
+static int64_t record_floats(const std::vector<float>& t, int64_t at) {
+  if (at < 0 || at >= (int64_t)t.size()) return 0;
+  const float type = t[(size_t)at];
+  if (type == 0.0f) return 7;
+  if (type == 1.0f || type == 2.0f) return 8;
+  return 0;
+}
+
+// Emits light: the quantised emission is non-zero (VoxLoader::getMaterialEmisiveness).
+static bool emits(const vt_material& m) {
+  return vtb::h2f(vtb::f2h(m.emission[0])) + vtb::h2f(vtb::f2h(m.emission[1])) +
+         vtb::h2f(vtb::f2h(m.emission[2])) > 0.0f;
+}
+
+extern "C" int vt_scene_write_material_table(vt_scene* s, int64_t off, const float* values, int32_t n) {
+  VT_CHECK_ARG(s && values && n > 0, "bad argument");
+  vt_context* ctx = s->ctx;
+  const std::vector<float>& t = s->mat_table;
+  // the record holding [off, off + n): a palette entry's, or any record of
+  // the table walked as getMaterials walks it
+  int64_t rec = -1;
+  for (int64_t o : s->mat_offset) {
+    const int64_t len = record_floats(t, o);
+    if (len && off > o && off + n <= o + len) { rec = o; break; }
+  }
+  for (int64_t at = 0; rec < 0 && at < (int64_t)t.size();) {
+    const int64_t len = record_floats(t, at);
+    if (!len) break;
+    if (off > at && off + n <= at + len) rec = at;
+    at += len;
+  }
+  if (rec < 0)
+    return fail(VT_EINVAL, "floats [%lld, %lld) are not inside the data of one material record", (long long)off,
+                (long long)(off + n));
+  for (int32_t i = 0; i < n; ++i) s->mat_table[(size_t)(off + i)] = values[i];
+  cudaSetDevice(ctx->device);
+  bool relist = false;
+  for (int32_t k = 0; k < s->n_palette; ++k) {
+    if (s->mat_offset[k] != rec) continue;
+    vt_material m = s->host_palette[k];
+    const float* r = &s->mat_table[(size_t)rec];
+    for (int c = 0; c < 3; ++c) { m.emission[c] = r[1 + c]; m.albedo[c] = r[4 + c]; }
+    m.roughness = m.type == VT_MATERIAL_LAMBERT ? 0.0f : r[7];
+    uint4 q;
+    const int rc = pack_material(m, &q);
+    if (rc != VT_OK) return rc;
+    relist = relist || emits(m) != emits(s->host_palette[k]);
+    s->host_palette[k] = m;
+    // pageable source: staged before the call returns; ordered after earlier passes
+    VT_CUDA(cudaMemcpyAsync(s->palette + k, &q, sizeof(q), cudaMemcpyHostToDevice, ctx->stream), "material update");
+  }
+  if (relist && (s->flags & VT_SCENE_AUTO_EMISSIVE)) {
+    const int rc = scene_emissive(ctx, s, nullptr, 0, s->flags);
+    if (rc != VT_OK) return rc;
+    s->generation++;   // jobs pick up the new list before their next pass
   }
   return VT_OK;
 }

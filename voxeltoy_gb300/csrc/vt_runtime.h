@@ -73,6 +73,10 @@ struct vt_scene {
   uint32_t flags = 0;            // creation flags (emissive list policy for edits)
   uint64_t generation = 0;       // bumped by edits that move device buffers
   std::vector<vt_material> host_palette;
+  // the reference's flat material table and the record offset of each
+  // palette entry in it (-1: the entry has no record there)
+  std::vector<float> mat_table;
+  std::vector<int64_t> mat_offset;
   ~vt_scene();
 };
 

@@ -213,6 +213,18 @@ class Scene:
         L.call("vt_scene_read_voxels", self.h, L.ptr(out), out.nbytes)
         return out
 
+    def material_table(self) -> np.ndarray:
+        """The materials as the reference's flat float table (type + data per record)."""
+        n = C.c_int64()
+        L.call("vt_scene_read_material_table", self.h, None, 0, C.byref(n))
+        out = np.empty(max(1, n.value), np.float32)
+        L.call("vt_scene_read_material_table", self.h, L.ptr(out), out.size, C.byref(n))
+        return out[: n.value]
+
+    def write_material_table(self, data_offset: int, values) -> None:
+        v = np.ascontiguousarray(np.atleast_1d(values), dtype=np.float32)
+        L.call("vt_scene_write_material_table", self.h, data_offset, L.ptr(v), v.size)
+
     def emissive(self) -> np.ndarray:
         n = C.c_int64()
         L.call("vt_scene_read_emissive", self.h, None, 0, C.byref(n))
@@ -454,6 +466,24 @@ class Renderer:
             self.job = Job(self.ctx, scene, self.env, self._camera, self._settings, self.width, self.height)
         if old:
             old.close()
+
+    # Renderer::getMaterials (renderer.h:120): (record offset, type, data) per
+    # record of the flat material table, walked as the reference walks it
+    def get_materials(self) -> list[tuple[int, int, np.ndarray]]:
+        t = self.scene.material_table()
+        out, at = [], 0
+        while at < len(t) and t[at] in (0.0, 1.0, 2.0):
+            n = 6 if t[at] == 0.0 else 7
+            out.append((at, int(t[at]), t[at + 1: at + 1 + n].copy()))
+            at += 1 + n
+        return out
+
+    # Renderer::updateMaterialColor / updateMaterialValue (renderer.h:121-122)
+    def update_material_color(self, data_offset: int, color):
+        self.scene.write_material_table(data_offset, np.asarray(color, np.float32)[:3])
+
+    def update_material_value(self, data_offset: int, value: float):
+        self.scene.write_material_table(data_offset, [value])
 
     # Renderer::resizeFrame (renderer.h:37-40)
     def resize_frame(self, width: int, height: int):
