@@ -19,6 +19,8 @@ INCLUDE = PKG.parent / "include"
 OUT_DIR = PKG / "_lib"
 BUILD_DIR = PKG / "_lib" / "obj"
 LIB = OUT_DIR / "libvoxeltoy.so"
+CLI_SRC = PKG / "host" / "vt_cli.cpp"
+CLI = OUT_DIR / "vt_cli"
 
 SOURCES = ["vt_api.cu", "vt_render.cu", "vt_scene.cu", "vt_server.cu", "vt_fixed.cu", "vt_io.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -47,9 +49,24 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _deps() + [Path(__file__)])
 
 
+def build_cli(force: bool = False) -> Path:
+    """The C++ host program (host/vt_cli.cpp), linked against libvoxeltoy.so
+    with an rpath to it, so that it runs from anywhere."""
+    if not force and CLI.exists() and CLI.stat().st_mtime >= max(LIB.stat().st_mtime, CLI_SRC.stat().st_mtime):
+        return CLI
+    cmd = [os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-Wall", "-I", str(INCLUDE), str(CLI_SRC),
+           "-o", str(CLI), "-L", str(OUT_DIR), "-lvoxeltoy", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        raise RuntimeError("vt_cli build failed:\n" + r.stdout.decode(errors="replace"))
+    return CLI
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
-    """Compile every CUDA source and link libvoxeltoy.so; returns its path."""
+    """Compile every CUDA source and link libvoxeltoy.so (and the C++ host
+    program vt_cli next to it); returns the library's path."""
     if not force and up_to_date():
+        build_cli()
         return LIB
     BUILD_DIR.mkdir(parents=True, exist_ok=True)
     procs = []
@@ -74,6 +91,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
     os.replace(tmp, LIB)
+    build_cli(force=True)
     return LIB
 
 
