@@ -377,6 +377,14 @@ VT_API int vt_job_set_scene(vt_job* job, const vt_scene* scene, const vt_env* en
 VT_API int vt_job_resize(vt_job* job, int32_t width, int32_t height);
 /* Renderer::resetRender (renderer.cpp:941-945). */
 VT_API int vt_job_reset(vt_job* job);
+/* Renderer::Integrator (src/renderer/renderer.h:112-117), switched with the
+ * space key in the reference (renderer.cpp:678-683): VT_INTEGRATOR_PATH_TRACER
+ * (pathTracer.fs, the default) or VT_INTEGRATOR_EDIT_MODE (editMode.fs: white
+ * voxels, a fixed light with one shadow ray, the selected voxel red, the
+ * wireframe overlay; one launch per pass).  A switch restarts the
+ * accumulation. */
+enum { VT_INTEGRATOR_PATH_TRACER = 0, VT_INTEGRATOR_EDIT_MODE = 1 };
+VT_API int vt_job_set_integrator(vt_job* job, int32_t integrator);
 /* Renderer::render (renderer.cpp:556-645) called `passes` times: each pass
  * adds one sample per pixel until max_samples are accumulated.  *result
  * receives VT_SAMPLES_PENDING or VT_FINISHED_RENDERING.  The call queues GPU

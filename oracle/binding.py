@@ -27,7 +27,7 @@ class OrcSettings(C.Structure):
                 ("wireframe_opacity", C.c_float), ("wireframe_thickness", C.c_float),
                 ("background_top", f3), ("background_bottom", f3), ("background_rotation", C.c_float),
                 ("selected_voxel", i3), ("select_enabled", C.c_int32), ("ground_material", C.c_int32),
-                ("quirks", C.c_uint32), ("rng_mode", C.c_int32), ("seed", C.c_uint32)]
+                ("quirks", C.c_uint32), ("rng_mode", C.c_int32), ("seed", C.c_uint32), ("integrator", C.c_int32)]
 
 
 class OrcMaterial(C.Structure):
@@ -100,9 +100,14 @@ def camera(cam) -> OrcCamera:
     return o
 
 
-def settings(s) -> OrcSettings:
+def settings(s, integrator: int = 0) -> OrcSettings:
+    """The oracle's copy of render settings `s`; `integrator` 0 path tracer,
+    1 edit mode (a job attribute in the library, vt_job_set_integrator)."""
     o = OrcSettings()
     for name, _t in OrcSettings._fields_:
+        if name == "integrator":
+            o.integrator = integrator
+            continue
         v = getattr(s, name)
         if hasattr(v, "__len__"):
             getattr(o, name)[:] = list(v)
@@ -158,21 +163,23 @@ def noise_table() -> np.ndarray:
 
 
 def render_samples(cam, s, scene: Scene, env: Env, width: int, height: int, sample: int, precision: int = 32,
-                   threads: int = 0, noise: np.ndarray | None = None):
+                   threads: int = 0, noise: np.ndarray | None = None, integrator: int = 0):
     rgba = np.empty((height, width, 4), np.float32)
     hits = np.empty((height, width, 4), np.int32)
     cnt = np.zeros(8, np.uint64)
-    rc = lib().orc_render_samples(C.byref(camera(cam)), C.byref(settings(s)), C.byref(scene.s), C.byref(env.e),
+    rc = lib().orc_render_samples(C.byref(camera(cam)), C.byref(settings(s, integrator)), C.byref(scene.s),
+                                  C.byref(env.e),
                                   _p(noise), width, height, sample, precision, threads, _p(rgba), _p(hits), _p(cnt))
     assert rc == 0
     return rgba, hits, cnt
 
 
 def render_average(cam, s, scene: Scene, env: Env, width: int, height: int, spp: int, precision: int = 32,
-                   threads: int = 0, rows=(0, 0), noise: np.ndarray | None = None):
+                   threads: int = 0, rows=(0, 0), noise: np.ndarray | None = None, integrator: int = 0):
     rgba = np.zeros((height, width, 4), np.float32)
     cnt = np.zeros(8, np.uint64)
-    rc = lib().orc_render_average(C.byref(camera(cam)), C.byref(settings(s)), C.byref(scene.s), C.byref(env.e),
+    rc = lib().orc_render_average(C.byref(camera(cam)), C.byref(settings(s, integrator)), C.byref(scene.s),
+                                  C.byref(env.e),
                                   _p(noise), width, height, spp, precision, threads, rows[0], rows[1], _p(rgba),
                                   _p(cnt))
     assert rc == 0

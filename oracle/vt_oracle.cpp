@@ -748,8 +748,73 @@ struct Tracer {
     return (((bf.f * L) * M<R>::abs(dot(dir, b.normal))) * mis) / pdf;
   }
 
+  // main() of editMode.fs:58-144: white voxels lit by sqrt(max(0, -d.n)),
+  // halved when the shadow ray towards -lightDirection = (-1, 1, 1) is
+  // blocked (the uniform keeps its initialiser: renderer.cpp:279-280 sets a
+  // name the shader does not declare), the selected voxel red, the
+  // wireframe overlay; the background on a miss; no gamma.
+  void trace_edit(int px, int py, int sample, R out[4], int32_t* hitrec, Counters& C) const {
+    Rng rng;
+    rng.init(S->rng_mode, S->seed, noise, width, px, py, sample);
+    C.c[0] += 1;
+    vec3 o, d;
+    generate_ray(v3<R>(R((float)px + 0.5f), R((float)py + 0.5f), frag_z), rng, &o, &d);
+    if (hitrec) { hitrec[0] = hitrec[1] = hitrec[2] = -1; hitrec[3] = 0; }
+    out[3] = R(1);
+    vec3 col;
+    const R t = aabb(o, d, bmin, bmax);
+    int vs[3], steps;
+    bool ground = false;
+    bool hit = false;
+    if (t >= R(0)) {
+      hit = traverse(o + t * d, d, vs, &ground, &steps, C);
+      if (hitrec) {
+        hitrec[0] = vs[0]; hitrec[1] = vs[1]; hitrec[2] = vs[2];
+        int flags = (hit ? 1 : 0) << 8 | (ground ? 1 : 0) << 9;
+        if (hit) {
+          const Basis b = voxel_basis(vs, o, d);
+          flags |= ((int)b.normal.x + 1) | (((int)b.normal.y + 1) << 2) | (((int)b.normal.z + 1) << 4);
+        }
+        hitrec[3] = flags;
+      }
+    }
+    if (!hit) {                                                          // :79-92
+      col = background(d, C);
+    } else if (S->select_enabled && vs[0] == S->selected_voxel[0] && vs[1] == S->selected_voxel[1] &&
+               vs[2] == S->selected_voxel[2]) {
+      col = v3<R>(R(1), R(0), R(0));                                     // :107-112
+    } else {
+      const Basis b = voxel_basis(vs, o, d, !(S->quirks & Q_UNGUARDED));
+      vec3 albedo = v3<R>(R(1), R(1), R(1));
+      if (S->wireframe_opacity > 0.0f) {                                 // :114-125
+        const vec3 resv = v3<R>(R(res[0]), R(res[1]), R(res[2]));
+        const vec3 vc = ((b.position - bmin) / (bmax - bmin)) * resv;
+        const vec3 uvw = v3<R>(R(vs[0]), R(vs[1]), R(vs[2])) - vc;
+        const R ux = M<R>::abs(dot(v3<R>(b.normal.y, b.normal.z, b.normal.x), uvw));
+        const R uy = M<R>::abs(dot(v3<R>(b.normal.z, b.normal.x, b.normal.y), uvw));
+        const R th = R(S->wireframe_thickness);
+        R wire = (glstep(th, ux) ? R(1) : R(0)) * (glstep(ux, R(1) - th) ? R(1) : R(0));
+        wire = wire * (glstep(th, uy) ? R(1) : R(0));
+        wire = wire * (glstep(uy, R(1) - th) ? R(1) : R(0));
+        wire = (R(1) - R(S->wireframe_opacity)) + R(S->wireframe_opacity) * wire;
+        albedo = albedo * v3<R>(wire, wire, wire);
+      }
+      R lighting = glmax(R(0), dot(-d, b.normal));                      // :129-130
+      lighting = M<R>::sqrt(lighting);
+      int sh[3], st2;
+      bool g2;
+      if (traverse(b.position, v3<R>(R(-1), R(1), R(1)), sh, &g2, &st2, C)) lighting = lighting * R(0.5);
+      col = albedo * lighting;
+    }
+    out[0] = col.x; out[1] = col.y; out[2] = col.z;
+  }
+
   // main() (pathTracer.fs:172-296); returns the per-sample output.
   void trace(int px, int py, int sample, R out[4], int32_t* hitrec, Counters& C) const {
+    if (S->integrator == 1) {
+      trace_edit(px, py, sample, out, hitrec, C);
+      return;
+    }
     Rng rng;
     rng.init(S->rng_mode, S->seed, noise, width, px, py, sample);
     C.c[0] += 1;

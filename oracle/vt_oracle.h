@@ -61,6 +61,7 @@ typedef struct orc_settings {
   uint32_t quirks;
   int32_t rng_mode;     /* 0 philox, 1 noise table */
   uint32_t seed;
+  int32_t integrator;   /* 0 pathTracer.fs, 1 editMode.fs */
 } orc_settings;
 
 /* One material record: type, emission[3], albedo[3], roughness. */

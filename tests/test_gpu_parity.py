@@ -172,6 +172,72 @@ def test_samples_bitexact_ortho_wireframe_selection(ctx, orc):
     _compare_samples(ctx, orc, cfg, samples=(0, 1))
 
 
+def _compare_edit_samples(ctx, orc, cfg, samples=(0, 1), noise=False):
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        job.set_integrator(L.VT_INTEGRATOR_EDIT_MODE)
+        osc, oenv = oracle_setup(orc, cfg, scene, env)
+        table = ctx.noise_table() if noise else None
+        for smp in samples:
+            g_rgba, g_hits, g_cnt = job.samples_diag(smp)
+            o_rgba, o_hits, o_cnt = orc.render_samples(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height,
+                                                       smp, 32, noise=table, integrator=1)
+            np.testing.assert_array_equal(g_hits, o_hits, err_msg=f"first hits, sample {smp}")
+            np.testing.assert_array_equal(g_rgba.view(np.uint32), o_rgba.view(np.uint32), err_msg=f"sample {smp}")
+            np.testing.assert_array_equal(g_cnt[:7], o_cnt[:7])
+        return g_rgba
+    finally:
+        close_all(job, scene, env)
+
+
+def test_edit_mode_samples_bitexact(ctx, orc):
+    """editMode.fs on the GPU against the oracle: selection and wireframe,
+    an environment background, and the reference's quirks (ground hits,
+    noise-table random numbers)."""
+    cfg = small_config1(edge=32, w=33, h=29, seed=21)
+    cfg.settings.wireframe_opacity = 0.6
+    cfg.settings.wireframe_thickness = 0.05
+    occ = np.argwhere(cfg.voxels > 0)
+    z, y, x = occ[len(occ) // 3]
+    cfg.settings.selected_voxel[:] = [int(x), int(y), int(z)]
+    cfg.settings.select_enabled = 1
+    img = _compare_edit_samples(ctx, orc, cfg)
+    assert np.isfinite(img).all() and img[..., :3].max() > 0
+    _compare_edit_samples(ctx, orc, small_config2(edge=40, w=36, h=28, seed=22), samples=(0,))
+    _compare_edit_samples(ctx, orc, reference_config(seed=23), samples=(0, 2), noise=True)
+
+
+def test_edit_mode_accumulation_and_switch(ctx, orc):
+    """Edit-mode passes through vt_job_render and vt_render_batch_fixed
+    accumulate like the oracle's running average; a switch restarts the
+    accumulation."""
+    import ctypes as C
+    cfg = small_config2(edge=32, w=30, h=22, seed=24)
+    scene, env, job = gpu_setup(ctx, cfg)
+    other = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
+    try:
+        job.render(2)
+        assert job.samples() == 2
+        job.set_integrator(L.VT_INTEGRATOR_EDIT_MODE)
+        assert job.samples() == 0
+        job.render(3)
+        got = job.readback()
+        osc, oenv = oracle_setup(orc, cfg, scene, env)
+        want, _ = orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 3, 32, integrator=1)
+        np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
+        other.set_integrator(L.VT_INTEGRATOR_EDIT_MODE)
+        arr = (C.c_void_p * 1)(other.h.value)
+        res = (C.c_int32 * 1)()
+        assert L.load().vt_render_batch_fixed(ctx.h, arr, 1, 3, 0, res) == L.VT_OK
+        np.testing.assert_array_equal(other.readback().view(np.uint32), got.view(np.uint32))
+        job.set_integrator(L.VT_INTEGRATOR_PATH_TRACER)
+        assert job.samples() == 0
+        with pytest.raises(L.VtError):
+            job.set_integrator(2)
+    finally:
+        close_all(other, job, scene, env)
+
+
 def _plain_equals_wavefront(ctx, cfg, passes=3):
     scene, env, job = gpu_setup(ctx, cfg)
     try:

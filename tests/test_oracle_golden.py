@@ -121,3 +121,28 @@ def test_prune_emissive_against_numpy(orc):
         else:
             i += 1
     assert pruned.tolist() == lst
+
+
+def test_edit_mode_known_answers(orc):
+    """editMode.fs on volumes with known answers: an empty volume shows the
+    background (the path tracer's miss), and a full volume seen from above
+    through its top faces shows them white and unshadowed (sqrt(-d.n) of a
+    view from above; the shadow ray leaves upwards, so nothing halves it)."""
+    from voxeltoy_gb300 import scenes as S
+    cfg = S.config1(edge=8, width=12, height=10, spp=1)
+    empty = np.zeros((8, 8, 8), np.uint8)
+    osc, env = orc.Scene(empty, cfg.palette, None), orc.Env()
+    a, ha, _ = orc.render_samples(cfg.camera, cfg.settings, osc, env, 12, 10, 0, integrator=1)
+    b, hb, _ = orc.render_samples(cfg.camera, cfg.settings, osc, env, 12, 10, 0, integrator=0)
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert (ha[..., 3] == 0).all()
+    full = np.ones((8, 8, 8), np.uint8)
+    cam = S.orbit_camera(distance=2000.0, theta_deg=160.0, phi_deg=30.0)   # eye above the volume
+    img, hits, _ = orc.render_samples(cam, cfg.settings, orc.Scene(full, cfg.palette, None), env, 12, 10, 0,
+                                      integrator=1)
+    top = (hits[..., 3] & 0x3f) == (1 | (2 << 2) | (1 << 4))       # normal (0, +1, 0)
+    assert top.any()
+    v = img[top][:, :3]
+    assert np.all(v[:, 0] == v[:, 1]) and np.all(v[:, 1] == v[:, 2])   # white voxels
+    assert np.all((v > 0.5) & (v <= 1.0))        # sqrt(cos) of a view from above, never halved by a shadow
+

@@ -23,6 +23,7 @@ VT_VOXELIZE_THIN, VT_VOXELIZE_FAT = 0, 1
 VT_MESH_VOXEL_SPACE, VT_MESH_FIT_UNIT_CUBE = 0, 1
 VT_LENS_PINHOLE, VT_LENS_THIN_LENS, VT_LENS_ORTHOGRAPHIC = 0, 1, 2
 VT_SERVE_ARRIVAL, VT_SERVE_LEAST_WORK = 0, 1
+VT_INTEGRATOR_PATH_TRACER, VT_INTEGRATOR_EDIT_MODE = 0, 1
 VT_BUTTON_ROTATE, VT_BUTTON_PAN = 1, 2
 VT_KEY_FORWARD, VT_KEY_BACK, VT_KEY_RIGHT, VT_KEY_LEFT = 0, 1, 2, 3
 VT_QUIRK_GAMMA_BEFORE_AVERAGE = 1 << 0
@@ -136,6 +137,7 @@ SIGNATURES = {
     "vt_job_set_scene": [P, P, P],
     "vt_job_resize": [P, C.c_int32, C.c_int32],
     "vt_job_reset": [P],
+    "vt_job_set_integrator": [P, C.c_int32],
     "vt_job_render": [P, C.c_int32, C.POINTER(C.c_int32)],
     "vt_job_synchronize": [P],
     "vt_job_sample_count": [P, C.POINTER(C.c_int32)],

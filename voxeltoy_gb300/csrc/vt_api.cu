@@ -1068,6 +1068,7 @@ int vt::build_frame(vt_job* j) {
   F.seed = S.seed;
   F.width = j->w;
   F.height = j->h;
+  F.integrator = j->integrator;
   j->scene_generation = s->generation;
   JobDev& D = j->dev;
   D.grid = s->grid;
@@ -1173,6 +1174,16 @@ extern "C" int vt_job_reset(vt_job* j) {
   return VT_OK;
 }
 
+extern "C" int vt_job_set_integrator(vt_job* j, int32_t integrator) {
+  VT_CHECK_ARG(j, "job is null");
+  VT_CHECK_ARG(integrator == VT_INTEGRATOR_PATH_TRACER || integrator == VT_INTEGRATOR_EDIT_MODE,
+               "unknown integrator");
+  if (integrator == j->integrator) return VT_OK;
+  j->integrator = integrator;
+  j->frame.integrator = integrator;
+  return vt_job_reset(j);   // the reference restarts the accumulation on a switch (renderer.cpp:678-683)
+}
+
 // Launch `passes` samples per pixel for a set of jobs with the selected kernel.
 int vt::refresh_job(vt_job* j) {
   if (j->scene && j->scene_generation != j->scene->generation) return build_frame(j);
@@ -1187,17 +1198,24 @@ int vt::render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32
     if (rc != VT_OK) return rc;
   }
   if (count) VT_CUDA(cudaMemsetAsync(ctx->d_counters, 0, sizeof(unsigned long long) * C_NUM, ctx->stream), "counters");
-  if (kernel == 1) {
-    for (int i = 0; i < n; ++i) {
-      vt_job* j = jobs[i];
-      for (int k = 0; k < passes[i]; ++k)
-        VT_CUDA(launch_plain(j->frame, j->dev, j->samples + k, 1, count ? ctx->d_counters : nullptr, ctx->stream),
-                "plain render");
-      ctx->launches += (uint64_t)passes[i];
+  // the plain kernel: every job when asked for, and edit-mode jobs always
+  std::vector<vt_job*> wf_jobs;
+  std::vector<int32_t> wf_passes;
+  for (int i = 0; i < n; ++i) {
+    vt_job* j = jobs[i];
+    if (kernel != 1 && j->integrator == VT_INTEGRATOR_PATH_TRACER) {
+      wf_jobs.push_back(j);
+      wf_passes.push_back(passes[i]);
+      continue;
     }
-    return VT_OK;
+    for (int k = 0; k < passes[i]; ++k)
+      VT_CUDA(launch_plain(j->frame, j->dev, j->samples + k, 1, count ? ctx->d_counters : nullptr, ctx->stream),
+              "plain render");
+    ctx->launches += (uint64_t)passes[i];
   }
-  return render_wavefront(ctx, jobs, n, passes, path_slots, blocks_per_sm, count);
+  if (wf_jobs.empty()) return VT_OK;
+  return render_wavefront(ctx, wf_jobs.data(), (int32_t)wf_jobs.size(), wf_passes.data(), path_slots, blocks_per_sm,
+                          count);
 }
 
 // Device buffers of the wavefront for `slots` path slots and `items` samples.

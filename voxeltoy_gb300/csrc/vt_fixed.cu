@@ -155,6 +155,20 @@ extern "C" int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs, int32
   char* base = nullptr;
   int rc = fixed_base(ctx->device, &base);
   if (rc != VT_OK) return rc;
+  for (int i = 0; i < n_jobs; ++i) {   // frames of jobs whose scene was edited (no allocation)
+    rc = refresh_job(jobs[i]);
+    if (rc != VT_OK) return rc;
+  }
+  // edit-mode jobs take the per-pixel kernel, which needs no working memory
+  for (int i = 0; i < n_jobs; ++i) {
+    if (jobs[i]->integrator == VT_INTEGRATOR_PATH_TRACER) continue;
+    for (int32_t k = 0; k < np[i]; ++k) {
+      e = launch_plain(jobs[i]->frame, jobs[i]->dev, jobs[i]->samples + k, 1, nullptr, ctx->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "fixed edit-mode pass");
+    }
+    ctx->launches += (uint64_t)np[i];
+    done[i] = np[i];
+  }
   const int64_t slots_cap = path_slots > 0 ? path_slots : VT_FIXED_MAX_PATH_SLOTS;
   JobEntry entries[VT_FIXED_MAX_JOBS];
   Grid grids[VT_FIXED_MAX_JOBS];

@@ -70,6 +70,7 @@ struct Frame {
   uint32_t seed;
   int32_t width;
   int32_t height;
+  int32_t integrator;        // 0 path tracer (pathTracer.fs), 1 edit mode (editMode.fs)
 };
 
 // What the DDA needs of a volume: extents, bounds, brick layout, step cap.

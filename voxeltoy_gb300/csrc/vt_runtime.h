@@ -101,6 +101,7 @@ struct vt_job {
   float4* comp = nullptr;
   float4* staging = nullptr;
   int32_t samples = 0;
+  int32_t integrator = 0;        // VT_INTEGRATOR_* (Renderer::m_currentIntegrator)
   uint64_t scene_generation = 0; // scene->generation when frame/dev were built
   vt::Frame frame;
   vt::JobDev dev;

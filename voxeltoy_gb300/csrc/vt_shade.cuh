@@ -768,6 +768,22 @@ VT_D bool ext_resolve(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kC
   return true;
 }
 
+// Wireframe factor of a hit (pathTracer.fs:260-270, editMode.fs:113-124):
+// 1 inside the face, 1 - opacity within `thickness` of a voxel edge.
+VT_D float wire_factor(const Frame& F, const Basis& b, int x, int y, int z) {
+  const v3 res = mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
+  const v3 vc = ((b.position - ld3(F.bmin)) / (ld3(F.bmax) - ld3(F.bmin))) * res;
+  const v3 uvw = mk3((float)x, (float)y, (float)z) - vc;
+  const v3 nyzx = mk3(b.normal.y, b.normal.z, b.normal.x);
+  const v3 nzxy = mk3(b.normal.z, b.normal.x, b.normal.y);
+  const float ux = fabsf(dot(nyzx, uvw)), uy = fabsf(dot(nzxy, uvw));
+  const float th = F.wire_thickness;
+  float wire = (vtb::gstep(th, ux) ? 1.0f : 0.0f) * (vtb::gstep(ux, 1.0f - th) ? 1.0f : 0.0f);
+  wire = wire * (vtb::gstep(th, uy) ? 1.0f : 0.0f);
+  wire = wire * (vtb::gstep(uy, 1.0f - th) ? 1.0f : 0.0f);
+  return (1.0f - F.wire_opacity) + F.wire_opacity * wire;
+}
+
 // Second part (pathTracer.fs:220-279): shade a hit that ext_resolve kept.
 // Leaves a shadow segment (ro, sd) and, if p.has_cont, a continuation
 // segment (ro, rd).
@@ -783,17 +799,7 @@ VT_D void ext_hit(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount
   float u_rr;
   v3 lwi = sample_bsdf<kCount>(F, J, m, lwo, p.rng, bs, u_rr);    // :254-258
   if (F.wire_opacity > 0.0f) {                                    // :260-270
-    const v3 res = mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
-    const v3 vc = ((b.position - ld3(F.bmin)) / (ld3(F.bmax) - ld3(F.bmin))) * res;
-    const v3 uvw = mk3((float)e.x, (float)e.y, (float)e.z) - vc;
-    const v3 nyzx = mk3(b.normal.y, b.normal.z, b.normal.x);
-    const v3 nzxy = mk3(b.normal.z, b.normal.x, b.normal.y);
-    const float ux = fabsf(dot(nyzx, uvw)), uy = fabsf(dot(nzxy, uvw));
-    const float th = F.wire_thickness;
-    float wire = (vtb::gstep(th, ux) ? 1.0f : 0.0f) * (vtb::gstep(ux, 1.0f - th) ? 1.0f : 0.0f);
-    wire = wire * (vtb::gstep(th, uy) ? 1.0f : 0.0f);
-    wire = wire * (vtb::gstep(uy, 1.0f - th) ? 1.0f : 0.0f);
-    wire = (1.0f - F.wire_opacity) + F.wire_opacity * wire;
+    const float wire = wire_factor(F, b, e.x, e.y, e.z);
     bs.f = bs.f * mk3(wire, wire, wire);
   }
   const v3 wwi = local_to_world(lwi, b);                          // :273
@@ -837,9 +843,61 @@ VT_D int hit_class(const Frame& F, const JobDev& J, SegEnd e) {
 }
 
 // One complete sample, run to the end by a single lane (megakernel form).
+// The edit-mode integrator (editMode.fs:58-144): white voxels lit by
+// sqrt(max(0, -d.n)), halved (ambientLight 0.5) when a shadow ray towards
+// the fixed light direction (1, -1, -1) is blocked, the selected voxel red,
+// the wireframe overlay; the background where the ray misses.  The reference
+// uploads its light direction to a uniform the shader does not declare
+// (renderer.cpp:279-280 sets "wsLightDir"), so the shader's initialiser is
+// the direction in effect.  No gamma: the shader writes linear values.
+template <bool kCount>
+VT_D float4 edit_sample(const Frame& F, const JobDev& J, int px, int py, int sample, Cnt<kCount>& cnt,
+                        HitRecord* first_hit) {
+  const Grid g = grid_of(F, J);
+  Path p;
+  Dda s;
+  if (first_hit) { first_hit->x = -1; first_hit->y = -1; first_hit->z = -1; first_hit->flags = 0; }
+  float t_enter;
+  if (!path_start(F, J, p, px, py, sample, cnt, t_enter)) return make_float4(p.L.x, p.L.y, p.L.z, 1.0f);
+  dda_begin(g, s, p.ro + t_enter * p.rd, p.rd);
+  if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
+  const bool hit = dda_hit(F, s);
+  Basis b;
+  if (hit) b = voxel_basis(F, s.x, s.y, s.z, p.ro, p.rd, !(F.quirks & Q_UNGUARDED));
+  if (first_hit) {
+    first_hit->x = s.x; first_hit->y = s.y; first_hit->z = s.z;
+    int flags = (hit ? 1 : 0) << 8 | ((hit && s.state != DDA_HIT) ? 1 : 0) << 9;
+    if (hit) {
+      const Basis fb = voxel_basis(F, s.x, s.y, s.z, p.ro, p.rd);
+      flags |= ((int)fb.normal.x + 1) | (((int)fb.normal.y + 1) << 2) | (((int)fb.normal.z + 1) << 4);
+    }
+    first_hit->flags = flags;
+  }
+  if (!hit) {                                                     // :88-92
+    const v3 bg = background(F, J, p.rd, cnt);
+    return make_float4(bg.x, bg.y, bg.z, 1.0f);
+  }
+  if (F.sel_enabled && s.x == F.sel[0] && s.y == F.sel[1] && s.z == F.sel[2])
+    return make_float4(1.0f, 0.0f, 0.0f, 1.0f);                   // :107-112
+  v3 albedo = mk3(1.0f, 1.0f, 1.0f);
+  if (F.wire_opacity > 0.0f) {                                    // :114-125
+    const float wire = wire_factor(F, b, s.x, s.y, s.z);
+    albedo = albedo * mk3(wire, wire, wire);
+  }
+  float lighting = vtb::gmax(0.0f, dot(-p.rd, b.normal));         // :129-130
+  lighting = sqrtf(lighting);
+  cnt.add(C_SEGMENTS, 1);
+  dda_begin(g, s, b.position, mk3(-1.0f, 1.0f, 1.0f));            // :133: -lightDirection
+  if (s.state == DDA_RUNNING) dda_advance(g, s, 0x7fffffff, cnt);
+  if (dda_hit(F, s)) lighting = lighting * 0.5f;
+  const v3 radiance = albedo * lighting;
+  return make_float4(radiance.x, radiance.y, radiance.z, 1.0f);
+}
+
 template <bool kCount>
 VT_D float4 trace_sample(const Frame& F, const JobDev& J, int px, int py, int sample, Cnt<kCount>& cnt,
                          HitRecord* first_hit) {
+  if (F.integrator == 1) return edit_sample(F, J, px, py, sample, cnt, first_hit);
   const Grid g = grid_of(F, J);
   Path p;
   Dda s;

@@ -279,6 +279,10 @@ class Job:
         L.call("vt_job_render", self.h, passes, C.byref(r))
         return r.value
 
+    def set_integrator(self, integrator: int):
+        """VT_INTEGRATOR_PATH_TRACER or VT_INTEGRATOR_EDIT_MODE; restarts the accumulation."""
+        L.call("vt_job_set_integrator", self.h, integrator)
+
     def render_counted(self, passes: int) -> np.ndarray:
         cnt = np.zeros(8, np.uint64)
         r = C.c_int32()
@@ -410,6 +414,7 @@ class Renderer:
         self.job: Job | None = None
         self._camera = default_camera()
         self._settings = default_settings()
+        self._integrator = L.VT_INTEGRATOR_PATH_TRACER
         self.width, self.height = 512, 512
 
     # Renderer::initialize (renderer.h:31)
@@ -464,6 +469,7 @@ class Renderer:
             L.call("vt_job_set_scene", self.job.h, scene.h, self.env.h if self.env else None)
         else:
             self.job = Job(self.ctx, scene, self.env, self._camera, self._settings, self.width, self.height)
+            self.job.set_integrator(self._integrator)
         if old:
             old.close()
 
@@ -500,6 +506,13 @@ class Renderer:
     def update_render_settings(self):
         if self.job:
             self.job.set_settings(self._settings)
+
+    # Renderer::onKeyPress(Qt::Key_Space) (renderer.cpp:678-683): path tracer <-> edit mode
+    def toggle_integrator(self) -> int:
+        self._integrator = 1 - self._integrator
+        if self.job:
+            self.job.set_integrator(self._integrator)
+        return self._integrator
 
     # Renderer::resetRender (renderer.h:76)
     def reset_render(self):
