@@ -6,9 +6,10 @@
 // Parity status: see vt_oracle.h (pinned only by the reference's documented
 // known-answer examples and analytic known answers).
 //
-// The integrator below is written as straight-line code following
-// src/shaders/integrator/pathTracer.fs:172-296 (not as the GPU's state
-// machine), so that a mismatch in the GPU's restructuring shows up.
+// The integrators below are written as straight-line code following
+// src/shaders/integrator/pathTracer.fs:172-296 and editMode.fs:58-144 (not
+// as the GPU's state machine), so that a mismatch in the GPU's
+// restructuring shows up.
 #include "vt_oracle.h"
 
 #include <algorithm>
