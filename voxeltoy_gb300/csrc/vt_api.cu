@@ -278,18 +278,23 @@ static int scene_emissive(vt_context* ctx, vt_scene* s, const int32_t* emissive,
                       vtb::h2f(vtb::f2h(m.emission[2]));
       em[i + 1] = e > 0.0f ? 1 : 0;
     }
+    bool lit = false;   // no emitting entry: an empty list without a pass over the grid
+    for (int i = 1; i <= n_palette; ++i) lit = lit || em[i] != 0;
     // voxel order, found on the device (two passes over the grid)
-    const int64_t chunks = emissive_chunks(nvox);
+    const int64_t chunks = lit ? emissive_chunks(nvox) : 0;
     void* tmp = nullptr;
     rc = ctx->alloc(&tmp, 256 + sizeof(uint32_t) * (size_t)(chunks + 1));
     if (rc != VT_OK) return rc;
     uint8_t* d_em = (uint8_t*)tmp;
     uint32_t* d_counts = (uint32_t*)((char*)tmp + 256);
     uint32_t total = 0;   // pageable: the read has completed when the copy returns
-    cudaError_t e = cudaMemcpyAsync(d_em, em, 256, cudaMemcpyHostToDevice, ctx->stream);
-    if (e == cudaSuccess) e = launch_emissive_count(s->grid, nvox, d_em, d_counts, ctx->stream);
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(&total, d_counts + chunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaSuccess;
+    if (lit) {
+      e = cudaMemcpyAsync(d_em, em, 256, cudaMemcpyHostToDevice, ctx->stream);
+      if (e == cudaSuccess) e = launch_emissive_count(s->grid, nvox, d_em, d_counts, ctx->stream);
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(&total, d_counts + chunks, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    }
     int32_t* d_out = nullptr;
     if (e == cudaSuccess && total > 0) {
       rc = ctx->alloc((void**)&d_out, sizeof(int32_t) * (size_t)total);

@@ -25,20 +25,41 @@ __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int
     const int x0 = ((int)(b % px) - 1) * 4;
     const int y0 = ((int)((b / px) % py) - 1) * 4;
     const int z0 = ((int)(b / (px * py)) - 1) * 4;
+    // rows of four voxels as one aligned 32-bit word where the brick's x
+    // range lies inside the volume and rows start on 4-byte boundaries: the
+    // sixteen row loads are independent
+    const bool words = (rx & 3) == 0 && x0 >= 0 && x0 + 4 <= rx;
     unsigned long long w = 0ull;
-    for (int dz = 0; dz < 4; ++dz) {
-      const int z = z0 + dz;
-      for (int dy = 0; dy < 4; ++dy) {
-        const int y = y0 + dy;
-        for (int dx = 0; dx < 4; ++dx) {
-          const int x = x0 + dx;
-          const bool outside = x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz;
-          const unsigned v = outside ? 0u : grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)];
-          top = v > top ? v : top;
-          if (outside || v != 0) w |= 1ull << (dx | (dy << 2) | (dz << 4));
+    unsigned tops = 0u;   // byte-wise maximum of the word rows
+    if (words) {
+#pragma unroll
+      for (int r = 0; r < 16; ++r) {
+        const int y = y0 + (r & 3), z = z0 + (r >> 2);
+        const bool in = y >= 0 && z >= 0 && y < ry && z < rz;
+        const uint32_t v4 =
+            in ? *reinterpret_cast<const uint32_t*>(grid + (size_t)x0 + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z))
+               : 0u;
+        tops = __vmaxu4(tops, v4);
+        uint32_t m = __vcmpne4(v4, 0u) & 0x01010101u;   // bit 0 of each non-zero byte
+        m = (m | (m >> 7) | (m >> 14) | (m >> 21)) & 0xfu;
+        w |= (unsigned long long)(in ? m : 0xfu) << (4 * r);   // rows outside the volume read as set
+      }
+    } else {
+      for (int dz = 0; dz < 4; ++dz) {
+        const int z = z0 + dz;
+        for (int dy = 0; dy < 4; ++dy) {
+          const int y = y0 + dy;
+          for (int dx = 0; dx < 4; ++dx) {
+            const int x = x0 + dx;
+            const bool outside = x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz;
+            const unsigned v = outside ? 0u : grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)];
+            top = v > top ? v : top;
+            if (outside || v != 0) w |= 1ull << (dx | (dy << 2) | (dz << 4));
+          }
         }
       }
     }
+    for (int k = 0; k < 32; k += 8) top = max(top, (tops >> k) & 0xffu);
     bricks[b] = w;
   }
   top = __reduce_max_sync(0xffffffffu, top);
@@ -110,7 +131,8 @@ constexpr int kEmThreads = 256;
 constexpr int kEmRows = 16;
 constexpr int64_t kEmChunk = (int64_t)kEmThreads * kEmRows;
 
-// Exclusive prefix of `v` over the block (kEmThreads threads); *total gets the sum.
+// Exclusive prefix of `v` over the block (kThreads threads); *total gets the sum.
+template <int kThreads = kEmThreads>
 __device__ __forceinline__ uint32_t block_prefix(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v;
@@ -122,7 +144,7 @@ __device__ __forceinline__ uint32_t block_prefix(uint32_t v, uint32_t* warp_sums
   if (lane == 31) warp_sums[warp] = x;
   __syncthreads();
   uint32_t before = 0, all = 0;
-  for (int w = 0; w < kEmThreads / 32; ++w) {
+  for (int w = 0; w < kThreads / 32; ++w) {
     before += w < warp ? warp_sums[w] : 0u;
     all += warp_sums[w];
   }
@@ -148,15 +170,17 @@ __global__ void k_emissive_count(const uint8_t* __restrict__ grid, int64_t n_vox
   if (threadIdx.x == 0) counts[blockIdx.x] = total;
 }
 
-// In place: counts[0..n) -> exclusive offsets, counts[n] = total.  One block.
-__global__ void k_emissive_offsets(uint32_t* counts, int64_t n) {
-  __shared__ uint32_t s_warp[kEmThreads / 32];
-  const int64_t per = (n + kEmThreads - 1) / kEmThreads;
+// In place: counts[0..n) -> exclusive offsets, counts[n] = total.  One block
+// of kScanThreads threads, each over a contiguous run of counts.
+constexpr int kScanThreads = 1024;
+__global__ void __launch_bounds__(kScanThreads) k_emissive_offsets(uint32_t* counts, int64_t n) {
+  __shared__ uint32_t s_warp[kScanThreads / 32];
+  const int64_t per = (n + kScanThreads - 1) / kScanThreads;
   const int64_t b = (int64_t)threadIdx.x * per, e = b + per < n ? b + per : n;
   uint32_t sum = 0;
   for (int64_t i = b; i < e; ++i) sum += counts[i];
   uint32_t total;
-  uint32_t run = block_prefix(sum, s_warp, &total);
+  uint32_t run = block_prefix<kScanThreads>(sum, s_warp, &total);
   for (int64_t i = b; i < e; ++i) {
     const uint32_t c = counts[i];
     counts[i] = run;
@@ -191,7 +215,7 @@ cudaError_t launch_emissive_count(const uint8_t* grid, int64_t n_voxels, const u
   const int64_t chunks = emissive_chunks(n_voxels);
   if (chunks <= 0) return cudaSuccess;
   k_emissive_count<<<(unsigned)chunks, kEmThreads, 0, st>>>(grid, n_voxels, emissive_entry, counts);
-  k_emissive_offsets<<<1, kEmThreads, 0, st>>>(counts, chunks);
+  k_emissive_offsets<<<1, kScanThreads, 0, st>>>(counts, chunks);
   return cudaGetLastError();
 }
 
