@@ -430,3 +430,34 @@ def test_renderer_material_records(ctx):
     finally:
         close_all(r.job, r.scene)
 
+
+def test_contexts_on_two_threads(ctx):
+    """Two contexts driven from two host threads at once (ctypes releases the
+    GIL during library calls) give the images each gives alone."""
+    import threading
+    cfgs = [small_config1(edge=32, w=40, h=30, seed=51), small_config2(edge=32, w=36, h=28, seed=52)]
+
+    def render(cfg, out, key):
+        c = Context()
+        try:
+            sc, env, job = gpu_setup(c, cfg)
+            try:
+                for _ in range(3):
+                    job.render(2)
+                out[key] = job.readback().view(np.uint32).copy()
+            finally:
+                close_all(job, sc, env)
+        finally:
+            c.close()
+
+    alone, both = {}, {}
+    for i, cfg in enumerate(cfgs):
+        render(cfg, alone, i)
+    threads = [threading.Thread(target=render, args=(cfg, both, i)) for i, cfg in enumerate(cfgs)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for i in range(len(cfgs)):
+        np.testing.assert_array_equal(both[i], alone[i])
+

@@ -666,3 +666,35 @@ def test_batch_of_many_jobs_equals_alone(ctx):
     finally:
         for s, e, j in made:
             close_all(j, s, e)
+
+
+def test_full_size_config2(ctx, orc):
+    """The benchmark's own frame: 256^3 fBm volume, 17 materials, 1024x512
+    sky+sun environment, 1024^2 thin lens.  Per-sample radiance and first
+    hits of two whole samples bit for bit against the oracle, and 8 spp
+    accumulated identically by the wavefront in two lanes of 16M slots with
+    CUDA graphs, in one lane of 1M slots without graphs, and by the plain
+    kernel."""
+    cfg = S.config2()
+    _compare_samples(ctx, orc, cfg, samples=(0, 1))
+    scene, env, job = gpu_setup(ctx, cfg)
+    images = []
+    try:
+        for kernel, lanes, slots, graphs in ((2, 2, 1 << 25, 1), (2, 1, 1 << 20, 0), (1, 2, 0, 1)):
+            ctx.set_kernel(kernel)
+            ctx.set_lanes(lanes)
+            ctx.set_graphs(graphs)
+            if slots:
+                ctx.set_tuning(slots, 0, 16)
+            job.reset()
+            job.render(8)
+            images.append(job.readback().view(np.uint32).copy())
+        for img in images[1:]:
+            np.testing.assert_array_equal(img, images[0])
+    finally:
+        ctx.set_kernel(2)
+        ctx.set_lanes(2)
+        ctx.set_graphs(1)
+        ctx.set_tuning(1 << 23, 0, 16)                 # the context defaults
+        close_all(job, scene, env)
+
