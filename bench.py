@@ -391,7 +391,8 @@ def run_serving(args, world, rank, local):
     ctx = Context(local)
     from voxeltoy_gb300 import _lib as L
     order = L.VT_SERVE_LEAST_WORK if args.order == "least-work" else L.VT_SERVE_ARRIVAL
-    srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4, order=order)
+    srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4, order=order,
+                 quick_paths=args.quick_paths)
     resident = []
     reqs = []
     for k in range(n):
@@ -438,7 +439,7 @@ def run_serving(args, world, rank, local):
             "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s ({n} requests), "
                                    f"sphere-union scenes edge 64-512 (pool of {pool_n}), reuse 0.5, resolution "
                                    f"256^2-1024^2, 16-1024 spp log-uniform, 4 bounces, 60 GB admission budget, "
-                                   f"admission order {args.order}",
+                                   f"admission order {args.order}, quick paths {args.quick_paths}",
                        "requests": n, "offered_mpaths_s": paths / args.duration / 1e6},
             "time_to_spp_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
                                "max": float(lat.max() * 1e3)},
@@ -539,6 +540,8 @@ def main():
     ap.add_argument("--duration", type=float, default=5.0, help="serving: seconds of arrivals")
     ap.add_argument("--order", default="arrival", choices=["arrival", "least-work"],
                     help="serving: admission order of queued requests")
+    ap.add_argument("--quick-paths", type=int, default=1 << 24,
+                    help="serving: requests with at most this many paths left finish in one round (0 = off)")
     ap.add_argument("--check", action="store_true", help="voxelize: compare the occupancy with the oracle")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up and timed renders of the resident frame (for ncu captures)")

@@ -515,6 +515,10 @@ typedef struct vt_server_opts {
                                   VT_SERVE_LEAST_WORK (fewest paths w*h*spp first,
                                   arrival order among equals; under sustained
                                   overload large requests can wait indefinitely) */
+  uint64_t quick_paths;        /* a running request whose remaining paths
+                                  (w*h*(spp - samples)) are at most this many gets
+                                  them all in the next round instead of
+                                  passes_per_round; 0 = off                       */
 } vt_server_opts;
 
 enum { VT_SERVE_ARRIVAL = 0, VT_SERVE_LEAST_WORK = 1 };

@@ -389,6 +389,31 @@ def test_server_results_equal_alone(ctx):
             close_all(m[2], m[0], m[1])
 
 
+def test_server_quick_paths(ctx):
+    """Requests whose remaining work fits quick_paths finish in one round,
+    with the same images as rendered alone."""
+    cfgs = [small_config1(edge=32, w=24, h=20, seed=61), small_config2(edge=32, w=20, h=16, seed=62)]
+    spps = [9, 6]
+    made = [gpu_setup(ctx, c) for c in cfgs]
+    srv = Server(ctx, max_active_jobs=4, passes_per_round=2, quick_paths=1 << 20)
+    try:
+        alone = []
+        for (_s, _e, j), spp in zip(made, spps):
+            j.render(spp)
+            alone.append(j.readback().copy())
+        tickets = [srv.submit(s, e, c.camera, c.settings, c.width, c.height, spp)
+                   for (s, e, _j), c, spp in zip(made, cfgs, spps)]
+        for t, want, c in zip(tickets, alone, cfgs):
+            assert srv.wait(t, 60.0) == L.VT_OK
+            got, _ = srv.result(t, c.width, c.height)
+            np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+        assert srv.stats().rounds <= 2       # one round each at most, against 5 at two passes a round
+    finally:
+        srv.close()
+        for m in made:
+            close_all(m[2], m[0], m[1])
+
+
 def test_server_admission_order(ctx):
     """One slot, a long request holding it, then a large and a small request
     queued behind it: arrival order finishes the large one first, least-work

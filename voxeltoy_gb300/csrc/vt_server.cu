@@ -165,7 +165,10 @@ void vt_server::run() {
     uint64_t paths = 0;
     for (Request* r : round) {
       jobs.push_back(r->job);
-      const int32_t p = std::min(opts.passes_per_round, r->spp - r->samples);
+      const int32_t left = r->spp - r->samples;
+      const uint64_t left_paths = (uint64_t)r->w * r->h * (uint64_t)left;
+      const int32_t p = (opts.quick_paths && left_paths <= opts.quick_paths) ? left
+                                                                             : std::min(opts.passes_per_round, left);
       passes.push_back(p);
       paths += (uint64_t)r->w * r->h * (uint64_t)p;
     }
