@@ -55,7 +55,8 @@ VT_API int vt_diag_set_graphs(vt_context* ctx, int32_t enabled);
 
 /* Wavefront lanes: 2 (the default) runs two independent wavefronts over the
  * two halves of a launch's samples on two streams, so that one's shading
- * overlaps the other's DDA; 1 runs one.  Results are identical. */
+ * overlaps the other's DDA; 1 runs one, 3 and 4 as many.  Results are
+ * identical. */
 VT_API int vt_diag_set_lanes(vt_context* ctx, int32_t lanes);
 
 /* Evaluate a builtin of the renderer on the GPU: fn 0 sin, 1 cos, 2 pow(a, b),

@@ -307,18 +307,22 @@ def test_plain_and_persistent_kernels_agree(ctx):
         close_all(job, scene, env)
 
 
-def test_one_and_two_lanes_agree(ctx):
-    """Two wavefront lanes on two streams give the same bits as one."""
-    cfg = small_config2(edge=40, w=96, h=80, seed=16)     # enough samples for two lanes
+def test_one_to_four_lanes_agree(ctx):
+    """Two, three or four wavefront lanes on their own streams give the same
+    bits as one."""
+    cfg = small_config2(edge=40, w=96, h=80, seed=16)     # enough samples for four lanes
     scene, env, job = gpu_setup(ctx, cfg)
     try:
         out = []
-        for lanes in (1, 2):
+        for lanes in (1, 2, 3, 4):
             ctx.set_lanes(lanes)
             job.reset()
             job.render(3)
             out.append(job.readback().view(np.uint32).copy())
-        np.testing.assert_array_equal(out[0], out[1])
+        for o in out[1:]:
+            np.testing.assert_array_equal(out[0], o)
+        with pytest.raises(L.VtError):
+            ctx.set_lanes(5)
     finally:
         ctx.set_lanes(2)
         close_all(job, scene, env)
@@ -428,9 +432,15 @@ def test_server_admission_order(ctx):
             try:
                 t0 = time.perf_counter()
                 sub = {}
-                for name, res, spp in (("hold", 256, 256), ("large", 96, 64), ("small", 16, 4)):
+                for name, res, spp in (("hold", 384, 256), ("large", 96, 64), ("small", 16, 4)):
                     sub[name] = (srv.submit(scene, None, cfg.camera, cfg.settings, res, res, spp),
                                  time.perf_counter() - t0, res)
+                    if name == "hold":          # queue the others only once it holds the slot
+                        for _ in range(2000):
+                            if srv.poll(sub[name][0])[0] != L.VT_REQ_QUEUED:
+                                break
+                            time.sleep(0.001)
+                        assert srv.poll(sub[name][0])[0] == L.VT_REQ_RUNNING
                 done = {}
                 for name, (t, at, res) in sub.items():
                     assert srv.wait(t, 120.0) == L.VT_OK

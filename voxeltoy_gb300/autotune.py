@@ -4,7 +4,7 @@ Times short renders of the caller's own jobs over a grid of
   path_slots            paths in flight per launch (state + queues per slot)
   trace_blocks_per_sm   resident blocks of the DDA kernel
   trace_steps           DDA steps between ray-pool refills
-  lanes                 wavefronts side by side on two streams (2) or one
+  lanes                 wavefronts side by side on as many streams (1-3)
 and applies the fastest setting to the context.  Path-slot counts above the
 workload's samples collapse to one setting; frames shorter than a few
 milliseconds are timed several times per setting.  Results are cached in a JSON
@@ -25,7 +25,7 @@ DEFAULT_GRID = {
     "path_slots": [1 << 22, 1 << 23, 1 << 24, 1 << 25],
     "trace_blocks_per_sm": [0, 3, 5],
     "trace_steps": [8, 16, 32],
-    "lanes": [2, 1],
+    "lanes": [2, 3, 1],
 }
 
 

@@ -155,8 +155,10 @@ extern "C" int vt_destroy(vt_context* ctx) {
   if (ctx->h_live) cudaFreeHost(ctx->h_live);
   if (ctx->rounds_exec) cudaGraphExecDestroy(ctx->rounds_exec);
   if (ctx->lane_ready) cudaEventDestroy(ctx->lane_ready);
-  if (ctx->lane_done) cudaEventDestroy(ctx->lane_done);
-  if (ctx->lane_stream) cudaStreamDestroy(ctx->lane_stream);
+  for (int l = 0; l < vt_context::kMaxLanes - 1; ++l) {
+    if (ctx->lane_done[l]) cudaEventDestroy(ctx->lane_done[l]);
+    if (ctx->lane_stream[l]) cudaStreamDestroy(ctx->lane_stream[l]);
+  }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VT_OK;
@@ -1243,14 +1245,16 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
     ctx->sbuf_items = items;
   }
   if (!ctx->wf_ctl) {
-    int rc = ctx->alloc((void**)&ctx->wf_ctl, 2 * kCtlBytes);
+    int rc = ctx->alloc((void**)&ctx->wf_ctl, vt_context::kMaxLanes * kCtlBytes);
     if (rc != VT_OK) return rc;
   }
-  if (!ctx->lane_stream) {
-    cudaError_t e = cudaStreamCreateWithFlags(&ctx->lane_stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_ready, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_done, cudaEventDisableTiming);
-    if (e != cudaSuccess) return cuda_fail(e, "lane stream");
+  if (!ctx->lane_ready) {
+    cudaError_t e = cudaEventCreateWithFlags(&ctx->lane_ready, cudaEventDisableTiming);
+    for (int l = 0; l < vt_context::kMaxLanes - 1 && e == cudaSuccess; ++l) {
+      e = cudaStreamCreateWithFlags(&ctx->lane_stream[l], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->lane_done[l], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "lane streams");
   }
   if (!ctx->h_live) {
     cudaError_t e = cudaHostAlloc((void**)&ctx->h_live, 64, cudaHostAllocDefault);
@@ -1296,13 +1300,14 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     }
     T = &table;
   }
-  // Lanes: independent wavefronts over halves of the items, each with half
-  // the path slots and its own stream, so that one lane's memory-bound
-  // shading overlaps the other's ALU-bound DDA.
-  const int lanes = (ctx->lanes == 2 && items >= 8192 && slots >= 2048) ? 2 : 1;
-  const size_t lane_slots = lanes == 2 ? ((size_t)slots / 2) & ~(size_t)31 : (size_t)slots;   // 256-byte lane bases
-  cudaStream_t lane_st[2] = {st, ctx->lane_stream};
-  WfParams P[2];
+  // Lanes: independent wavefronts over equal shares of the items, each with
+  // its share of the path slots and its own stream, so that one lane's
+  // memory-bound shading overlaps another's ALU-bound DDA.
+  int lanes = ctx->lanes;
+  while (lanes > 1 && (items < 4096 * (int64_t)lanes || slots < 1024 * (int64_t)lanes)) --lanes;
+  const size_t lane_slots = lanes > 1 ? ((size_t)slots / lanes) & ~(size_t)31 : (size_t)slots;   // 256-byte lane bases
+  cudaStream_t lane_st[vt_context::kMaxLanes] = {st, ctx->lane_stream[0], ctx->lane_stream[1], ctx->lane_stream[2]};
+  WfParams P[vt_context::kMaxLanes];
   for (int l = 0; l < lanes; ++l) {
     memset(&P[l], 0, sizeof(P[l]));
     P[l].jobs = ctx->d_jobs;
@@ -1317,27 +1322,26 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     P[l].counters = count ? ctx->d_counters : nullptr;
   }
   // control words zero (first stream empty), item counters at each lane's first item
-  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, 2 * kCtlBytes, st), "wavefront control");
-  unsigned long long begins[2] = {0ull, (unsigned long long)(items / lanes)};
-  if (lanes == 2)
-    VT_CUDA(cudaMemcpyAsync(P[1].next_item, &begins[1], sizeof(unsigned long long), cudaMemcpyHostToDevice, st),
+  VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, vt_context::kMaxLanes * kCtlBytes, st), "wavefront control");
+  for (int l = 1; l < lanes; ++l) {
+    const unsigned long long begin = (unsigned long long)(items / lanes * l);
+    VT_CUDA(cudaMemcpyAsync(P[l].next_item, &begin, sizeof(begin), cudaMemcpyHostToDevice, st),
             "lane items");   // pageable source: read when the call returns
+  }
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
   int bps = blocks_per_sm > 0 ? blocks_per_sm
                               : (ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy);
-  if (lanes == 2 && blocks_per_sm <= 0 && ctx->trace_blocks_per_sm <= 0) bps = std::max(1, bps * 2 / 3);
+  if (lanes > 1 && blocks_per_sm <= 0 && ctx->trace_blocks_per_sm <= 0) bps = std::max(1, bps * 2 / 3);
   const int trace_blocks = ctx->sm_count * bps;
   // Eight rounds of every lane: per round and lane its counters cleared,
-  // shade + hit + regen, trace.  The second lane's stream forks from the
-  // first and joins it again, so the group is one unit of work on `st` (one
+  // shade + hit + regen, trace.  The other lanes' streams fork from the
+  // first and join it again, so the group is one unit of work on `st` (one
   // CUDA graph when graphs are on); within it the lanes run free of each
   // other.
   auto group = [&]() -> cudaError_t {
     cudaError_t e = cudaSuccess;
-    if (lanes == 2) {
-      e = cudaEventRecord(ctx->lane_ready, st);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->lane_stream, ctx->lane_ready, 0);
-    }
+    if (lanes > 1) e = cudaEventRecord(ctx->lane_ready, st);
+    for (int l = 1; l < lanes && e == cudaSuccess; ++l) e = cudaStreamWaitEvent(lane_st[l], ctx->lane_ready, 0);
     for (int r = 0; r < 8 && e == cudaSuccess; ++r) {
       const int par = r & 1;
       for (int l = 0; l < lanes && e == cudaSuccess; ++l) {
@@ -1347,9 +1351,9 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
         if (e == cudaSuccess) e = launch_wf_trace(P[l], par, trace_blocks, ctx->trace_steps, count, lane_st[l], T);
       }
     }
-    if (e == cudaSuccess && lanes == 2) {
-      e = cudaEventRecord(ctx->lane_done, ctx->lane_stream);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->lane_done, 0);
+    for (int l = 1; l < lanes && e == cudaSuccess; ++l) {
+      e = cudaEventRecord(ctx->lane_done[l - 1], lane_st[l]);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->lane_done[l - 1], 0);
     }
     return e;
   };
@@ -1753,7 +1757,7 @@ extern "C" int vt_diag_render_counted(vt_job* j, int32_t passes, uint64_t* count
 }
 
 extern "C" int vt_diag_set_lanes(vt_context* ctx, int32_t lanes) {
-  VT_CHECK_ARG(ctx && (lanes == 1 || lanes == 2), "lanes must be 1 or 2");
+  VT_CHECK_ARG(ctx && lanes >= 1 && lanes <= vt_context::kMaxLanes, "lanes must be 1 to 4");
   ctx->lanes = lanes;
   return VT_OK;
 }

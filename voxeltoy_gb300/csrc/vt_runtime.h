@@ -44,9 +44,13 @@ struct vt_context {
   uint64_t launches = 0;         // render kernels launched by this context
   cudaGraphExec_t rounds_exec = nullptr;   // eight rounds of every lane, replayed
   bool use_graphs = true;
-  cudaStream_t lane_stream = nullptr;   // the second lane of a wavefront launch
-  cudaEvent_t lane_ready = nullptr, lane_done = nullptr;
-  int lanes = 2;                 // wavefront lanes run side by side (1 or 2)
+  // the second and later lanes of a wavefront launch: streams, and the
+  // events that fork them from `stream` and join them back
+  static constexpr int kMaxLanes = 4;
+  cudaStream_t lane_stream[kMaxLanes - 1] = {nullptr, nullptr, nullptr};
+  cudaEvent_t lane_ready = nullptr;
+  cudaEvent_t lane_done[kMaxLanes - 1] = {nullptr, nullptr, nullptr};
+  int lanes = 2;                 // wavefront lanes run side by side (1 to kMaxLanes)
   unsigned long long* d_counters = nullptr;
   unsigned long long* d_queue = nullptr;
   int32_t* d_error = nullptr;

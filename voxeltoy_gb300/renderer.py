@@ -87,7 +87,7 @@ class Context:
         L.call("vt_diag_set_kernel", self.h, kernel)
 
     def set_lanes(self, lanes: int):
-        """Wavefront lanes side by side on two streams (2, default) or one."""
+        """Wavefront lanes side by side on their own streams (1-4; 2 is the default)."""
         L.call("vt_diag_set_lanes", self.h, lanes)
 
     def set_graphs(self, enabled: bool):
