@@ -527,7 +527,7 @@ def main():
     ap.add_argument("--kernel", type=int, default=2, help="1 plain per-pass launches, 2 wavefront")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (library defaults)")
     ap.add_argument("--slots", type=int, default=0, help="path slots per launch (skips the autotuner)")
-    ap.add_argument("--lanes", type=int, default=2, choices=[1, 2], help="wavefront lanes with --slots")
+    ap.add_argument("--lanes", type=int, default=2, choices=[1, 2, 3, 4], help="wavefront lanes with --slots")
     ap.add_argument("--trace-steps", type=int, default=0, help="DDA steps between refills (with --slots)")
     ap.add_argument("--trace-bps", type=int, default=-1, help="trace blocks per SM, 0 = occupancy (with --slots)")
     ap.add_argument("--workload", default="config2",
