@@ -407,7 +407,20 @@ def run_serving(args, world, rank, local):
     settings = S.physical_settings(max_bounces=4, rr_start=-1, seed=0)
     scenes = []
     tickets = []
+    large = None
+    if args.alongside:
+        # config 5 served alongside the stream: the voxelized icosphere at
+        # 2048^2 x 1024 spp, 8 bounces, submitted when the stream starts
+        v, f = S.fbm_displaced_icosphere(level=8)
+        big = Scene.voxelize(ctx, np.ascontiguousarray(v, np.float32), np.ascontiguousarray(f, np.uint32),
+                             (1024, 1024, 1024), mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
+                             palette=[S.lambert(0.7)])
+        scenes.append(big)
+        bcfg = S.config1(edge=8, width=2048, height=2048, spp=1024)
+        bcfg.settings.max_bounces = 8
     t_start = time.perf_counter()
+    if args.alongside:
+        large = srv.submit(big, None, bcfg.camera, bcfg.settings, 2048, 2048, 1024)
     for k, (res, spp, reuse, pick, cam) in enumerate(reqs):
         wait = arrivals[k] - (time.perf_counter() - t_start)
         if wait > 0:
@@ -425,6 +438,13 @@ def run_serving(args, world, rank, local):
         if rc != 0:
             raise RuntimeError(f"request {t} failed: {rc}")
         lat.append(delay + srv_latency(srv, t))
+    large_ms = None
+    if large is not None:
+        rc = srv.wait(large, 3600.0)
+        if rc != 0:
+            raise RuntimeError(f"the large request failed: {rc}")
+        large_ms = srv_latency(srv, large) * 1e3
+        tickets.append((large, 0.0, 2048 * 2048 * 1024))
     t_end = time.perf_counter() - t_start
     lat = np.array(lat)
     stats = srv.stats()
@@ -444,6 +464,9 @@ def run_serving(args, world, rank, local):
             "time_to_spp_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
                                "max": float(lat.max() * 1e3)},
             "server": {"completed": int(stats.completed), "failed": int(stats.failed)},
+            "alongside": None if large_ms is None else
+            {"request": "voxelized icosphere (1.3M triangles, 1024^3) at 2048^2 x 1024 spp, 8 bounces, "
+                        "submitted with the first request of the stream", "time_to_spp_ms": large_ms},
             "e2e": {"value": paths / t_end / 1e6, "unit": UNIT,
                     "h2d_bytes_per_step": int(sum(pool[r[3]].nbytes for r in reqs if not r[2])),
                     "d2h_bytes_per_step": 0}}
@@ -540,6 +563,8 @@ def main():
     ap.add_argument("--duration", type=float, default=5.0, help="serving: seconds of arrivals")
     ap.add_argument("--order", default="arrival", choices=["arrival", "least-work"],
                     help="serving: admission order of queued requests")
+    ap.add_argument("--alongside", action="store_true",
+                    help="serving: also serve the voxelized 1.3M-triangle icosphere at 2048^2 x 1024 spp")
     ap.add_argument("--quick-paths", type=int, default=1 << 24,
                     help="serving: requests with at most this many paths left finish in one round (0 = off)")
     ap.add_argument("--check", action="store_true", help="voxelize: compare the occupancy with the oracle")
