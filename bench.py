@@ -392,7 +392,7 @@ def run_serving(args, world, rank, local):
     from voxeltoy_gb300 import _lib as L
     order = L.VT_SERVE_LEAST_WORK if args.order == "least-work" else L.VT_SERVE_ARRIVAL
     srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4, order=order,
-                 quick_paths=args.quick_paths)
+                 quick_paths=args.quick_paths, round_paths_cap=args.round_cap)
     resident = []
     reqs = []
     for k in range(n):
@@ -459,7 +459,8 @@ def run_serving(args, world, rank, local):
             "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s ({n} requests), "
                                    f"sphere-union scenes edge 64-512 (pool of {pool_n}), reuse 0.5, resolution "
                                    f"256^2-1024^2, 16-1024 spp log-uniform, 4 bounces, 60 GB admission budget, "
-                                   f"admission order {args.order}, quick paths {args.quick_paths}",
+                                   f"admission order {args.order}, quick paths {args.quick_paths}, "
+                                   f"round cap {args.round_cap}",
                        "requests": n, "offered_mpaths_s": paths / args.duration / 1e6},
             "time_to_spp_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
                                "max": float(lat.max() * 1e3)},
@@ -563,6 +564,8 @@ def main():
     ap.add_argument("--duration", type=float, default=5.0, help="serving: seconds of arrivals")
     ap.add_argument("--order", default="arrival", choices=["arrival", "least-work"],
                     help="serving: admission order of queued requests")
+    ap.add_argument("--round-cap", type=int, default=0,
+                    help="serving: at most this many paths of one request per round (0 = off)")
     ap.add_argument("--alongside", action="store_true",
                     help="serving: also serve the voxelized 1.3M-triangle icosphere at 2048^2 x 1024 spp")
     ap.add_argument("--quick-paths", type=int, default=1 << 24,

@@ -519,6 +519,9 @@ typedef struct vt_server_opts {
                                   (w*h*(spp - samples)) are at most this many gets
                                   them all in the next round instead of
                                   passes_per_round; 0 = off                       */
+  uint64_t round_paths_cap;    /* at most this many paths of one request per round
+                                  (at least one pass), so that a large request
+                                  does not lengthen every round; 0 = off          */
 } vt_server_opts;
 
 enum { VT_SERVE_ARRIVAL = 0, VT_SERVE_LEAST_WORK = 1 };

@@ -418,6 +418,25 @@ def test_server_quick_paths(ctx):
             close_all(m[2], m[0], m[1])
 
 
+def test_server_round_paths_cap(ctx):
+    """A request larger than the per-round cap advances one pass a round,
+    with the same image as rendered alone."""
+    cfg = small_config2(edge=32, w=32, h=32, seed=63)
+    scene, env, job = gpu_setup(ctx, cfg)
+    srv = Server(ctx, max_active_jobs=2, passes_per_round=4, round_paths_cap=1000)
+    try:
+        job.render(6)
+        want = job.readback().copy()
+        t = srv.submit(scene, env, cfg.camera, cfg.settings, 32, 32, 6)
+        assert srv.wait(t, 60.0) == L.VT_OK
+        got, _ = srv.result(t, 32, 32)
+        np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+        assert srv.stats().rounds == 6       # 1024 pixels > 1000: one pass per round
+    finally:
+        srv.close()
+        close_all(job, scene, env)
+
+
 def test_server_admission_order(ctx):
     """One slot, a long request holding it, then a large and a small request
     queued behind it: arrival order finishes the large one first, least-work

@@ -84,7 +84,8 @@ class BatchOpts(C.Structure):
 
 class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_int32), ("passes_per_round", C.c_int32),
-                ("path_slots", C.c_int32), ("order", C.c_int32), ("quick_paths", C.c_uint64)]
+                ("path_slots", C.c_int32), ("order", C.c_int32), ("quick_paths", C.c_uint64),
+                ("round_paths_cap", C.c_uint64)]
 
 
 class ServerStats(C.Structure):

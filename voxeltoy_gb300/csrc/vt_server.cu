@@ -167,8 +167,11 @@ void vt_server::run() {
       jobs.push_back(r->job);
       const int32_t left = r->spp - r->samples;
       const uint64_t left_paths = (uint64_t)r->w * r->h * (uint64_t)left;
-      const int32_t p = (opts.quick_paths && left_paths <= opts.quick_paths) ? left
-                                                                             : std::min(opts.passes_per_round, left);
+      int32_t p = (opts.quick_paths && left_paths <= opts.quick_paths) ? left : std::min(opts.passes_per_round, left);
+      if (opts.round_paths_cap) {
+        const uint64_t px = (uint64_t)r->w * r->h;
+        p = (int32_t)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)p, opts.round_paths_cap / px));
+      }
       passes.push_back(p);
       paths += (uint64_t)r->w * r->h * (uint64_t)p;
     }

@@ -364,8 +364,9 @@ class Job:
 class Server:
     def __init__(self, ctx: Context, hbm_budget_bytes: int = 0, max_active_jobs: int = 64,
                  passes_per_round: int = 4, path_slots: int = 0, order: int = L.VT_SERVE_ARRIVAL,
-                 quick_paths: int = 0):
-        opts = L.ServerOpts(hbm_budget_bytes, max_active_jobs, passes_per_round, path_slots, order, quick_paths)
+                 quick_paths: int = 0, round_paths_cap: int = 0):
+        opts = L.ServerOpts(hbm_budget_bytes, max_active_jobs, passes_per_round, path_slots, order, quick_paths,
+                            round_paths_cap)
         h = C.c_void_p()
         L.call("vt_server_create", ctx.h, C.byref(opts), C.byref(h))
         self.h = h
