@@ -461,3 +461,24 @@ def test_contexts_on_two_threads(ctx):
     for i in range(len(cfgs)):
         np.testing.assert_array_equal(both[i], alone[i])
 
+
+def test_server_teardown_returns_device_memory(ctx):
+    """A server's own launch lane (wavefront buffers, sample buffer, graphs,
+    lane streams) is freed with the server: create, serve and destroy three
+    times and the device's free memory comes back."""
+    import torch
+    cfg = small_config1(edge=32, w=64, h=64, seed=71)
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        for _ in range(3):
+            srv = Server(ctx, max_active_jobs=2, passes_per_round=4, path_slots=1 << 20)
+            t = srv.submit(scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height, 8)
+            assert srv.wait(t, 60.0) == L.VT_OK
+            srv.close()
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] >= free0 - (64 << 20)
+    finally:
+        close_all(job, scene, env)
+

@@ -138,8 +138,9 @@ extern "C" int vt_create(const vt_device_opts* opts, vt_context** out) {
   return VT_OK;
 }
 
-extern "C" int vt_destroy(vt_context* ctx) {
-  if (!ctx) return VT_OK;
+// Every device buffer, host staging word, graph, event and stream a context
+// owns (the context object itself stays).
+void vt::release_context(vt_context* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->release(ctx->noise);
@@ -160,6 +161,19 @@ extern "C" int vt_destroy(vt_context* ctx) {
     if (ctx->lane_stream[l]) cudaStreamDestroy(ctx->lane_stream[l]);
   }
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  ctx->h_live = nullptr;
+  ctx->rounds_exec = nullptr;
+  ctx->lane_ready = nullptr;
+  for (int l = 0; l < vt_context::kMaxLanes - 1; ++l) {
+    ctx->lane_done[l] = nullptr;
+    ctx->lane_stream[l] = nullptr;
+  }
+  ctx->stream = nullptr;
+}
+
+extern "C" int vt_destroy(vt_context* ctx) {
+  if (!ctx) return VT_OK;
+  release_context(ctx);
   delete ctx;
   return VT_OK;
 }

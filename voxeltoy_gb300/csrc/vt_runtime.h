@@ -116,6 +116,8 @@ namespace vt {
 int fail(int code, const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);
 int build_frame(vt_job* j);
+// Frees everything a context owns (vt_destroy, and the server's own lane).
+void release_context(vt_context* ctx);
 // Rebuilds a job's frame when its scene was edited since (scene->generation).
 int refresh_job(vt_job* j);
 // passes[i] samples per pixel for jobs[i]; kernel 1 = plain, 2 = wavefront.

@@ -337,16 +337,7 @@ extern "C" int vt_server_destroy(vt_server* s) {
     if (kv.second->job) vt_job_destroy(kv.second->job);
     delete kv.second;
   }
-  vt_context& L = s->lane;
-  cudaSetDevice(L.device);
-  if (L.stream) cudaStreamSynchronize(L.stream);
-  L.release(L.noise);
-  L.release(L.scratch);
-  L.release(L.d_counters);
-  L.release(L.d_queue);
-  L.release(L.d_error);
-  L.release(L.d_jobs);
-  if (L.stream) cudaStreamDestroy(L.stream);
+  release_context(&s->lane);   // wavefront buffers, graphs and lane streams included
   delete s;
   return VT_OK;
 }
