@@ -669,7 +669,8 @@ vt_env::~vt_env() {
   ctx->release(cdf_v);
 }
 
-static size_t env_scratch_bytes(int32_t w, int32_t h, size_t* offs) {
+// Scratch layout of an environment build: nine offsets into one buffer.
+static size_t env_scratch_bytes(int32_t w, int32_t h, size_t (&offs)[9]) {
   const size_t n = (size_t)w * h;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += (bytes + 255) & ~(size_t)255; return at; };
@@ -681,6 +682,7 @@ static size_t env_scratch_bytes(int32_t w, int32_t h, size_t* offs) {
   offs[5] = take(sizeof(double) * h);                // row integrals
   offs[6] = take(sizeof(double) * (h + 1));          // marginal prefixes
   offs[7] = take(sizeof(float) * 3 * n);             // rgb input
+  offs[8] = take(2 * sizeof(uint32_t));              // integral, first non-finite texel
   return o;
 }
 
@@ -701,8 +703,6 @@ extern "C" int vt_env_create_image(vt_context* ctx, const float* rgb, int32_t w,
   VT_CHECK_ARG(ctx && rgb && out, "null argument");
   VT_CHECK_ARG(w > 0 && h > 0 && (int64_t)w * h < ((int64_t)1 << 28), "bad image size");
   *out = nullptr;
-  for (int64_t i = 0; i < (int64_t)w * h * 3; ++i)
-    if (!std::isfinite(rgb[i])) return fail(VT_EINVAL, "environment texel %lld is not finite", (long long)(i / 3));
   vt_env* env = new vt_env();
   env->ctx = ctx;
   env->w = w;
@@ -711,33 +711,34 @@ extern "C" int vt_env_create_image(vt_context* ctx, const float* rgb, int32_t w,
   int rc = ctx->alloc((void**)&env->texels, sizeof(uint2) * n);
   if (rc == VT_OK) rc = ctx->alloc((void**)&env->cdf_u, sizeof(float) * (size_t)(w + 1) * h);
   if (rc == VT_OK) rc = ctx->alloc((void**)&env->cdf_v, sizeof(float) * (size_t)(h + 1));
-  size_t offs[8];
+  size_t offs[9];
   const size_t sb = env_scratch_bytes(w, h, offs);
-  void* scratch = nullptr;
-  if (rc == VT_OK) rc = ctx->alloc(&scratch, sb);
+  if (rc == VT_OK) rc = ctx->ensure_scratch(sb);   // kept by the context for the next build
   if (rc != VT_OK) { delete env; return rc; }
+  void* scratch = ctx->scratch;
   EnvScratch S = env_scratch(scratch, offs);
   // row weights sin(pi (y + 0.5) / h) as calculateImageIntegral computes them (image.cpp:366)
   std::vector<float> sin_theta(h);
   for (int y = 0; y < h; ++y) sin_theta[y] = (float)std::sin(M_PI * (double)((float)y + 0.5f) / (double)(float)h);
   float* d_rgb = (float*)((char*)scratch + offs[7]);
-  float* d_int = (float*)S.row_int;  // reuse: integral written after the marginal
-  float integral = 0.0f;
+  uint32_t* d_out = (uint32_t*)((char*)scratch + offs[8]);   // integral bits, first non-finite texel
+  uint32_t res[2] = {0u, 0u};   // pageable: the read has completed when the copy returns
   cudaError_t e = cudaMemcpyAsync(d_rgb, rgb, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(S.sin_theta, sin_theta.data(), sizeof(float) * h, cudaMemcpyHostToDevice, ctx->stream);
-  float* d_integral = nullptr;
-  if (e == cudaSuccess) {
-    rc = ctx->alloc((void**)&d_integral, sizeof(float));
-    if (rc != VT_OK) { ctx->release(scratch); delete env; return rc; }
-  }
-  (void)d_int;
-  if (e == cudaSuccess) e = launch_env_build(d_rgb, w, h, S, env->texels, env->cdf_u, env->cdf_v, d_integral, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&integral, d_integral, sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_out + 1, 0xff, sizeof(uint32_t), ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_env_build(d_rgb, w, h, S, env->texels, env->cdf_u, env->cdf_v, (float*)d_out, d_out + 1,
+                         ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(res, d_out, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  ctx->release(d_integral);
-  ctx->release(scratch);
   if (e != cudaSuccess) { delete env; return cuda_fail(e, "environment build"); }
+  if (res[1] != 0xffffffffu) {
+    delete env;
+    return fail(VT_EINVAL, "environment texel %lld is not finite", (long long)res[1]);
+  }
+  float integral;
+  memcpy(&integral, &res[0], sizeof(integral));
   env->integral = integral;
   *out = env;
   return VT_OK;
@@ -1810,7 +1811,7 @@ extern "C" int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int
                                          float* cdf_v, float* integral) {
   VT_CHECK_ARG(ctx && func && cdf_u && cdf_v && w > 0 && h > 0, "bad argument");
   cudaSetDevice(ctx->device);
-  size_t offs[8];
+  size_t offs[9];
   const size_t sb = env_scratch_bytes(w, h, offs);
   const size_t extra = ((sizeof(float) * (size_t)(w + 1) * h + 255) & ~(size_t)255) +
                        ((sizeof(float) * (size_t)(h + 2) + 255) & ~(size_t)255) + 256;

@@ -146,8 +146,9 @@ struct EnvScratch {
   double* row_int;   // h row integrals
   double* marg_pre;  // h+1 marginal prefix sums
 };
+// bad: set to the smallest index of a non-finite texel (the caller sets it to ~0 first)
 cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, const EnvScratch& S, uint2* texels,
-                             float* cdf_u, float* cdf_v, float* integral, cudaStream_t st);
+                             float* cdf_u, float* cdf_v, float* integral, uint32_t* bad, cudaStream_t st);
 // CDFs of a caller-supplied function (w*h floats) without blur or weighting.
 cudaError_t launch_cdf(const float* func, int32_t w, int32_t h, const EnvScratch& S, float* cdf_u,
                        float* cdf_v, float* integral, cudaStream_t st);

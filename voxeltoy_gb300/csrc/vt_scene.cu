@@ -235,10 +235,12 @@ cudaError_t launch_emissive_write(const uint8_t* grid, int64_t n_voxels, const u
 
 // FP16 texels (A = 1) and the luminance of the quantised RGB
 // (generateImageFunction's channel_sum, src/renderer/image.cpp:326-335).
+// `bad` receives the smallest index of a texel with a non-finite channel.
 __global__ void k_env_texels(const float* __restrict__ rgb, int64_t n, uint2* __restrict__ texels,
-                             float* __restrict__ lum) {
+                             float* __restrict__ lum, uint32_t* bad) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  if (!(isfinite(rgb[3 * i]) && isfinite(rgb[3 * i + 1]) && isfinite(rgb[3 * i + 2]))) atomicMin(bad, (uint32_t)i);
   const uint16_t r = vtb::f2h(vtb::clamp_half(rgb[3 * i])), g = vtb::f2h(vtb::clamp_half(rgb[3 * i + 1])),
                  b = vtb::f2h(vtb::clamp_half(rgb[3 * i + 2]));
   texels[i] = make_uint2((uint32_t)r | ((uint32_t)g << 16), (uint32_t)b | (0x3c00u << 16));
@@ -347,10 +349,10 @@ cudaError_t launch_cdf(const float* func, int32_t w, int32_t h, const EnvScratch
 }
 
 cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, const EnvScratch& S, uint2* texels,
-                             float* cdf_u, float* cdf_v, float* integral, cudaStream_t st) {
+                             float* cdf_u, float* cdf_v, float* integral, uint32_t* bad, cudaStream_t st) {
   const int64_t n = (int64_t)w * h;
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  k_env_texels<<<blocks, 256, 0, st>>>(rgb, n, texels, S.lum);
+  k_env_texels<<<blocks, 256, 0, st>>>(rgb, n, texels, S.lum, bad);
   k_env_blur<<<blocks, 256, 0, st>>>(S.lum, S.tmp, w, h, 0, S.sin_theta);
   k_env_blur<<<blocks, 256, 0, st>>>(S.tmp, S.func, w, h, 1, S.sin_theta);
   cudaError_t e = cudaGetLastError();
