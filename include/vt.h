@@ -148,8 +148,16 @@ VT_API int vt_scene_create_from_offsets(vt_context* ctx, int32_t rx, int32_t ry,
                                         int64_t n_emissive, uint32_t flags,
                                         vt_scene** out);
 
-/* Voxelizer coverage rule (src/shaders/shared/voxelize.gs:14-19). */
-enum { VT_VOXELIZE_THIN = 0, VT_VOXELIZE_FAT = 1 };
+/* Voxelizer coverage rule (src/shaders/shared/voxelize.gs:14-19), optionally
+ * OR'd with VT_VOXELIZE_REFERENCE_BOUNDS.  Each triangle is scanned in its
+ * swizzled frame (dominant normal axis as Z); its voxel range there is
+ * clamped to the grid's extent along the same swizzled axes, so FAT marks
+ * exactly the voxels a separating-axis overlap test marks on any grid.  The
+ * reference clamps the swizzled range against the unswizzled resolution
+ * (voxelize.gs:247-248, cpuVoxelizer.cpp:265-270), which is the same on
+ * cubic grids and drops voxels on others; VT_VOXELIZE_REFERENCE_BOUNDS
+ * reproduces that. */
+enum { VT_VOXELIZE_THIN = 0, VT_VOXELIZE_FAT = 1, VT_VOXELIZE_REFERENCE_BOUNDS = 0x100 };
 enum { VT_MESH_VOXEL_SPACE = 0, VT_MESH_FIT_UNIT_CUBE = 1 };
 
 /* Voxelize a triangle mesh on the GPU into a new scene whose occupied voxels

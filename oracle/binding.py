@@ -70,7 +70,7 @@ def lib() -> C.CDLL:
             "orc_binary_search": ([P, C.c_int32, C.c_float], C.c_int32),
             "orc_voxelize": ([P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
                               C.c_int32, P], C.c_int),
-            "orc_voxelize_sat": ([P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, P], C.c_int),
+            "orc_voxelize_sat": ([P, C.c_int64, P, C.c_int64, C.c_int32, C.c_int32, C.c_int32, C.c_double, P], C.c_int),
             "orc_prune_emissive": ([P, P, P, C.c_int64], C.c_int64),
             "orc_noise_table": ([P], C.c_int),
             "orc_philox": ([P, P, P], None),
@@ -233,12 +233,12 @@ def voxelize(vertices, indices, res, mode: int, placement: int = 0, threads: int
     return g
 
 
-def voxelize_sat(vertices_voxel_space, indices, res) -> np.ndarray:
+def voxelize_sat(vertices_voxel_space, indices, res, half: float = 0.5) -> np.ndarray:
     v = np.ascontiguousarray(vertices_voxel_space, dtype=np.float32)
     i = np.ascontiguousarray(indices, dtype=np.uint32)
     rx, ry, rz = res
     g = np.empty((rz, ry, rx), np.uint8)
-    lib().orc_voxelize_sat(_p(v), v.size // 3, _p(i), i.size // 3, rx, ry, rz, _p(g))
+    lib().orc_voxelize_sat(_p(v), v.size // 3, _p(i), i.size // 3, rx, ry, rz, half, _p(g))
     return g
 
 

@@ -1027,9 +1027,13 @@ int sat_int(float f) {
 }
 
 // voxelizeTriPostSwizzle after swizzleTri (cpuVoxelizer.cpp:42-235,
-// voxelize.gs:55-251), THIN (mode 0) or FAT (mode 1).
-void voxelize_triangle(const float* vv0, const float* vv1, const float* vv2, const int* res, int mode,
-                       uint8_t* grid) {
+// voxelize.gs:55-251), THIN (mode 0) or FAT (mode 1).  The swizzled bounding
+// box is clamped to the grid's extent along the swizzled axes, or with
+// ref_bounds to the unswizzled resolution as voxelize.gs:247-248 and
+// cpuVoxelizer.cpp:265-270 do.
+void voxelize_triangle(const float* vv0, const float* vv1, const float* vv2, const int* res_xyz, int mode,
+                       bool ref_bounds, uint8_t* grid) {
+  const int* res = res_xyz;
   float v0[3] = {vv0[0], vv0[1], vv0[2]}, v1[3] = {vv1[0], vv1[1], vv1[2]}, v2[3] = {vv2[0], vv2[1], vv2[2]};
   // n = cross(v1 - v0, v2 - v1)
   const float a[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
@@ -1042,12 +1046,21 @@ void voxelize_triangle(const float* vv0, const float* vv1, const float* vv2, con
   else if (ay >= ax && ay >= az) { perm = 1; swz(v0, 2, 0, 1); swz(v1, 2, 0, 1); swz(v2, 2, 0, 1); swz(n, 2, 0, 1); }
   else perm = 2;
   const float* V[3] = {v0, v1, v2};
+  int ext[3] = {res[0], res[1], res[2]};
+  if (!ref_bounds && perm == 0) { ext[0] = res[1]; ext[1] = res[2]; ext[2] = res[0]; }
+  if (!ref_bounds && perm == 1) { ext[0] = res[2]; ext[1] = res[0]; ext[2] = res[1]; }
+  // A FAT scan also takes the voxels that only touch the box at an integer
+  // bound (ceil(min) - 1 and floor(max) + 1); the reference's floor/ceil
+  // range skips them, so a triangle lying in an integer plane marks nothing.
+  const bool touch = !ref_bounds && mode == 1;
   int lo[3], hi[3];
   for (int c = 0; c < 3; ++c) {
     const float mn = glmin(glmin(v0[c], v1[c]), v2[c]);
     const float mx = glmax(glmax(v0[c], v1[c]), v2[c]);
-    lo[c] = std::min(std::max(sat_int(std::floor(mn)), 0), res[c]);
-    hi[c] = std::min(std::max(sat_int(std::ceil(mx)), 0), res[c]);
+    const int l = touch ? sat_int(std::ceil(mn)) - 1 : sat_int(std::floor(mn));
+    const int u = touch ? sat_int(std::floor(mx)) + 1 : sat_int(std::ceil(mx));
+    lo[c] = std::min(std::max(l, 0), ext[c]);
+    hi[c] = std::min(std::max(u, 0), ext[c]);
   }
   float e[3][3];
   for (int c = 0; c < 3; ++c) { e[0][c] = v1[c] - v0[c]; e[1][c] = v2[c] - v1[c]; e[2][c] = v0[c] - v2[c]; }
@@ -1109,10 +1122,9 @@ void voxelize_triangle(const float* vv0, const float* vv1, const float* vv2, con
 
 // Separating-axis triangle/box overlap (Akenine-Moller, "Fast 3D
 // Triangle-Box Overlap Testing", JGT 2001) for a unit box, in double.
-bool tri_box_overlap(const double* c, const double* t0, const double* t1, const double* t2) {
+bool tri_box_overlap(const double* c, double h, const double* t0, const double* t1, const double* t2) {
   double v[3][3];
   for (int k = 0; k < 3; ++k) { v[0][k] = t0[k] - c[k]; v[1][k] = t1[k] - c[k]; v[2][k] = t2[k] - c[k]; }
-  const double h = 0.5;
   for (int ax = 0; ax < 3; ++ax) {   // box face normals
     const double mn = std::min(v[0][ax], std::min(v[1][ax], v[2][ax]));
     const double mx = std::max(v[0][ax], std::max(v[1][ax], v[2][ax]));
@@ -1327,7 +1339,7 @@ int orc_voxelize(const float* vertices, int64_t nv, const uint32_t* indices, int
         if (b >= nt) break;
         for (int64_t k = b; k < std::min(nt, b + 4096); ++k)
           voxelize_triangle(&vs[3 * (size_t)indices[3 * k]], &vs[3 * (size_t)indices[3 * k + 1]],
-                            &vs[3 * (size_t)indices[3 * k + 2]], res, mode, grid);
+                            &vs[3 * (size_t)indices[3 * k + 2]], res, mode & 1, (mode & 0x100) != 0, grid);
       }
     });
   for (auto& th : pool) th.join();
@@ -1335,7 +1347,7 @@ int orc_voxelize(const float* vertices, int64_t nv, const uint32_t* indices, int
 }
 
 int orc_voxelize_sat(const float* v, int64_t nv, const uint32_t* idx, int64_t nt, int32_t rx, int32_t ry, int32_t rz,
-                     uint8_t* grid) {
+                     double half, uint8_t* grid) {
   (void)nv;
   std::memset(grid, 0, (size_t)rx * ry * rz);
   for (int64_t t = 0; t < nt; ++t) {
@@ -1354,7 +1366,7 @@ int orc_voxelize_sat(const float* v, int64_t nv, const uint32_t* idx, int64_t nt
       for (int y = lo[1]; y < hi[1]; ++y)
         for (int x = lo[0]; x < hi[0]; ++x) {
           const double c[3] = {x + 0.5, y + 0.5, z + 0.5};
-          if (tri_box_overlap(c, p[0], p[1], p[2])) grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * z)] = 1;
+          if (tri_box_overlap(c, half, p[0], p[1], p[2])) grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * z)] = 1;
         }
   }
   return 0;

@@ -133,15 +133,18 @@ int orc_cdf_reference_float(const float* func, int32_t w, int32_t h, float* cdf_
 /* binarySearchCDFV (envMapSample.h:70-94) over cdf[0..n). */
 int32_t orc_binary_search(const float* cdf, int32_t n, float u);
 
-/* Voxelizer (cpuVoxelizer.cpp / voxelize.gs), mode 0 THIN, 1 FAT; placement 1
+/* Voxelizer (cpuVoxelizer.cpp / voxelize.gs), mode 0 THIN, 1 FAT, OR'd with
+ * 0x100 to clamp each triangle's swizzled voxel range against the unswizzled
+ * resolution as the reference does (voxelize.gs:247-248); placement 1
  * applies computeMeshTransform; grid receives 1 for covered voxels. */
 int orc_voxelize(const float* vertices, int64_t nv, const uint32_t* indices, int64_t nt,
                  int32_t rx, int32_t ry, int32_t rz, int32_t mode, int32_t placement,
                  int32_t threads, uint8_t* grid);
-/* Independent check: conservative triangle/box overlap by the separating
- * axis theorem (Akenine-Moller 2001) in double precision. */
+/* Independent check: triangle/box overlap by the separating axis theorem
+ * (Akenine-Moller 2001) in double precision, for the box of half-size `half`
+ * around each voxel centre (0.5 = the voxel; contact counts as overlap). */
 int orc_voxelize_sat(const float* vertices_voxel_space, int64_t nv, const uint32_t* indices,
-                     int64_t nt, int32_t rx, int32_t ry, int32_t rz, uint8_t* grid);
+                     int64_t nt, int32_t rx, int32_t ry, int32_t rz, double half, uint8_t* grid);
 
 /* pruneInteriorEmissiveVoxels (import.cpp:180-203) in place; returns new n. */
 int64_t orc_prune_emissive(const uint8_t* grid, const int32_t* res, int32_t* list, int64_t n);

@@ -491,7 +491,9 @@ def _tri_soup(seed, n_small=3000, n_large=40, res=(96, 80, 64)):
     return v, np.arange(len(v), dtype=np.uint32)
 
 
-@pytest.mark.parametrize("mode", [L.VT_VOXELIZE_THIN, L.VT_VOXELIZE_FAT])
+@pytest.mark.parametrize("mode", [L.VT_VOXELIZE_THIN, L.VT_VOXELIZE_FAT,
+                                  L.VT_VOXELIZE_THIN | L.VT_VOXELIZE_REFERENCE_BOUNDS,
+                                  L.VT_VOXELIZE_FAT | L.VT_VOXELIZE_REFERENCE_BOUNDS])
 def test_voxelize_bitexact_triangle_soup(ctx, orc, mode):
     res = (96, 80, 64)
     v, idx = _tri_soup(3)

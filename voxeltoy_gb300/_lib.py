@@ -19,7 +19,7 @@ VT_OK, VT_EINVAL, VT_ENOMEM, VT_EBUDGET, VT_EDEVICE, VT_ETIMEOUT, VT_ECANCELLED,
 VT_SAMPLES_PENDING, VT_FINISHED_RENDERING = 0, 1
 VT_MATERIAL_LAMBERT, VT_MATERIAL_METAL, VT_MATERIAL_PLASTIC = 0, 1, 2
 VT_SCENE_PRUNE_EMISSIVE, VT_SCENE_AUTO_EMISSIVE = 1, 2
-VT_VOXELIZE_THIN, VT_VOXELIZE_FAT = 0, 1
+VT_VOXELIZE_THIN, VT_VOXELIZE_FAT, VT_VOXELIZE_REFERENCE_BOUNDS = 0, 1, 0x100
 VT_MESH_VOXEL_SPACE, VT_MESH_FIT_UNIT_CUBE = 0, 1
 VT_LENS_PINHOLE, VT_LENS_THIN_LENS, VT_LENS_ORTHOGRAPHIC = 0, 1, 2
 VT_SERVE_ARRIVAL, VT_SERVE_LEAST_WORK = 0, 1

@@ -514,7 +514,9 @@ extern "C" int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices, in
   VT_CHECK_ARG(ctx && out, "null argument");
   VT_CHECK_ARG(n_triangles == 0 || (vertices && indices), "vertices/indices is null");
   VT_CHECK_ARG(n_vertices >= 0 && n_triangles >= 0, "negative counts");
-  VT_CHECK_ARG(mode == VT_VOXELIZE_THIN || mode == VT_VOXELIZE_FAT, "unknown voxelization mode");
+  VT_CHECK_ARG((mode & ~VT_VOXELIZE_REFERENCE_BOUNDS) == VT_VOXELIZE_THIN ||
+                   (mode & ~VT_VOXELIZE_REFERENCE_BOUNDS) == VT_VOXELIZE_FAT,
+               "unknown voxelization mode");
   VT_CHECK_ARG(palette && n_palette >= 1 && n_palette <= 255, "palette needs 1..255 entries");
   for (int64_t i = 0; i < 3 * n_triangles; ++i)
     if ((int64_t)indices[i] >= n_vertices) return fail(VT_EINVAL, "triangle index %u out of range", indices[i]);
@@ -538,7 +540,8 @@ extern "C" int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices, in
     e = cudaMemcpyAsync(d_v, vsrc, sizeof(float) * 3 * n_vertices, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && n_triangles)
     e = cudaMemcpyAsync(d_i, indices, sizeof(uint32_t) * 3 * n_triangles, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = launch_voxelize(d_v, d_i, n_triangles, rx, ry, rz, mode, s->grid, 1, ctx->stream);
+  if (e == cudaSuccess) e = launch_voxelize(d_v, d_i, n_triangles, rx, ry, rz, mode & 1,
+                                                (mode & VT_VOXELIZE_REFERENCE_BOUNDS) != 0, s->grid, 1, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   ctx->release(d_v);
   ctx->release(d_i);

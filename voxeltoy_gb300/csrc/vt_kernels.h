@@ -152,9 +152,11 @@ cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, const EnvSc
 // CDFs of a caller-supplied function (w*h floats) without blur or weighting.
 cudaError_t launch_cdf(const float* func, int32_t w, int32_t h, const EnvScratch& S, float* cdf_u,
                        float* cdf_v, float* integral, cudaStream_t st);
+// mode 0 = THIN, 1 = FAT; reference_bounds clamps each triangle's swizzled
+// voxel range against the unswizzled resolution as the reference does.
 cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indices, int64_t n_tris,
-                            int32_t rx, int32_t ry, int32_t rz, int32_t mode, uint8_t* grid,
-                            uint8_t value, cudaStream_t st);
+                            int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
+                            uint8_t* grid, uint8_t value, cudaStream_t st);
 cudaError_t launch_transform_vertices(const float* in, int64_t n, const float* m44_row_major,
                                       int32_t rx, int32_t ry, int32_t rz, float* out, cudaStream_t st);
 

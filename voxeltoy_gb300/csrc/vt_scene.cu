@@ -366,7 +366,13 @@ cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, const EnvSc
 // and src/voxelize/cpuVoxelizer.cpp:42-235: project on the dominant axis,
 // test the XY edge functions per column, derive the Z range from the plane,
 // test the YZ and ZX edge functions per voxel.  mode 0 = THIN (6-separating,
-// figure 18), 1 = FAT (conservative, figure 17).
+// figure 18), 1 = FAT (conservative, figure 17).  The scan range of a
+// triangle is its bounding box in the swizzled frame, clamped to the grid's
+// extent along the swizzled axes; with ref_bounds, against the unswizzled
+// resolution as voxelize.gs:247-248 does (the same on cubic grids; on others
+// voxels near the far faces of the shorter axes are lost).  FAT without
+// ref_bounds marks exactly the voxels that a separating-axis test marks,
+// up to float rounding where a voxel only touches the triangle.
 struct TriSetup {
   float d_xy[3], d_yz[3], d_zx[3];
   float n_xy[3][2], n_yz[3][2], n_zx[3][2];
@@ -398,7 +404,7 @@ __device__ __forceinline__ float edge_d(const float* nrm, float pa, float pb, in
 }
 
 __device__ bool tri_setup(const float* V, const uint32_t* I, int64_t t, int32_t rx, int32_t ry, int32_t rz,
-                          int mode, TriSetup& S) {
+                          int mode, bool ref_bounds, TriSetup& S) {
   float v[3][3];
   for (int k = 0; k < 3; ++k) {
     const uint32_t vi = I[3 * t + k];
@@ -423,13 +429,22 @@ __device__ bool tri_setup(const float* V, const uint32_t* I, int64_t t, int32_t 
     n[0] = m0; n[1] = m1; n[2] = m2;
   }
   S.perm = perm;
-  const int res[3] = {rx, ry, rz};
+  // grid extent along the swizzled axes: yzx -> (ry, rz, rx), zxy -> (rz, rx, ry)
+  int res[3] = {rx, ry, rz};
+  if (!ref_bounds && perm == 0) { res[0] = ry; res[1] = rz; res[2] = rx; }
+  if (!ref_bounds && perm == 1) { res[0] = rz; res[1] = rx; res[2] = ry; }
+  // ivec3(clamp(floor(min), 0, res)), ivec3(clamp(ceil(max), 0, res))
+  // (voxelize.gs:247-248); a FAT scan also takes the voxels that only touch
+  // the triangle at an integer bound, ceil(min) - 1 and floor(max) + 1, which
+  // that range skips (a triangle lying in an integer plane would mark nothing).
+  const bool touch = !ref_bounds && mode == 1;
   for (int c = 0; c < 3; ++c) {
     const float mn = vtb::gmin(vtb::gmin(v[0][c], v[1][c]), v[2][c]);
     const float mx = vtb::gmax(vtb::gmax(v[0][c], v[1][c]), v[2][c]);
-    // ivec3(clamp(floor(min), 0, res)) with the unswizzled resolution (voxelize.gs:247-248)
-    S.lo[c] = min(max(sat_int(floorf(mn)), 0), res[c]);
-    S.hi[c] = min(max(sat_int(ceilf(mx)), 0), res[c]);
+    const int l = touch ? sat_int(ceilf(mn)) - 1 : sat_int(floorf(mn));
+    const int u = touch ? sat_int(floorf(mx)) + 1 : sat_int(ceilf(mx));
+    S.lo[c] = min(max(l, 0), res[c]);
+    S.hi[c] = min(max(u, 0), res[c]);
   }
   float e[3][3];
   for (int c = 0; c < 3; ++c) {
@@ -501,12 +516,12 @@ constexpr int kLargeColumns = 64;
 // One thread per triangle for triangles whose XY footprint is small; larger
 // ones are appended to a list for the block-per-triangle kernel.
 __global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restrict__ I, int64_t n_tris,
-                            int32_t rx, int32_t ry, int32_t rz, int mode, uint8_t* grid, uint8_t value,
-                            int64_t* large, unsigned long long* n_large) {
+                            int32_t rx, int32_t ry, int32_t rz, int mode, bool ref_bounds, uint8_t* grid,
+                            uint8_t value, int64_t* large, unsigned long long* n_large) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tris) return;
   TriSetup S;
-  if (!tri_setup(V, I, t, rx, ry, rz, mode, S)) return;
+  if (!tri_setup(V, I, t, rx, ry, rz, mode, ref_bounds, S)) return;
   const int64_t cols = (int64_t)(S.hi[0] - S.lo[0]) * (int64_t)(S.hi[1] - S.lo[1]);
   if (cols > kLargeColumns) {
     const unsigned long long slot = atomicAdd(n_large, 1ull);
@@ -519,12 +534,12 @@ __global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restr
 
 __global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restrict__ I, const int64_t* large,
                             const unsigned long long* n_large, int32_t rx, int32_t ry, int32_t rz, int mode,
-                            uint8_t* grid, uint8_t value) {
+                            bool ref_bounds, uint8_t* grid, uint8_t value) {
   __shared__ TriSetup S;
   const unsigned long long n = *n_large;
   for (unsigned long long k = blockIdx.x; k < n; k += gridDim.x) {
     __syncthreads();
-    if (threadIdx.x == 0) tri_setup(V, I, large[k], rx, ry, rz, mode, S);
+    if (threadIdx.x == 0) tri_setup(V, I, large[k], rx, ry, rz, mode, ref_bounds, S);
     __syncthreads();
     const int wx = S.hi[0] - S.lo[0], wy = S.hi[1] - S.lo[1];
     const int64_t cols = (int64_t)wx * wy;
@@ -536,8 +551,8 @@ __global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restr
 }
 
 cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indices, int64_t n_tris,
-                            int32_t rx, int32_t ry, int32_t rz, int32_t mode, uint8_t* grid,
-                            uint8_t value, cudaStream_t st) {
+                            int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
+                            uint8_t* grid, uint8_t value, cudaStream_t st) {
   if (n_tris <= 0) return cudaSuccess;
   int64_t* large = nullptr;
   unsigned long long* n_large = nullptr;
@@ -547,8 +562,10 @@ cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indi
   if (e != cudaSuccess) { cudaFreeAsync(large, st); return e; }
   cudaMemsetAsync(n_large, 0, sizeof(unsigned long long), st);
   k_vox_small<<<(unsigned)((n_tris + 127) / 128), 128, 0, st>>>(verts_voxel_space, indices, n_tris, rx, ry, rz,
-                                                                mode, grid, value, large, n_large);
-  k_vox_large<<<152 * 4, 256, 0, st>>>(verts_voxel_space, indices, large, n_large, rx, ry, rz, mode, grid, value);
+                                                                mode, reference_bounds, grid, value, large,
+                                                                n_large);
+  k_vox_large<<<152 * 4, 256, 0, st>>>(verts_voxel_space, indices, large, n_large, rx, ry, rz, mode,
+                                       reference_bounds, grid, value);
   e = cudaGetLastError();
   cudaFreeAsync(large, st);
   cudaFreeAsync(n_large, st);

@@ -166,6 +166,10 @@ class Scene:
     @classmethod
     def voxelize(cls, ctx: Context, vertices: np.ndarray, indices: np.ndarray, resolution, mode: int = 1,
                  placement: int = L.VT_MESH_FIT_UNIT_CUBE, palette=None) -> "Scene":
+        """Triangle mesh voxelized on the GPU (GPUVoxelizer::voxelizeMesh).  mode is
+        VT_VOXELIZE_THIN or VT_VOXELIZE_FAT, optionally | VT_VOXELIZE_REFERENCE_BOUNDS
+        for the reference's clamp of the swizzled scan range (drops voxels on
+        non-cubic grids)."""
         v = np.ascontiguousarray(vertices, dtype=np.float32)
         i = np.ascontiguousarray(indices, dtype=np.uint32)
         pal = palette or [(0, (0, 0, 0), (0.7, 0.7, 0.7), 0.0)]
