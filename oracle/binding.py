@@ -75,6 +75,10 @@ def lib() -> C.CDLL:
             "orc_noise_table": ([P], C.c_int),
             "orc_philox": ([P, P, P], None),
             "orc_builtins": ([C.c_int32, P, P, P, C.c_int64], C.c_int),
+            "orc_bsdf_sample": ([C.c_int32, P, C.c_float, C.c_uint32, P, P, C.c_int64, P], C.c_int),
+            "orc_bsdf_eval": ([C.c_int32, P, C.c_float, C.c_uint32, P, P, C.c_int64, P], C.c_int),
+            "orc_env_sample": ([C.POINTER(OrcEnv), C.c_float, P, C.c_int64, P], C.c_int),
+            "orc_env_eval": ([C.POINTER(OrcEnv), C.c_float, P, C.c_int64, P], C.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -257,6 +261,43 @@ def philox(ctr, key):
     out = np.empty(4, np.uint32)
     lib().orc_philox(_p(c), _p(k), _p(out))
     return out
+
+
+def bsdf_sample(material, wo, u, quirks: int = 0):
+    """material = (type, albedo[3], roughness); wo (n, 3) local, u (n, 2) ->
+    wi (n, 3), f (n, 3), pdf (n,)."""
+    t, a, r = material
+    alb = np.ascontiguousarray(a, dtype=np.float32)
+    w = np.ascontiguousarray(wo, dtype=np.float32)
+    uu = np.ascontiguousarray(u, dtype=np.float32)
+    out = np.empty((w.shape[0], 8), np.float32)
+    assert lib().orc_bsdf_sample(int(t), _p(alb), float(r), quirks, _p(w), _p(uu), w.shape[0], _p(out)) == 0
+    return out[:, :3], out[:, 3:6], out[:, 6]
+
+
+def bsdf_eval(material, wo, wi, quirks: int = 0):
+    t, a, r = material
+    alb = np.ascontiguousarray(a, dtype=np.float32)
+    w = np.ascontiguousarray(wo, dtype=np.float32)
+    v = np.ascontiguousarray(wi, dtype=np.float32)
+    out = np.empty((w.shape[0], 4), np.float32)
+    assert lib().orc_bsdf_eval(int(t), _p(alb), float(r), quirks, _p(w), _p(v), w.shape[0], _p(out)) == 0
+    return out[:, :3], out[:, 3]
+
+
+def env_sample(env: Env, u, rotation: float = 0.0):
+    """u (n, 2) -> dir (n, 3), radiance (n, 3), pdf (n,)."""
+    uu = np.ascontiguousarray(u, dtype=np.float32)
+    out = np.empty((uu.shape[0], 8), np.float32)
+    assert lib().orc_env_sample(C.byref(env.e), rotation, _p(uu), uu.shape[0], _p(out)) == 0
+    return out[:, :3], out[:, 3:6], out[:, 6]
+
+
+def env_eval(env: Env, dirs, rotation: float = 0.0):
+    d = np.ascontiguousarray(dirs, dtype=np.float32)
+    out = np.empty((d.shape[0], 4), np.float32)
+    assert lib().orc_env_eval(C.byref(env.e), rotation, _p(d), d.shape[0], _p(out)) == 0
+    return out[:, :3], out[:, 3]
 
 
 def builtins(fn: int, a, b=None) -> np.ndarray:

@@ -1249,7 +1249,7 @@ int orc_build_env(const float* rgb, int32_t w, int32_t h, int32_t chunk, uint16_
     lum[i] = (vtb::h2f(r) * 0.2126f + vtb::h2f(g) * 0.7152f) + vtb::h2f(b) * 0.0722f;
   }
   // 3x3 Gaussian, sigma 0.75, clamp to edge (image.cpp:337-342)
-  const float ws = 0.225604179501533508f, wm = 0.548791640996932983f;
+  const float ws = 0.225610111284051620f, wm = 0.548779777431896800f;
   for (int y = 0; y < h; ++y)
     for (int x = 0; x < w; ++x) {
       const int xm = x > 0 ? x - 1 : 0, xp = x < w - 1 ? x + 1 : w - 1;
@@ -1398,6 +1398,94 @@ int orc_noise_table(float* out) {
 }
 
 void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox4x32(ctr, key, out); }
+
+namespace {
+Tracer<float> unit_tracer(const orc_settings* s, const orc_env* env, float rotation) {
+  Tracer<float> T;
+  T.S = s; T.env = env; T.scene = nullptr; T.noise = nullptr;
+  T.bg_rot = rotation;
+  T.bg_top = v3<float>(0.0f, 0.0f, 0.0f); T.bg_bottom = T.bg_top;
+  return T;
+}
+Mat unit_material(int32_t type, const float* albedo, float rough) {
+  Mat m;
+  m.type = type;
+  for (int k = 0; k < 3; ++k) { m.e[k] = 0.0f; m.a[k] = q16(albedo[k]); }
+  m.rough = q16(rough);
+  return m;
+}
+}  // namespace
+
+int orc_bsdf_sample(int32_t type, const float* albedo, float rough, uint32_t quirks, const float* wo,
+                    const float* u, int64_t n, float* out) {
+  orc_settings s;
+  std::memset(&s, 0, sizeof(s));
+  s.quirks = quirks;
+  const Tracer<float> T = unit_tracer(&s, nullptr, 0.0f);
+  const Mat m = unit_material(type, albedo, rough);
+  for (int64_t i = 0; i < n; ++i) {
+    // the noise-table stream reads its block from u: one rand() call
+    const float block[4] = {u[2 * i], u[2 * i + 1], 0.0f, 0.0f};
+    Rng rng;
+    rng.mode = 1; rng.noise = block; rng.ox = 0; rng.oy = 0;
+    Tracer<float>::FP fp;
+    float u_rr;
+    const V3<float> w = T.sample_bsdf(m, v3<float>(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]), rng, fp, u_rr);
+    float* o = out + 8 * i;
+    o[0] = w.x; o[1] = w.y; o[2] = w.z; o[3] = fp.f.x; o[4] = fp.f.y; o[5] = fp.f.z; o[6] = fp.pdf; o[7] = 0.0f;
+  }
+  return 0;
+}
+
+int orc_bsdf_eval(int32_t type, const float* albedo, float rough, uint32_t quirks, const float* wo,
+                  const float* wi, int64_t n, float* out) {
+  orc_settings s;
+  std::memset(&s, 0, sizeof(s));
+  s.quirks = quirks;
+  const Tracer<float> T = unit_tracer(&s, nullptr, 0.0f);
+  const Mat m = unit_material(type, albedo, rough);
+  for (int64_t i = 0; i < n; ++i) {
+    const Tracer<float>::FP fp = T.eval_bsdf(m, v3<float>(wo[3 * i], wo[3 * i + 1], wo[3 * i + 2]),
+                                             v3<float>(wi[3 * i], wi[3 * i + 1], wi[3 * i + 2]));
+    float* o = out + 4 * i;
+    o[0] = fp.f.x; o[1] = fp.f.y; o[2] = fp.f.z; o[3] = fp.pdf;
+  }
+  return 0;
+}
+
+int orc_env_sample(const orc_env* env, float rotation, const float* u, int64_t n, float* out) {
+  if (!env || !env->texels) return -1;
+  orc_settings s;
+  std::memset(&s, 0, sizeof(s));
+  const Tracer<float> T = unit_tracer(&s, env, rotation);
+  Tracer<float>::Basis b;
+  b.position = v3<float>(0.0f, 0.0f, 0.0f); b.normal = v3<float>(0.0f, 1.0f, 0.0f);
+  b.tangent = v3<float>(1.0f, 0.0f, 0.0f); b.binormal = v3<float>(0.0f, 0.0f, 1.0f);
+  Counters C;
+  for (int64_t i = 0; i < n; ++i) {
+    V3<float> d;
+    float pdf;
+    const V3<float> L = T.sample_env(b, u[2 * i], u[2 * i + 1], &d, &pdf, C);
+    float* o = out + 8 * i;
+    o[0] = d.x; o[1] = d.y; o[2] = d.z; o[3] = L.x; o[4] = L.y; o[5] = L.z; o[6] = pdf; o[7] = 0.0f;
+  }
+  return 0;
+}
+
+int orc_env_eval(const orc_env* env, float rotation, const float* dirs, int64_t n, float* out) {
+  if (!env || !env->texels) return -1;
+  orc_settings s;
+  std::memset(&s, 0, sizeof(s));
+  const Tracer<float> T = unit_tracer(&s, env, rotation);
+  Counters C;
+  for (int64_t i = 0; i < n; ++i) {
+    float pdf = 0.0f;
+    const V3<float> L = T.eval_env(v3<float>(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2]), &pdf, C);
+    float* o = out + 4 * i;
+    o[0] = L.x; o[1] = L.y; o[2] = L.z; o[3] = pdf;
+  }
+  return 0;
+}
 
 int orc_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n) {
   for (int64_t i = 0; i < n; ++i) {

@@ -153,6 +153,19 @@ int64_t orc_prune_emissive(const uint8_t* grid, const int32_t* res, int32_t* lis
 int orc_noise_table(float* out);
 /* Philox-4x32-10 block for known-answer tests. */
 void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* BSDF of one material record (materials.h:7-43; type 0 Lambert, 1 metal,
+ * 2 plastic), with the palette's FP16 rounding: sample n directions from
+ * local wo (n*3, +Y = normal) and uniforms u (n*2) -> out n*8 {wi[3], f[3],
+ * pdf, 0}; evaluate at (wo, wi) -> out n*4 {f[3], pdf}. */
+int orc_bsdf_sample(int32_t type, const float* albedo, float roughness, uint32_t quirks,
+                    const float* wo, const float* u, int64_t n, float* out);
+int orc_bsdf_eval(int32_t type, const float* albedo, float roughness, uint32_t quirks,
+                  const float* wo, const float* wi, int64_t n, float* out);
+/* Environment light (lights.h:20-55, envMapSample.h:23-123): sample from
+ * uniforms u (n*2) -> out n*8 {dir[3], L[3], pdf, 0}; evaluate along dirs
+ * (n*3) -> out n*4 {L[3], pdf}.  The environment must hold an image. */
+int orc_env_sample(const orc_env* env, float rotation, const float* u, int64_t n, float* out);
+int orc_env_eval(const orc_env* env, float rotation, const float* dirs, int64_t n, float* out);
 /* Builtins of the float build for accuracy tests (fn as vt_diag_builtins). */
 int orc_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n);
 

@@ -230,8 +230,8 @@ cudaError_t launch_emissive_write(const uint8_t* grid, int64_t n_voxels, const u
 // ------------------------------------------------------------ environment
 // Three-tap Gaussian (sigma = 0.75 px) normalised to sum 1:
 //   w_side = e / (1 + 2e), w_mid = 1 / (1 + 2e), e = exp(-1 / (2 * 0.75^2)).
-#define VT_BLUR_SIDE 0.225604179501533508f
-#define VT_BLUR_MID 0.548791640996932983f
+#define VT_BLUR_SIDE 0.225610111284051620f
+#define VT_BLUR_MID 0.548779777431896800f
 
 // FP16 texels (A = 1) and the luminance of the quantised RGB
 // (generateImageFunction's channel_sum, src/renderer/image.cpp:326-335).
