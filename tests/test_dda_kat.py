@@ -11,9 +11,12 @@ or after int(2 ceil(|res|)) steps (:98).  Checked here against:
     on the hit flag, the voxel and the step count except where the float
     traversal meets a near-tie (an origin within 1e-5 voxel of a voxel
     face, or two axis crossings within 1e-5 voxel of each other);
-  * hand-computed answers: axis-aligned rays, exact diagonals through voxel
-    corners (all three axes step at once), grazing components, origins in
-    an occupied voxel and outside the grid.
+  * hand-computed answers, on the oracle and on the CUDA traversal:
+    axis-aligned rays, exact diagonals through voxel corners (all three
+    axes step at once), grazing components, origins in an occupied voxel
+    and outside the grid.
+The GPU tests also compare the CUDA traversal with the double-precision
+one directly.
 """
 import numpy as np
 import pytest
@@ -71,7 +74,7 @@ def traverse_exact(vox, o, d):
         gap[idx] = np.minimum(gap[idx], tm[:, 1] - tm[:, 0])
         mask = tmax[idx] == tm[:, :1]
         p[idx] += mask * step[idx]
-        tmax[idx] += mask * tdel[idx]
+        tmax[idx] += np.where(mask, tdel[idx], 0.0)
         steps[idx] += 1
     return hit, p, steps, gap
 
@@ -107,68 +110,110 @@ def test_random_rays_match_exact_traversal(orc, res):
     assert (gap[~same] < 1e-5).all()
 
 
-def one_ray(orc, vox, o, d):
-    hit, p, steps = decode(orc.trace_rays(orc.Scene(vox, PAL), np.array([o], np.float32), np.array([d], np.float32)))
-    return bool(hit[0]), tuple(int(c) for c in p[0]), int(steps[0])
-
-
 def voxel_point(res, ijk, frac=(0.5, 0.5, 0.5)):
     bmin, vs = world_bounds(res)
     return bmin + (np.array(ijk, float) + np.array(frac)) * vs
 
 
-def test_axis_aligned_rays(orc):
+def unit(v):
+    v = np.array(v, float)
+    return v / np.linalg.norm(v)
+
+
+def kat_cases():
+    """(name, grid shape (x, y, z), occupied voxels, origin, direction,
+    expected (hit, voxel, steps)), every answer worked out by hand."""
+    cases = []
     res = (32, 32, 32)
-    vox = np.zeros(res[::-1], np.uint8)
-    vox[9, 7, 20] = 1          # (x, y, z) = (20, 7, 9)
-    vox[9, 7, 2] = 1
-    vox[25, 7, 3] = 1
+    occ = [(20, 7, 9), (2, 7, 9), (3, 7, 25)]
     o = voxel_point(res, (10, 7, 9))
-    assert one_ray(orc, vox, o, (1, 0, 0)) == (True, (20, 7, 9), 10)
-    assert one_ray(orc, vox, o, (-1, 0, 0)) == (True, (2, 7, 9), 8)
-    # nothing along +y: leaves the grid after 32 - 7 steps
-    assert one_ray(orc, vox, o, (0, 1, 0)) == (False, (10, 32, 9), 25)
-    assert one_ray(orc, vox, voxel_point(res, (3, 7, 0)), (0, 0, 1)) == (True, (3, 7, 25), 25)
-
-
-def test_exact_diagonal_steps_all_axes_together(orc):
-    """A ray along (1,1,1) through voxel corners crosses the three boundaries
-    at once and moves diagonally, so the face neighbours it passes at a
-    corner are never visited."""
-    res = (32, 32, 32)
-    vox = np.zeros(res[::-1], np.uint8)
-    for k in range(1, 9):
-        vox[k - 1, k - 1, k] = 1     # (k, k-1, k-1): the +x neighbour of each diagonal voxel
-        vox[k - 1, k, k - 1] = 1     # (k-1, k, k-1)
-    vox[9, 9, 9] = 1
-    d = np.full(3, 1.0 / np.sqrt(3.0))
-    assert one_ray(orc, vox, voxel_point(res, (0, 0, 0), (0.25, 0.25, 0.25)), d) == (True, (9, 9, 9), 9)
-    hit, p, steps, gap = traverse_exact(vox, voxel_point(res, (0, 0, 0), (0.25, 0.25, 0.25))[None],
-                                        d[None].astype(np.float32))
-    assert hit[0] and tuple(p[0]) == (9, 9, 9) and steps[0] == 9 and gap[0] == 0.0
-
-
-def test_grazing_component_is_replaced_by_plus_1e_5(orc):
-    """|d.y| <= 1e-5 becomes +1e-5 whatever its sign: from 5e-5 voxel below
-    the top face of row 12, such a ray climbs into row 13 within a few voxels
-    and hits the voxel there; a ray with d.y = -2e-5 keeps heading down and
-    stays in row 12."""
-    res = (32, 32, 32)
-    vox = np.zeros(res[::-1], np.uint8)
-    vox[4, 12, 30] = 1         # (30, 12, 4)
-    vox[4, 13, 20] = 1         # (20, 13, 4)
+    cases += [("axis +x", res, occ, o, (1, 0, 0), (True, (20, 7, 9), 10)),
+              ("axis -x", res, occ, o, (-1, 0, 0), (True, (2, 7, 9), 8)),
+              # nothing along +y: leaves the grid after 32 - 7 steps
+              ("axis +y", res, occ, o, (0, 1, 0), (False, (10, 32, 9), 25)),
+              ("axis +z", res, occ, voxel_point(res, (3, 7, 0)), (0, 0, 1), (True, (3, 7, 25), 25))]
+    # A ray along (1,1,1) through voxel corners crosses the three boundaries
+    # at once and moves diagonally, so the face neighbours it passes at each
+    # corner are never visited.
+    occ = [(k, k - 1, k - 1) for k in range(1, 9)] + [(k - 1, k, k - 1) for k in range(1, 9)] + [(9, 9, 9)]
+    cases.append(("diagonal", res, occ, voxel_point(res, (0, 0, 0), (0.25, 0.25, 0.25)), unit((1, 1, 1)),
+                  (True, (9, 9, 9), 9)))
+    # |d.y| <= 1e-5 becomes +1e-5 whatever its sign: from 5e-5 voxel below
+    # the top face of row 12 such a ray climbs into row 13 within a few
+    # voxels and hits the voxel there; d.y = -2e-5 keeps heading down.
+    occ = [(30, 12, 4), (20, 13, 4)]
     o = voxel_point(res, (0, 12, 4), (0.5, 0.99995, 0.5))
-    for dy, want in ((-5e-6, (True, (20, 13, 4), 21)), (0.0, (True, (20, 13, 4), 21)),
-                     (5e-6, (True, (20, 13, 4), 21)), (-2e-5, (True, (30, 12, 4), 30))):
-        d = np.array([1.0, dy, 0.0])
-        assert one_ray(orc, vox, o, d / np.linalg.norm(d)) == want, dy
-
-
-def test_origin_in_an_occupied_voxel_and_outside(orc):
+    for dy in (-5e-6, 0.0, 5e-6):
+        cases.append((f"grazing {dy:g}", res, occ, o, unit((1.0, dy, 0.0)), (True, (20, 13, 4), 21)))
+    cases.append(("not grazing", res, occ, o, unit((1.0, -2e-5, 0.0)), (True, (30, 12, 4), 30)))
     res = (16, 16, 16)
+    cases.append(("inside occupied", res, [(7, 6, 5)], voxel_point(res, (7, 6, 5)), (0.0, 0.6, 0.8),
+                  (True, (7, 6, 5), 0)))
+    return cases
+
+
+def case_grid(res, occ):
     vox = np.zeros(res[::-1], np.uint8)
-    vox[5, 6, 7] = 1
-    assert one_ray(orc, vox, voxel_point(res, (7, 6, 5)), (0.0, 0.6, 0.8)) == (True, (7, 6, 5), 0)
-    # outside the volume: no traversal at all
-    hit, _, steps = one_ray(orc, vox, voxel_point(res, (-3, 6, 5)), (1.0, 0.0, 0.0))
-    assert not hit and steps == 0
+    for x, y, z in occ:
+        vox[z, y, x] = 1
+    return vox
+
+
+@pytest.mark.parametrize("case", kat_cases(), ids=lambda c: c[0])
+def test_hand_computed_rays(orc, case):
+    _, res, occ, o, d, want = case
+    vox = case_grid(res, occ)
+    hit, p, steps = decode(orc.trace_rays(orc.Scene(vox, PAL), np.array([o], np.float32),
+                                          np.array([d], np.float32)))
+    assert (bool(hit[0]), tuple(int(c) for c in p[0]), int(steps[0])) == want
+    # the exact traversal agrees
+    ehit, ep, esteps, _ = traverse_exact(vox, np.array([o], np.float32), np.array([d], np.float32))
+    if case[0] != "not grazing" and not case[0].startswith("grazing"):
+        assert (bool(ehit[0]), tuple(int(c) for c in ep[0]), int(esteps[0])) == want
+
+
+def test_origin_outside_the_grid(orc):
+    res = (16, 16, 16)
+    vox = case_grid(res, [(7, 6, 5)])
+    hit, _, steps = decode(orc.trace_rays(orc.Scene(vox, PAL), np.array([voxel_point(res, (-3, 6, 5))], np.float32),
+                                          np.array([(1.0, 0.0, 0.0)], np.float32)))
+    assert not hit[0] and steps[0] == 0
+
+
+def _gpu_trace(ctx, vox, o, d):
+    from voxeltoy_gb300 import Job, Scene
+    from voxeltoy_gb300 import scenes as S
+    sc = Scene.dense(ctx, vox, [S.lambert(0.5)])
+    job = None
+    try:
+        job = Job(ctx, sc, None, S.orbit_camera(), S.physical_settings(max_bounces=1), 8, 8)
+        return decode(job.trace_rays(o, d))
+    finally:
+        if job is not None:
+            job.close()
+        sc.close()
+
+
+@pytest.mark.gpu
+def test_hand_computed_rays_gpu(ctx):
+    """The same answers from the CUDA traversal, through the C ABI."""
+    for name, res, occ, o, d, want in kat_cases():
+        hit, p, steps = _gpu_trace(ctx, case_grid(res, occ), np.array([o], np.float32), np.array([d], np.float32))
+        assert (bool(hit[0]), tuple(int(c) for c in p[0]), int(steps[0])) == want, name
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("res", [(64, 64, 64), (48, 32, 40)])
+def test_random_rays_match_exact_traversal_gpu(ctx, res):
+    rng = np.random.default_rng(sum(res))
+    vox = scene(res, 1)
+    bmin, vs = world_bounds(res)
+    d = rng.normal(size=(200000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d[(np.abs(d) > 1e-4).all(1)].astype(np.float32)
+    o = (bmin + rng.random(d.shape) * np.array(res) * vs).astype(np.float32)
+    hit, p, steps, gap = traverse_exact(vox, o, d)
+    ghit, gp, gsteps = _gpu_trace(ctx, vox, o, d)
+    same = (ghit == hit) & (gsteps == steps) & (~hit | (gp == p).all(1))
+    assert (~same).sum() <= 5
+    assert (gap[~same] < 1e-5).all()

@@ -129,3 +129,22 @@ def test_reference_bounds_equal_on_cubic_grids(orc):
         v = v + np.float32(0.37)     # off the integers, where only the FAT range differs
         for mode in (THIN, FAT):
             np.testing.assert_array_equal(orc.voxelize(v, i, res, mode), orc.voxelize(v, i, res, mode | REF))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("res", [(40, 40, 40), (48, 40, 32)])
+def test_gpu_fat_matches_separating_axis(ctx, orc, res):
+    """The CUDA voxelizer through the C ABI against the separating-axis test
+    directly, including triangles in an integer plane."""
+    from voxeltoy_gb300 import Scene
+    v, i = soup(res, 5)
+    plane = np.array([[4, 4, 10], [24, 4, 10], [4, 20, 10]], np.float32)
+    v = np.concatenate([v, plane])
+    i = np.arange(len(v), dtype=np.uint32)
+    sc = Scene.voxelize(ctx, v, i, res, mode=FAT, placement=L.VT_MESH_VOXEL_SPACE)
+    try:
+        fat = sc.voxels().astype(bool)
+    finally:
+        sc.close()
+    sat = check_between(orc, fat, v, i, res)
+    assert (fat != sat).sum() <= 2
