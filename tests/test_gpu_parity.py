@@ -289,6 +289,35 @@ def test_accumulation_matches_oracle_average(ctx, orc):
         close_all(job, scene, env)
 
 
+def test_kahan_accumulation_over_10k_samples(ctx):
+    """10,000 samples of a frame with a sun and emissive voxels accumulate in
+    FP32 with Kahan compensation to the float64 mean of the same per-sample
+    radiance within 3 ulp, where a plain FP32 running sum drifts far more."""
+    cfg = small_config2(edge=24, w=8, h=8)
+    cfg.settings.max_samples = 1 << 20
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        n = 10000
+        job.render(n)
+        got = job.readback()[..., :3].astype(np.float64)
+        exact = np.zeros((8, 8, 3))
+        plain = np.zeros((8, 8, 3), np.float32)
+        for k in range(n):
+            rgb = job.samples_diag(k)[0][..., :3]
+            exact += rgb
+            plain += rgb
+        exact /= n
+        plain = plain.astype(np.float64) / n
+        lit = exact > 1e-3
+        err = np.abs(got - exact)[lit] / exact[lit]
+        err_plain = np.abs(plain - exact)[lit] / exact[lit]
+        assert lit.sum() > 100
+        assert err.max() < 3 * 2.0 ** -23
+        assert err_plain.max() > 10 * err.max()
+    finally:
+        close_all(job, scene, env)
+
+
 def test_plain_and_persistent_kernels_agree(ctx):
     cfg = small_config2(edge=40, w=50, h=30)
     scene, env, job = gpu_setup(ctx, cfg)
