@@ -596,16 +596,37 @@ def test_pick_matches_oracle(ctx, orc):
         close_all(job, scene, env)
 
 
-def test_converged_image_rmse_vs_fp64(ctx, orc):
-    cfg = small_config1(edge=64, w=64, h=64)
+RMSE_CONFIGS = {
+    "config1": lambda: small_config1(edge=64, w=64, h=64),
+    "config2": lambda: small_config2(edge=48, w=48, h=40),
+    "reference": lambda: reference_config(edge=40, w=40, h=32),
+}
+
+
+@pytest.mark.parametrize("name", list(RMSE_CONFIGS))
+def test_converged_image_rmse_vs_fp64(ctx, orc, name):
+    """Relative RMSE of the GPU's FP32 image against the oracle's FP64 build
+    at equal sample counts, per configuration (printed for the record)."""
+    cfg = RMSE_CONFIGS[name]()
+    cfg.settings.max_samples = 1 << 20
+    spp = 48
     scene, env, job = gpu_setup(ctx, cfg)
     try:
-        job.render(48)
+        job.render(spp)
         got = job.readback()[..., :3].astype(np.float64)
         osc, oenv = oracle_setup(orc, cfg, scene, env)
-        ref, _ = orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, 48, 64)
+        noise = ctx.noise_table() if cfg.settings.rng_mode == L.VT_RNG_NOISE_TABLE else None
+        ref, _ = orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, spp, 64,
+                                    noise=noise)
         ref = ref[..., :3].astype(np.float64)
-        rel_rmse = np.sqrt(np.mean((got - ref) ** 2)) / np.sqrt(np.mean(ref ** 2))
+        # with the reference's unguarded divisions a pixel that met a zero pdf
+        # stays NaN (in either precision); the error is taken over the rest
+        ok = np.isfinite(got).all(-1) & np.isfinite(ref).all(-1)
+        rel_rmse = np.sqrt(np.mean((got[ok] - ref[ok]) ** 2)) / np.sqrt(np.mean(ref[ok] ** 2))
+        print(f"relative RMSE vs FP64 oracle, {name}, {cfg.width}x{cfg.height} x {spp} spp: {rel_rmse:.3e} "
+              f"({(~ok).sum()} non-finite pixels: {(~np.isfinite(got).all(-1)).sum()} FP32, "
+              f"{(~np.isfinite(ref).all(-1)).sum()} FP64)")
+        assert ok.mean() >= 0.95 if name == "reference" else ok.all()
         assert rel_rmse <= 1e-3, rel_rmse
     finally:
         close_all(job, scene, env)
