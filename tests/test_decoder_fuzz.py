@@ -5,6 +5,7 @@ consistent arrays or fail with a status code and a message, never crash or
 write past the caller's buffers.  The mutation loop runs in a child process
 so that a crash shows up as its exit status; the caller's output buffers
 carry guard bytes that are checked after every call."""
+import ast
 import os
 import subprocess
 import sys
@@ -121,5 +122,5 @@ def test_decoders_survive_malformed_input(tmp_path):
     script.write_text(f"ROOT = {ROOT!r}\nHERE = {HERE!r}\n" + CHILD)
     r = subprocess.run([sys.executable, str(script), "7", "3000"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
-    counts = eval(r.stdout.strip().splitlines()[-1])
+    counts = ast.literal_eval(r.stdout.strip().splitlines()[-1])
     assert counts["err"] > 2500 and counts["ok"] > 500
