@@ -79,6 +79,7 @@ def lib() -> C.CDLL:
             "orc_bsdf_eval": ([C.c_int32, P, C.c_float, C.c_uint32, P, P, C.c_int64, P], C.c_int),
             "orc_env_sample": ([C.POINTER(OrcEnv), C.c_float, P, C.c_int64, P], C.c_int),
             "orc_env_eval": ([C.POINTER(OrcEnv), C.c_float, P, C.c_int64, P], C.c_int),
+            "orc_noise_walk": ([P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P], C.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -298,6 +299,13 @@ def env_eval(env: Env, dirs, rotation: float = 0.0):
     out = np.empty((d.shape[0], 4), np.float32)
     assert lib().orc_env_eval(C.byref(env.e), rotation, _p(d), d.shape[0], _p(out)) == 0
     return out[:, :3], out[:, 3]
+
+
+def noise_walk(noise: np.ndarray, px: int, py: int, sample: int, n: int) -> np.ndarray:
+    t = np.ascontiguousarray(noise, dtype=np.float32)
+    out = np.empty((n, 4), np.float32)
+    assert lib().orc_noise_walk(_p(t), px, py, sample, n, _p(out)) == 0
+    return out
 
 
 def builtins(fn: int, a, b=None) -> np.ndarray:

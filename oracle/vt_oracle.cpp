@@ -1487,6 +1487,13 @@ int orc_env_eval(const orc_env* env, float rotation, const float* dirs, int64_t 
   return 0;
 }
 
+int orc_noise_walk(const float* noise, int32_t px, int32_t py, int32_t sample, int32_t n, float* out) {
+  Rng rng;
+  rng.init(1, 0u, noise, 1, px, py, sample);
+  for (int32_t i = 0; i < n; ++i) rng.next(out + 4 * (size_t)i);
+  return 0;
+}
+
 int orc_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n) {
   for (int64_t i = 0; i < n; ++i) {
     const float x = a[i];

@@ -166,6 +166,9 @@ int orc_bsdf_eval(int32_t type, const float* albedo, float roughness, uint32_t q
  * (n*3) -> out n*4 {L[3], pdf}.  The environment must hold an image. */
 int orc_env_sample(const orc_env* env, float rotation, const float* u, int64_t n, float* out);
 int orc_env_eval(const orc_env* env, float rotation, const float* dirs, int64_t n, float* out);
+/* The first n draws (n*4 floats) of the noise-table stream of pixel (px, py)
+ * and sample (randomNumberGeneratorOffset + rand, random.h:13-27). */
+int orc_noise_walk(const float* noise, int32_t px, int32_t py, int32_t sample, int32_t n, float* out);
 /* Builtins of the float build for accuracy tests (fn as vt_diag_builtins). */
 int orc_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n);
 

@@ -146,3 +146,66 @@ def test_edit_mode_known_answers(orc):
     assert np.all(v[:, 0] == v[:, 1]) and np.all(v[:, 1] == v[:, 2])   # white voxels
     assert np.all((v > 0.5) & (v <= 1.0))        # sqrt(cos) of a view from above, never halved by a shadow
 
+
+
+def _wang_hash(seed):
+    """Thomas Wang's 32-bit integer hash as random.h:3-11 writes it, in signed
+    32-bit arithmetic (arithmetic right shifts, wrapping products)."""
+    s = np.asarray(seed, np.int64).astype(np.int32)
+    with np.errstate(over="ignore"):
+        s = (s ^ np.int32(61)) ^ (s >> 16)
+        s = (s.astype(np.int64) * 9).astype(np.uint32).astype(np.int32)
+        s = s ^ (s >> 4)
+        s = (s.astype(np.int64) * 0x27D4EB2D).astype(np.uint32).astype(np.int32)
+        s = s ^ (s >> 15)
+    return s
+
+
+def test_noise_table_walk_against_restatement(orc):
+    """randomNumberGeneratorOffset (random.h:13-18): offset = hash(x + 1024 y)
+    ^ hash(sample), read as unsigned, split into (offset % 1024, offset / 1024
+    % 1024); rand (:20-27) returns that texel and advances x, wrapping into
+    the next row and from the last row to the first."""
+    table = orc.noise_table()
+    rng = np.random.default_rng(4)
+    cases = [(int(x), int(y), int(s)) for x, y, s in zip(rng.integers(0, 4096, 40), rng.integers(0, 4096, 40),
+                                                      rng.integers(0, 1 << 20, 40))]
+    # a stream that starts at the end of a row: find one by search
+    for s in range(200000):
+        off = int((_wang_hash(0) ^ _wang_hash(s)).astype(np.uint32))
+        if off % 1024 >= 1022:
+            cases.append((0, 0, s))
+            break
+    wrapped = False
+    for x, y, s in cases:
+        off = int((_wang_hash(x + 1024 * y) ^ _wang_hash(s)).astype(np.uint32))
+        ox, oy = off % 1024, (off // 1024) % 1024
+        want = []
+        for _ in range(4):
+            want.append(table[oy, ox])
+            ox = (ox + 1) % 1024
+            if ox == 0:
+                oy = (oy + 1) % 1024
+                wrapped = True
+        np.testing.assert_array_equal(orc.noise_walk(table, x, y, s, 4), np.array(want))
+    assert wrapped
+
+
+def test_wang_hash_restatement_is_the_published_function():
+    """The restatement above against the hash written with plain Python
+    integers modulo 2^32 (logical shifts of the two's-complement pattern
+    differ from arithmetic ones only in the high bits that the sign fills)."""
+    def ref(seed):
+        m = 0xFFFFFFFF
+        def sar(v, k):   # arithmetic shift of a 32-bit pattern
+            v &= m
+            return ((v >> k) | (m << (32 - k) & m if v & 0x80000000 else 0)) & m
+        s = seed & m
+        s = (s ^ 61) ^ sar(s, 16)
+        s = (s * 9) & m
+        s = s ^ sar(s, 4)
+        s = (s * 0x27D4EB2D) & m
+        s = s ^ sar(s, 15)
+        return s
+    for seed in [0, 1, 61, 1024, 123456789, 2 ** 31 - 1, -1, -2 ** 31, 987654]:
+        assert int(_wang_hash(seed).astype(np.uint32)) == ref(seed)
