@@ -80,6 +80,8 @@ def lib() -> C.CDLL:
             "orc_env_sample": ([C.POINTER(OrcEnv), C.c_float, P, C.c_int64, P], C.c_int),
             "orc_env_eval": ([C.POINTER(OrcEnv), C.c_float, P, C.c_int64, P], C.c_int),
             "orc_noise_walk": ([P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P], C.c_int),
+            "orc_generate_rays": ([C.POINTER(OrcCamera), C.POINTER(OrcSettings), C.c_int32, C.c_int32, P, P,
+                                   C.c_int64, P], C.c_int),
         }
         for name, (args, res) in sig.items():
             fn = getattr(L, name)
@@ -306,6 +308,17 @@ def noise_walk(noise: np.ndarray, px: int, py: int, sample: int, n: int) -> np.n
     out = np.empty((n, 4), np.float32)
     assert lib().orc_noise_walk(_p(t), px, py, sample, n, _p(out)) == 0
     return out
+
+
+def generate_rays(cam, s, width: int, height: int, frag, u):
+    """Camera rays for window positions frag (n, 2) and random blocks u (n, 4)
+    -> origins (n, 3), directions (n, 3)."""
+    f = np.ascontiguousarray(frag, dtype=np.float32)
+    uu = np.ascontiguousarray(u, dtype=np.float32)
+    out = np.empty((f.shape[0], 6), np.float32)
+    assert lib().orc_generate_rays(C.byref(camera(cam)), C.byref(settings(s)), width, height, _p(f), _p(uu),
+                                   f.shape[0], _p(out)) == 0
+    return out[:, :3], out[:, 3:]
 
 
 def builtins(fn: int, a, b=None) -> np.ndarray:

@@ -1494,6 +1494,27 @@ int orc_noise_walk(const float* noise, int32_t px, int32_t py, int32_t sample, i
   return 0;
 }
 
+int orc_generate_rays(const orc_camera* cam, const orc_settings* s, int32_t w, int32_t h, const float* frag,
+                      const float* u, int64_t n, float* out) {
+  const uint8_t cell = 0;
+  orc_material m;
+  std::memset(&m, 0, sizeof(m));
+  orc_scene sc;
+  sc.res[0] = sc.res[1] = sc.res[2] = 1;
+  sc.grid = &cell; sc.palette = &m; sc.n_palette = 1; sc.emissive = nullptr; sc.n_emissive = 0;
+  Tracer<float> T;
+  if (!T.setup(cam, s, &sc, nullptr, nullptr, w, h)) return -1;
+  for (int64_t i = 0; i < n; ++i) {
+    Rng rng;
+    rng.mode = 1; rng.noise = u + 4 * i; rng.ox = 0; rng.oy = 0;
+    V3<float> o, d;
+    T.generate_ray(v3<float>(frag[2 * i], frag[2 * i + 1], T.frag_z), rng, &o, &d);
+    float* r = out + 6 * i;
+    r[0] = o.x; r[1] = o.y; r[2] = o.z; r[3] = d.x; r[4] = d.y; r[5] = d.z;
+  }
+  return 0;
+}
+
 int orc_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n) {
   for (int64_t i = 0; i < n; ++i) {
     const float x = a[i];

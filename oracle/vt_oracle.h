@@ -169,6 +169,10 @@ int orc_env_eval(const orc_env* env, float rotation, const float* dirs, int64_t 
 /* The first n draws (n*4 floats) of the noise-table stream of pixel (px, py)
  * and sample (randomNumberGeneratorOffset + rand, random.h:13-27). */
 int orc_noise_walk(const float* noise, int32_t px, int32_t py, int32_t sample, int32_t n, float* out);
+/* generateRay (generateRay.h:1-123) for fragments at window positions frag
+ * (n*2) with the random block u (n*4) -> out n*6 {origin[3], direction[3]}. */
+int orc_generate_rays(const orc_camera* cam, const orc_settings* s, int32_t width, int32_t height,
+                      const float* frag, const float* u, int64_t n, float* out);
 /* Builtins of the float build for accuracy tests (fn as vt_diag_builtins). */
 int orc_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n);
 

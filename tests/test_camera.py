@@ -107,3 +107,73 @@ def test_focus_on_bounds_and_fly():
     np.testing.assert_allclose(np.array(cam.eye) - before, [100, 0, 100], atol=1e-3)
     with pytest.raises(L.VtError):
         L.call("vt_camera_fly_key", C.byref(cam), 9)
+
+
+def _frame(cam):
+    """CameraParameters::getBasis (cameraParameters.cpp:43-50): forward to the
+    target, right = (0, 1, 0) x forward, up = forward x right.  That right
+    vector points to the viewer's left, so window x runs the other way from
+    a gluLookAt frame: the reference's images are mirrored left to right."""
+    eye = np.array(cam.eye, float)
+    f = np.array(cam.target, float) - eye
+    f /= np.linalg.norm(f)
+    r = np.cross([0.0, 1.0, 0.0], f)
+    r /= np.linalg.norm(r)
+    return eye, f, r, np.cross(f, r)
+
+
+def _pixel_dirs(cam, w, h, frag):
+    """World direction through window position frag of a perspective camera
+    with vertical field of view fov_y and aspect w / h."""
+    eye, f, r, u = _frame(cam)
+    t = math.tan(cam.fov_y / 2)
+    nx = 2 * frag[:, 0] / w - 1
+    ny = 2 * frag[:, 1] / h - 1
+    d = f[None] + (nx * t * w / h)[:, None] * r[None] + (ny * t)[:, None] * u[None]
+    return d / np.linalg.norm(d, axis=1, keepdims=True)
+
+
+def test_generated_rays_follow_the_camera_geometry(orc):
+    """generateRay (generateRay.h:1-123) on the oracle, against the geometry it
+    implements: a pinhole ray leaves the eye through the jittered pixel
+    position; thin-lens rays for one window position leave the lens disk
+    and all pass through one point on the focal plane; orthographic rays are
+    parallel to the view axis."""
+    from voxeltoy_gb300 import scenes as S
+    rng = np.random.default_rng(8)
+    w, h = 320, 200
+    s = S.physical_settings(max_bounces=1)
+    n = 2000
+    frag = np.stack([rng.uniform(0, w, n), rng.uniform(0, h, n)], 1)
+    u = rng.random((n, 4))
+    # pinhole: jitter u - 0.5 in window units (generateRay.h:15-25)
+    cam = make_cam((-300.0, 800.0, 650.0), (10.0, -20.0, 30.0), 40.0, L.VT_LENS_PINHOLE)
+    o, d = orc.generate_rays(cam, s, w, h, frag, u)
+    want = _pixel_dirs(cam, w, h, frag + (u[:, :2] - 0.5))
+    assert np.abs(o - np.array(cam.eye)).max() < 1e-3
+    assert np.linalg.norm(d - want, axis=1).max() < 2e-5
+    # thin lens without jitter: the rays of one window position meet on the
+    # focal plane, at focal_distance along the view axis
+    cam = make_cam((0.0, 400.0, -1800.0), (0.0, 0.0, 0.0), 45.0, L.VT_LENS_THIN_LENS)
+    cam.lens_radius, cam.focal_distance = 40.0, 1500.0
+    s.quirks = L.VT_QUIRK_THINLENS_NO_JITTER
+    eye, f, r, up = _frame(cam)
+    for k in range(20):
+        fr = np.repeat(frag[k:k + 1], 64, 0)
+        o, d = orc.generate_rays(cam, s, w, h, fr, rng.random((64, 4)))
+        o = o.astype(np.float64)
+        d = d.astype(np.float64)
+        off = o - eye
+        assert np.abs(off @ f).max() < 1e-3                       # the lens lies in the eye plane
+        assert np.linalg.norm(off, axis=1).max() <= 40.0 + 1e-3
+        p = _pixel_dirs(cam, w, h, frag[k:k + 1])[0]
+        focus = eye + p * (1500.0 / (p @ f))                      # on the plane at 1500 along the view axis
+        t = ((focus - o) * d).sum(1)
+        miss = np.linalg.norm(o + t[:, None] * d - focus, axis=1)
+        assert miss.max() < 2e-2
+    # orthographic: every ray parallel to the view axis
+    cam = make_cam((500.0, 500.0, 500.0), (0.0, 0.0, 0.0), 60.0, L.VT_LENS_ORTHOGRAPHIC)
+    s.quirks = 0
+    o, d = orc.generate_rays(cam, s, w, h, frag, u)
+    assert np.abs(d - _frame(cam)[1]).max() < 1e-6
+    assert np.ptp((o - np.array(cam.eye)) @ _frame(cam)[1]) < 1e-2  # origins on one plane
