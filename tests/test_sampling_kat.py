@@ -9,7 +9,9 @@ BSDFs (lambertian.h:10-29, microfacet.h:1-123, materials.h:7-43):
   * reciprocity, f(wo, wi) = f(wi, wo);
   * the pdf integrates to 1 over the sphere (midpoint quadrature);
   * directional albedo: Lambert gives its albedo, Torrance-Sparrow with the
-    V-cavity G and a Fresnel term <= 1 stays at or below 1.
+    V-cavity G and a Fresnel term <= 1 stays at or below 1;
+  * closed forms at normal incidence, with and without the reference's
+    fixed IOR and exponent-is-roughness behaviours.
 Environment (image.cpp:68-389 as restated, lights.h:20-55,
 envMapSample.h:23-123):
   * the marginal and conditional CDFs equal an independent float64 build
@@ -166,3 +168,32 @@ def test_env_pdf_integrates_to_one(orc, sky):
     d, dw = sphere_grid(1000, 2000)
     _, p = orc.env_eval(env, d)
     assert abs(p.astype(np.float64).sum() * dw - 1.0) < 1e-3
+
+
+@pytest.mark.parametrize("quirks", [0, "reference"])
+def test_torrance_sparrow_at_normal_incidence(orc, quirks):
+    """wo = wi = the normal gives wh = the normal, G = 1 and Schlick's F = F0,
+    so f = R D(0) F0 / 4 and pdf = (e + 1) / (8 pi) (microfacet.h:19-37,
+    64-91).  With the reference's quirks F0 comes from the fixed IOR 7.3
+    ((6.3 / 8.3)^2), the Blinn exponent is the roughness field, and the
+    metal's reflectance scales D; without them F0 is the material's colour,
+    the exponent 2 / r^2 - 2 and D is unscaled."""
+    from voxeltoy_gb300 import _lib as L
+    q = 0 if quirks == 0 else (L.VT_QUIRK_FIXED_IOR | L.VT_QUIRK_EXPONENT_IS_ROUGHNESS)
+    up = np.array([[0.0, 1.0, 0.0]])
+    for t, albedo, rough in [(1, (0.9, 0.6, 0.3), 0.25), (1, (0.5, 0.5, 0.5), 0.5), (2, (0.2, 0.5, 0.9), 0.1)]:
+        a = np.array(albedo, np.float32).astype(np.float16).astype(np.float64)   # FP16 palette records
+        r = float(np.float16(rough))
+        f, pdf = orc.bsdf_eval((t, albedo, rough), up, up, quirks=q)
+        refl = a if t == 1 else np.ones(3)
+        if q:
+            e = r
+            f0 = np.full(3, ((1 - 7.3) / (1 + 7.3)) ** 2)
+            d_scale = refl
+        else:
+            e = max(2 / max(r * r, 1e-6) - 2, 0.0)
+            f0 = refl
+            d_scale = np.ones(3)
+        want = d_scale * (e + 2) / (2 * np.pi) * f0 / 4
+        np.testing.assert_allclose(f[0], want, rtol=2e-5)
+        np.testing.assert_allclose(pdf[0], (e + 1) / (8 * np.pi), rtol=2e-5)
