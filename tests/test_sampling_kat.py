@@ -20,7 +20,9 @@ envMapSample.h:23-123):
   * the pdf a sample reports equals the pdf evaluated along its direction;
   * a chi-square test of sampled directions against the texel
     probabilities of that independent build;
-  * the pdf integrates to 1 over the sphere.
+  * the pdf integrates to 1 over the sphere;
+  * the background rotation turns the map about +Y, for evaluation and
+    sampling alike.
 """
 import numpy as np
 import pytest
@@ -197,3 +199,27 @@ def test_torrance_sparrow_at_normal_incidence(orc, quirks):
         want = d_scale * (e + 2) / (2 * np.pi) * f0 / 4
         np.testing.assert_allclose(f[0], want, rtol=2e-5)
         np.testing.assert_allclose(pdf[0], (e + 1) / (8 * np.pi), rtol=2e-5)
+
+
+def test_env_rotation_turns_the_map_about_y(orc, sky):
+    """uvCoordFromVector (coordinates.h:97-109) adds the rotation to the
+    azimuth atan2(z, x): looking along d with rotation rho sees what d turned
+    by rho about +Y sees without it; sampling with rho returns directions
+    turned by -rho, with the same pdf."""
+    _, env = sky
+    rng = np.random.default_rng(5)
+    d = rng.normal(size=(20000, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    for rho in (0.5, 2.0, -1.25):
+        c, s = np.cos(rho), np.sin(rho)
+        # azimuth phi = atan2(z, x) -> phi + rho
+        turned = np.stack([c * d[:, 0] - s * d[:, 2], d[:, 1], s * d[:, 0] + c * d[:, 2]], 1)
+        L1, p1 = orc.env_eval(env, d, rotation=rho)
+        L0, p0 = orc.env_eval(env, turned)
+        assert np.quantile(np.abs(L1 - L0).max(1) / np.abs(L0).max(1), 0.99) < 1e-3
+        u = rng.random((5000, 2))
+        ds, _, ps = orc.env_sample(env, u, rotation=rho)
+        d0, _, p00 = orc.env_sample(env, u)
+        back = np.stack([c * ds[:, 0] - s * ds[:, 2], ds[:, 1], s * ds[:, 0] + c * ds[:, 2]], 1)
+        assert np.abs(back - d0).max() < 1e-4
+        np.testing.assert_array_equal(ps, p00)
