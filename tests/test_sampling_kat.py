@@ -11,7 +11,9 @@ BSDFs (lambertian.h:10-29, microfacet.h:1-123, materials.h:7-43):
   * directional albedo: Lambert gives its albedo, Torrance-Sparrow with the
     V-cavity G and a Fresnel term <= 1 stays at or below 1;
   * closed forms at normal incidence, with and without the reference's
-    fixed IOR and exponent-is-roughness behaviours.
+    fixed IOR and exponent-is-roughness behaviours;
+  * Kolmogorov-Smirnov tests of the cosine-hemisphere and Blinn half-vector
+    sampling distributions.
 Environment (image.cpp:68-389 as restated, lights.h:20-55,
 envMapSample.h:23-123):
   * the marginal and conditional CDFs equal an independent float64 build
@@ -223,3 +225,21 @@ def test_env_rotation_turns_the_map_about_y(orc, sky):
         back = np.stack([c * ds[:, 0] - s * ds[:, 2], ds[:, 1], s * ds[:, 0] + c * ds[:, 2]], 1)
         assert np.abs(back - d0).max() < 1e-4
         np.testing.assert_array_equal(ps, p00)
+
+
+def test_sampled_directions_follow_their_distributions(orc):
+    """Kolmogorov-Smirnov tests of the samplers' published distributions:
+    the cosine-weighted hemisphere of sampling.h:2-20 has P(cos theta <= t)
+    = t^2; the Blinn half vector of sampleD (microfacet.h:41-61), cos theta_h
+    = u^(1 / (e + 1)), has P(cos theta_h <= t) = t^(e + 1)."""
+    stats = pytest.importorskip("scipy.stats")
+    rng = np.random.default_rng(6)
+    n = 100000
+    wo = np.tile(WO, (n, 1))
+    wi, _, _ = orc.bsdf_sample(LAMBERT, wo, rng.random((n, 2)))
+    assert stats.kstest(wi[:, 1].astype(np.float64), lambda t: np.clip(t, 0, 1) ** 2).pvalue > 1e-3
+    for mat, e in ((METAL, 2 / np.float16(0.3) ** 2 - 2), (PLASTIC, 2 / np.float16(0.1) ** 2 - 2)):
+        wi, _, _ = orc.bsdf_sample(mat, wo, rng.random((n, 2)))
+        wh = wi.astype(np.float64) + wo
+        wh /= np.linalg.norm(wh, axis=1, keepdims=True)
+        assert stats.kstest(wh[:, 1], lambda t: np.clip(t, 0, 1) ** (float(e) + 1)).pvalue > 1e-3
