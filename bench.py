@@ -153,11 +153,13 @@ def all_max(world, x: float) -> float:
     return float(t.item())
 
 
-def workload_config(args):
+def workload_config(args, make=None):
+    """The workload's inputs; `make` = the oracle module builds the camera and
+    settings without the library (the reference arm)."""
     from voxeltoy_gb300 import scenes as S
     if args.workload == "config1":
-        return S.config1(edge=args.edge, width=args.res, height=args.res, spp=args.spp, seed=1)
-    return S.config2(edge=args.edge, width=args.res, height=args.res, spp=args.spp, seed=2)
+        return S.config1(edge=args.edge, width=args.res, height=args.res, spp=args.spp, seed=1, make=make)
+    return S.config2(edge=args.edge, width=args.res, height=args.res, spp=args.spp, seed=2, make=make)
 
 
 def cpu_sample_rate(cfg, seconds: float, threads: int = 0) -> dict:
@@ -196,22 +198,16 @@ def cpu_sample_rate(cfg, seconds: float, threads: int = 0) -> dict:
                       f"{times} ({paths} paths, {dt:.1f} s, FP32 oracle, {threads or os.cpu_count()} threads)"}
 
 
-def emissive_for_oracle(cfg):
-    from voxeltoy_gb300 import _lib as L
-    from oracle import binding as orc
-    if cfg.scene_flags & L.VT_SCENE_AUTO_EMISSIVE:
-        cand = np.flatnonzero(np.isin(cfg.voxels.ravel(), [i + 1 for i, m in enumerate(cfg.palette)
-                                                            if sum(m[1]) > 0])).astype(np.int32)
-        return orc.prune_emissive(cfg.voxels, cand) if cfg.scene_flags & L.VT_SCENE_PRUNE_EMISSIVE else cand
-    return None
-
-
 def run_reference(args, world, rank):
-    """CPU restatement of the reference path on the host cores."""
+    """CPU restatement of the reference path on the host cores.  Inputs,
+    camera and settings come from the numpy generators and the oracle
+    alone: this arm never loads the CUDA library."""
     if rank != 0:
         return 0
-    cfg = workload_config(args)
-    cfg._emissive = emissive_for_oracle(cfg)
+    from oracle import binding as orc
+    cfg = workload_config(args, make=orc)
+    # the emissive list of an auto-emissive, pruned scene (config 2); none otherwise
+    cfg._emissive = orc.emissive_list(cfg.voxels, cfg.palette, prune=True) if args.workload == "config2" else None
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_sample_rate(cfg, 0.5, threads)

@@ -6,6 +6,7 @@ bench.py as the checker; the product never imports it.
 from __future__ import annotations
 
 import ctypes as C
+import math
 
 import numpy as np
 
@@ -55,6 +56,9 @@ def lib() -> C.CDLL:
         P = C.c_void_p
         sig = {
             "orc_camera_uniforms": ([C.POINTER(OrcCamera), C.c_int32, C.c_int32, P], C.c_int),
+            "orc_camera_default": ([C.POINTER(OrcCamera)], None),
+            "orc_camera_orbit": ([C.POINTER(OrcCamera), C.c_float, C.c_float], None),
+            "orc_settings_default": ([C.POINTER(OrcSettings)], None),
             "orc_render_samples": ([C.POINTER(OrcCamera), C.POINTER(OrcSettings), C.POINTER(OrcScene),
                                     C.POINTER(OrcEnv), P, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, P, P,
                                     P], C.c_int),
@@ -121,6 +125,46 @@ def settings(s, integrator: int = 0) -> OrcSettings:
         else:
             setattr(o, name, v)
     return o
+
+
+# Cameras and settings built by the oracle alone, with the signatures of
+# voxeltoy_gb300.scenes.orbit_camera / physical_settings, so that a
+# configuration generated with make=<this module> never loads the library.
+def orbit_camera(distance: float = 2000.0, theta_deg: float = 120.0, phi_deg: float = 45.0, fov_deg: float = 45.0,
+                 lens: int = 0, aperture: float = 0.0, focus: float | None = None) -> OrcCamera:
+    cam = OrcCamera()
+    lib().orc_camera_default(C.byref(cam))
+    cam.target[:] = [0.0, 0.0, 0.0]
+    cam.eye[:] = [0.0, 0.0, -distance]
+    lib().orc_camera_orbit(C.byref(cam), math.radians(theta_deg), math.radians(phi_deg))
+    cam.fov_y = math.radians(fov_deg)
+    cam.lens_model = lens
+    cam.lens_radius = aperture
+    cam.focal_distance = distance if focus is None else focus
+    return cam
+
+
+def physical_settings(max_bounces: int, rr_start: int = -1, seed: int = 0, top=(1.0, 1.0, 1.0),
+                      bottom=(1.0, 1.0, 1.0)) -> OrcSettings:
+    s = OrcSettings()
+    lib().orc_settings_default(C.byref(s))
+    s.max_bounces = max_bounces
+    s.max_samples = 1 << 30
+    s.rr_start_bounce = rr_start
+    s.quirks = 0
+    s.nee_emission_scale = 1.0
+    s.background_top[:] = list(top)
+    s.background_bottom[:] = list(bottom)
+    s.seed = seed
+    return s
+
+
+def emissive_list(voxels: np.ndarray, palette, prune: bool = True) -> np.ndarray:
+    """Linear indices of the voxels whose palette entry emits, in voxel order,
+    then pruned of voxels with no empty 6-neighbour (import.cpp:133-203)."""
+    hot = [i + 1 for i, m in enumerate(palette) if sum(m[1]) > 0]
+    cand = np.flatnonzero(np.isin(np.asarray(voxels).ravel(), hot)).astype(np.int32)
+    return prune_emissive(voxels, cand) if prune else cand
 
 
 class Scene:

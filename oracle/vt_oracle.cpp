@@ -1170,6 +1170,38 @@ int orc_camera_uniforms(const orc_camera* cam, int32_t w, int32_t h, float* out)
   return 0;
 }
 
+void orc_camera_default(orc_camera* cam) {
+  std::memset(cam, 0, sizeof(*cam));
+  cam->eye[2] = -100.0f;
+  cam->near_distance = 0.1f;
+  cam->far_distance = 10000.0f;
+  cam->focal_distance = 99999999.0f;   // initial value of the focal-distance buffer (renderer.cpp:711-720)
+  cam->lens_model = 0;
+  cam->fov_y = std::atan2(36.0f * 0.5f, 50.0f) * 2.0f;   // setFocalLength(50) (cameraParameters.cpp:139-150)
+}
+
+void orc_camera_orbit(orc_camera* cam, float theta, float phi) {
+  const float d[3] = {cam->target[0] - cam->eye[0], cam->target[1] - cam->eye[1], cam->target[2] - cam->eye[2]};
+  const float r = std::sqrt((d[0] * d[0] + d[1] * d[1]) + d[2] * d[2]);
+  const float st = std::sin(theta);
+  const float s[3] = {st * std::cos(phi), std::cos(theta), st * std::sin(phi)};
+  for (int i = 0; i < 3; ++i) cam->eye[i] = cam->target[i] - r * s[i];
+}
+
+void orc_settings_default(orc_settings* s) {
+  std::memset(s, 0, sizeof(*s));
+  s->max_bounces = 1;
+  s->max_samples = 2048 * 2048;
+  s->rr_start_bounce = -1;
+  s->gamma = 2.2f;
+  s->exposure = 1.0f;
+  s->nee_emission_scale = 10.0f;
+  s->wireframe_thickness = 0.01f;
+  s->background_top[0] = 153.0f / 255 * 2; s->background_top[1] = 187.0f / 255 * 2; s->background_top[2] = 201.0f / 255 * 2;
+  s->background_bottom[0] = 77.0f / 255; s->background_bottom[1] = 64.0f / 255; s->background_bottom[2] = 50.0f / 255;
+  s->quirks = 0xFFu;
+}
+
 int orc_render_samples(const orc_camera* cam, const orc_settings* s, const orc_scene* scene, const orc_env* env,
                        const float* noise, int32_t w, int32_t h, int32_t sample, int32_t precision,
                        int32_t threads, float* rgba, int32_t* hits, uint64_t* counters) {

@@ -95,6 +95,17 @@ typedef struct orc_env {
  * [48:52] viewport. */
 int orc_camera_uniforms(const orc_camera* cam, int32_t width, int32_t height, float* out);
 
+/* CameraParameters defaults (cameraParameters.cpp:7-17): target 0, eye at
+ * distance 100 on -Z, near 0.1, far 10000, 50 mm on a 36 mm film, pinhole,
+ * focus at the pick buffer's initial value. */
+void orc_camera_default(orc_camera* cam);
+/* CameraParameters::orbitAroundTarget (cameraParameters.cpp:84-94):
+ * eye = target - |target - eye| * (sin t cos p, cos t, sin t sin p). */
+void orc_camera_orbit(orc_camera* cam, float theta, float phi);
+/* RenderSettings defaults with every reference quirk on
+ * (renderSettings.h, pathTracer.fs:25-26 background colours). */
+void orc_settings_default(orc_settings* s);
+
 /* One sample per pixel (sample index `sample`): per-sample output rgba
  * (w*h*4) and first-hit records hits (w*h*4 int32, nullable).
  * precision: 32 or 64.  counters (nullable): 8 event counts. */

@@ -196,23 +196,34 @@ class RenderConfig:
     notes: dict = field(default_factory=dict)
 
 
-def config1(edge: int = 64, width: int = 256, height: int = 256, spp: int = 16, seed: int = 1) -> RenderConfig:
+def _maker(make):
+    """Where cameras and settings come from: this module (the library's
+    camera math), or any object with the same orbit_camera and
+    physical_settings functions."""
+    import sys
+    return sys.modules[__name__] if make is None else make
+
+
+def config1(edge: int = 64, width: int = 256, height: int = 256, spp: int = 16, seed: int = 1,
+            make=None) -> RenderConfig:
     g = sphere_union(edge, 8, seed)
-    cam = orbit_camera()
-    s = physical_settings(max_bounces=4, rr_start=-1, seed=seed)
+    mk = _maker(make)
+    cam = mk.orbit_camera()
+    s = mk.physical_settings(max_bounces=4, rr_start=-1, seed=seed)
     return RenderConfig("config1", g, [lambert(0.7)], cam, s, width, height, spp)
 
 
 def config2(edge: int = 256, width: int = 1024, height: int = 1024, spp: int = 256, seed: int = 2,
-            env_size=(1024, 512)) -> RenderConfig:
+            env_size=(1024, 512), make=None) -> RenderConfig:
     field_ = value_noise_fbm(edge, 3, seed)
     occ = threshold_occupancy(field_, 0.35)
     rng = np.random.default_rng(seed + 7)
     vox = occ * rng.integers(1, 17, size=occ.shape, dtype=np.uint8)
     emissive = (rng.random(occ.shape) < 0.02) & (occ > 0)
     vox[emissive] = 17
-    cam = orbit_camera(lens=L.VT_LENS_THIN_LENS, aperture=0.02 * 1000.0)
-    s = physical_settings(max_bounces=8, rr_start=3, seed=seed)
+    mk = _maker(make)
+    cam = mk.orbit_camera(lens=L.VT_LENS_THIN_LENS, aperture=0.02 * 1000.0)
+    s = mk.physical_settings(max_bounces=8, rr_start=3, seed=seed)
     env = sky_sun_env(*env_size)
     return RenderConfig("config2", vox, config2_palette(seed), cam, s, width, height, spp, env_rgb=env,
                         scene_flags=L.VT_SCENE_AUTO_EMISSIVE | L.VT_SCENE_PRUNE_EMISSIVE)
