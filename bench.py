@@ -47,28 +47,13 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def l2_copy_gbs(device: int) -> float:
-    """Bandwidth of an L2-resident copy (read + write bytes; the best over
-    8, 16 and 32 MiB buffers and 5 runs of 200 copies each), the denominator
-    of the L2 fraction."""
-    import torch
-    best_gbs = 0.0
-    for mib in (8, 16, 32):
-        a = torch.ones(mib << 18, dtype=torch.float32, device=f"cuda:{device}")
-        b = torch.empty_like(a)
-        for _ in range(20):
-            b.copy_(a)
-        for _ in range(5):
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for _ in range(200):
-                b.copy_(a)
-            e1.record()
-            e1.synchronize()
-            best_gbs = max(best_gbs, 2 * a.numel() * 4 * 200 / (e0.elapsed_time(e1) * 1e-3) / 1e9)
-        del a, b
-    return best_gbs
+def l2_read_gbs(ctx) -> dict:
+    """L2 read bandwidth: the best of five single launches, each sweeping a
+    32 MiB buffer (a quarter of L2) 1000 times with L1-bypassing loads
+    (vt_diag_l2_read_bandwidth), the denominator of the L2 fraction."""
+    best = max(ctx.l2_read_bandwidth(32 << 20, 1000) for _ in range(5))
+    return {"gbs": best, "source": "one kernel launch reading a 32 MiB L2-resident buffer 1000 times "
+                                   "(ld.global.cg, best of 5), measured in this run"}
 
 
 class ClockSampler:
@@ -269,6 +254,39 @@ class EventTimer:
         self.ms = self.e0.elapsed_time(self.e1)
 
 
+def image_digest(img: np.ndarray) -> str:
+    import hashlib
+    return hashlib.blake2b(np.ascontiguousarray(img).view(np.uint8), digest_size=16).hexdigest()
+
+
+def rel_rmse(got: np.ndarray, ref: np.ndarray) -> dict:
+    """Relative RMSE of RGB over the pixels finite in both images:
+    sqrt(mean((got - ref)^2)) / sqrt(mean(ref^2))."""
+    g = got[..., :3].astype(np.float64)
+    r = ref[..., :3].astype(np.float64)
+    ok = np.isfinite(g).all(-1) & np.isfinite(r).all(-1)
+    err = float(np.sqrt(np.mean((g[ok] - r[ok]) ** 2)) / max(np.sqrt(np.mean(r[ok] ** 2)), 1e-300))
+    return {"rel_rmse": err, "pixels": int(ok.size), "nonfinite_pixels": int((~ok).sum())}
+
+
+def rmse_vs_fp64(cfg, img: np.ndarray, spp: int, rows, emissive=None, noise=None) -> dict:
+    """The FP64 oracle's image of rows [r0, r1) of `cfg`'s frame at `spp`
+    samples per pixel (the same counter-based random streams), against the
+    same rows of the GPU's image: the arithmetic error of the FP32 path.
+    The oracle is the checker here; nothing it computes is timed."""
+    from oracle import binding as orc
+    r0, r1 = rows
+    osc = orc.Scene(cfg.voxels, cfg.palette, emissive)
+    oenv = orc.Env(cfg.env_rgb) if cfg.env_rgb is not None else orc.Env()
+    t0 = time.perf_counter()
+    ref, _ = orc.render_average(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height, spp, 64, rows=(r0, r1),
+                                noise=noise)
+    rec = rel_rmse(img[r0:r1], ref[r0:r1])
+    rec.update(frame=f"{cfg.width}x{cfg.height}", rows=[int(r0), int(r1)], spp=int(spp),
+               paths=int((r1 - r0) * cfg.width * spp), oracle_s=round(time.perf_counter() - t0, 2))
+    return rec
+
+
 def batching_jobs(ctx, n: int):
     """The batching configuration: scene i from the sphere-union generator
     (seed 100 + i, edge log-uniform 32-512, occupancy U[10%, 50%]), a
@@ -278,44 +296,41 @@ def batching_jobs(ctx, n: int):
     for i in range(n):
         vox, res, seed = S.config3_scene(i)
         cfg = S.config1(edge=8, width=res, height=res, spp=64, seed=seed)
+        cfg.voxels = vox
         sc = Scene.dense(ctx, vox, cfg.palette)
-        made.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, res, res), vox))
+        made.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, res, res), cfg))
     return made
 
 
-def run_batching(args, world, rank, local):
+def batching_record(ctx, n_scenes: int, steps: int, rmse_scenes: int = 4, e2e: bool = True) -> dict:
+    """Config 3: n uneven scenes in one wavefront launch (batched) against one
+    wavefront launch per scene and against the reference's structure (the
+    per-pixel kernel, one launch per scene and pass), identical images in all
+    three forms; the relative RMSE of the batched images of the scenes with
+    the largest grids (and the smallest) against the FP64 oracle."""
     import torch
-    from voxeltoy_gb300 import Context
+    from voxeltoy_gb300 import autotune
     spp = 64
-    ctx = Context(local)
-    made = batching_jobs(ctx, args.scenes)
+    made = batching_jobs(ctx, n_scenes)
     jobs = [m[1] for m in made]
     paths = sum(j.width * j.height for j in jobs) * spp
-    from voxeltoy_gb300 import autotune
     best = autotune.tune(ctx, jobs, passes=16, repeats=1, use_cache=False,
                          grid={"path_slots": [1 << 22, 1 << 23, 1 << 24], "trace_blocks_per_sm": [0],
-                               "trace_steps": [16]})
-    timer = EventTimer(ctx, local)
+                               "trace_steps": [16], "lanes": [2]})
+    timer = EventTimer(ctx, ctx_device(ctx))
 
     def reset():
         for j in jobs:
             j.reset()
         torch.cuda.synchronize()
 
-    def batched():
-        ctx.render_batch(jobs, spp, kernel=2)
-
-    def plain_loop():                  # the reference's structure: one launch per scene and pass
-        ctx.render_batch(jobs, spp, kernel=1)
-
-    def per_scene():                   # one wavefront render per scene
-        for j in jobs:
-            j.render(spp)
-
-    out = {}
-    images = {}
-    for name, fn, reps in (("batched", batched, args.steps), ("per_scene_wavefront", per_scene, 1),
-                           ("plain_loop", plain_loop, 1)):
+    forms = (("batched", lambda: ctx.render_batch(jobs, spp, kernel=2), steps),
+             ("per_scene_wavefront", lambda: [j.render(spp) for j in jobs], 1),
+             ("plain_loop", lambda: ctx.render_batch(jobs, spp, kernel=1), 1))
+    out, digests, rmse_imgs = {}, {}, {}
+    by_edge = sorted(range(len(made)), key=lambda k: made[k][2].voxels.shape[0])
+    picks = sorted(set(by_edge[-(rmse_scenes - 1):] + by_edge[:1])) if rmse_scenes > 0 else []
+    for name, fn, reps in forms:
         times = []
         for k in range(reps + 1):
             reset()
@@ -323,150 +338,250 @@ def run_batching(args, world, rank, local):
                 fn()
             if k:
                 times.append(timer.ms)
-        out[name] = {"ms": float(np.median(times)), "mpaths_s": paths / (np.median(times) * 1e-3) / 1e6}
-        images[name] = [j.readback() for j in jobs]
-    same = all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
-               for name in ("per_scene_wavefront", "plain_loop") for a, b in zip(images["batched"], images[name]))
-    # end to end: upload every scene from pinned host memory, render the
-    # batch, read every image back into pinned host memory
+        ms = float(np.median(times))
+        out[name] = {"ms": ms, "mpaths_s": paths / (ms * 1e-3) / 1e6}
+        imgs = [j.readback() for j in jobs]
+        digests[name] = [image_digest(a) for a in imgs]
+        if name == "batched":
+            rmse_imgs = {k: imgs[k] for k in picks}
+        del imgs
+    same = digests["batched"] == digests["per_scene_wavefront"] == digests["plain_loop"]
+    rmse = []
+    for k in picks:
+        cfg = made[k][2]
+        band = min(32, cfg.height)
+        r0 = (cfg.height - band) // 2
+        rec = rmse_vs_fp64(cfg, rmse_imgs[k], spp, (r0, r0 + band))
+        rec.update(scene=k, grid=int(cfg.voxels.shape[0]))
+        rmse.append(rec)
+    rec = {"scenes": len(jobs), "spp": spp, "paths": int(paths),
+           "voxels": int(sum(m[2].voxels.size for m in made)),
+           "batched": out["batched"], "per_scene_wavefront": out["per_scene_wavefront"],
+           "plain_loop": out["plain_loop"],
+           "batched_vs_plain": out["plain_loop"]["ms"] / out["batched"]["ms"],
+           "batched_vs_per_scene": out["per_scene_wavefront"]["ms"] / out["batched"]["ms"],
+           "identical_images": bool(same), "rmse_vs_fp64": rmse,
+           "tuning": {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps", "lanes")}}
+    vox_h = [torch.from_numpy(np.ascontiguousarray(m[2].voxels)).pin_memory().numpy() for m in made] if e2e else []
+    cfgs = [m[2] for m in made]
+    for sc, j, _c in made:
+        j.close(); sc.close()
+    if e2e:
+        # upload every scene from pinned host memory, render the batch, read
+        # every image back into pinned host memory
+        from voxeltoy_gb300 import Job, Scene
+        outs = [torch.empty((c.height, c.width, 4), dtype=torch.float32).pin_memory().numpy() for c in cfgs]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_jobs = []
+        for vox, cfg in zip(vox_h, cfgs):
+            sc = Scene.dense(ctx, vox, cfg.palette)
+            e2e_jobs.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, cfg.width, cfg.height)))
+        ctx.render_batch([j for _s, j in e2e_jobs], spp, kernel=2)
+        d2h = 0
+        for (_s, j), dst in zip(e2e_jobs, outs):
+            d2h += j.readback(out=dst).nbytes
+        e2e_s = time.perf_counter() - t0
+        for sc, j in e2e_jobs:
+            j.close(); sc.close()
+        rec["e2e"] = {"value": paths / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(sum(v.nbytes for v in vox_h)),
+                      "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3}
+    return rec
+
+
+def ctx_device(ctx) -> int:
     import torch
-    vox_h = [torch.from_numpy(np.ascontiguousarray(m[2])).pin_memory().numpy() for m in made]
-    for sc, j, _v in made:
-        j.close(); sc.close()
-    from voxeltoy_gb300 import Job, Scene, scenes as S
-    cfgs = [S.config1(edge=8, width=jobs[i].width, height=jobs[i].width, spp=spp, seed=100 + i)
-            for i in range(len(vox_h))]
-    outs = [torch.empty((c.height, c.width, 4), dtype=torch.float32).pin_memory().numpy() for c in cfgs]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    e2e_jobs = []
-    for vox, cfg in zip(vox_h, cfgs):
-        sc = Scene.dense(ctx, vox, cfg.palette)
-        e2e_jobs.append((sc, Job(ctx, sc, None, cfg.camera, cfg.settings, cfg.width, cfg.height)))
-    ctx.render_batch([j for _s, j in e2e_jobs], spp, kernel=2)
-    d2h = 0
-    for (_s, j), dst in zip(e2e_jobs, outs):
-        d2h += j.readback(out=dst).nbytes
-    e2e_s = time.perf_counter() - t0
-    for sc, j in e2e_jobs:
-        j.close(); sc.close()
+    return torch.cuda.current_device()
+
+
+def run_batching(args, world, rank, local):
+    from voxeltoy_gb300 import Context
+    ctx = Context(local)
+    b = batching_record(ctx, args.scenes, args.steps)
     ctx.close()
-    b = out["batched"]
-    return {"metric": METRIC, "value": b["mpaths_s"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": 1, "ms_per_step": b["ms"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded batching configuration)",
-            "config": {"workload": f"batching: {len(jobs)} sphere-union scenes (seed 100+i, edges 32-512 "
+    return {"metric": METRIC, "value": b["batched"]["mpaths_s"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": 1, "ms_per_step": b["batched"]["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded batching configuration)",
+            "config": {"workload": f"batching: {b['scenes']} sphere-union scenes (seed 100+i, edges 32-512 "
                                    f"log-uniform, occupancy U[10%,50%]), resolutions from {{128,256,512,1024}}^2, "
-                                   f"Lambert 0.7, white sky, 4 bounces, {spp} spp, one launch",
-                       "paths_per_step": paths, "voxels": int(sum(v.size for v in vox_h))},
-            "batched": b, "per_scene_wavefront": out["per_scene_wavefront"], "plain_loop": out["plain_loop"],
-            "batched_vs_plain": out["plain_loop"]["ms"] / b["ms"],
-            "batched_vs_per_scene": out["per_scene_wavefront"]["ms"] / b["ms"],
-            "identical_images": bool(same),
-            "e2e": {"value": paths / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(sum(v.nbytes for v in vox_h)),
-                    "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_s * 1e3},
-            "tuning": {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps")}}
+                                   f"Lambert 0.7, white sky, 4 bounces, {b['spp']} spp, one launch",
+                       "paths_per_step": b["paths"], "voxels": b["voxels"]},
+            "e2e": b.pop("e2e"), **b}
 
 
-def run_serving(args, world, rank, local):
-    """Poisson request stream through vt_server: each request is a
-    sphere-union scene (edge 64-512), a random orbit camera, a resolution
-    with edge uniform in 256-1024 and an spp target log-uniform in
-    16-1024; half of the requests reuse a resident scene.  Latency = arrival
-    to the target sample count, read from the server's own clock plus the
-    host's submission delay."""
-    from voxeltoy_gb300 import Context, Scene, Server, scenes as S
-    rng = np.random.default_rng(3)
-    n = max(1, int(rng.poisson(args.rate * args.duration)))
-    arrivals = np.sort(rng.uniform(0.0, args.duration, n))
-    pool_n = 16
+def serving_requests(rate: float, duration: float, seed: int = 3, pool_n: int = 16):
+    """The seeded request stream: Poisson arrivals, sphere-union scenes (edge
+    64-512) from a pool with reuse probability 0.5, random orbit cameras,
+    resolution edge uniform in 256-1024, spp log-uniform in 16-1024."""
+    from voxeltoy_gb300 import scenes as S
+    rng = np.random.default_rng(seed)
+    n = max(1, int(rng.poisson(rate * duration)))
+    arrivals = np.sort(rng.uniform(0.0, duration, n))
     pool = []
     for i in range(pool_n):
         edge = int(rng.integers(64, 513))
         pool.append(S.sphere_union(edge, None, 300 + i, occupancy=float(rng.uniform(0.1, 0.5))))
-    ctx = Context(local)
-    from voxeltoy_gb300 import _lib as L
-    order = L.VT_SERVE_LEAST_WORK if args.order == "least-work" else L.VT_SERVE_ARRIVAL
-    srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4, order=order,
-                 quick_paths=args.quick_paths, round_paths_cap=args.round_cap)
-    resident = []
+    n_resident = 0
     reqs = []
     for k in range(n):
         res = int(rng.integers(256, 1025))
         spp = int(round(math.exp(rng.uniform(math.log(16), math.log(1024)))))
-        reuse = bool(resident) and rng.random() < 0.5
-        pick = int(rng.integers(0, len(resident))) if reuse else int(rng.integers(0, pool_n))
+        reuse = n_resident > 0 and rng.random() < 0.5
+        pick = int(rng.integers(0, n_resident)) if reuse else int(rng.integers(0, pool_n))
         cam = S.orbit_camera(distance=2000.0, theta_deg=float(rng.uniform(0, 360)), phi_deg=float(rng.uniform(10, 80)))
-        reqs.append((res, spp, reuse, pick, cam))
+        reqs.append({"arrival": float(arrivals[k]), "res": res, "spp": spp, "reuse": reuse, "pick": pick, "cam": cam})
         if not reuse:
-            resident.append(None)
+            n_resident += 1
+    return reqs, pool
+
+
+def serving_record(ctx, rate: float, duration: float, order: str = "arrival", quick_paths: int = 1 << 24,
+                   round_cap: int = 0, alongside: bool = False, replay: bool = True, round_paths: int = 0) -> dict:
+    """Config 4: the request stream served by vt_server (continuous batching)
+    at its arrival times, then (replay) the same requests one at a time in
+    arrival order in the plain form (the per-pixel kernel, one launch per
+    pass: the reference's structure) and as one wavefront launch per request.
+    Time-to-spp = arrival to the image being readable on the host; a replay's
+    timeline is its measured service times queued behind one another from
+    the same arrivals.  Every request's image is compared across the forms."""
+    from voxeltoy_gb300 import Job, Scene, Server, scenes as S
+    from voxeltoy_gb300 import _lib as L
+    reqs, pool = serving_requests(rate, duration)
     settings = S.physical_settings(max_bounces=4, rr_start=-1, seed=0)
-    scenes = []
-    tickets = []
-    large = None
-    if args.alongside:
+    srv = Server(ctx, hbm_budget_bytes=60 << 30, max_active_jobs=64, passes_per_round=4,
+                 order=L.VT_SERVE_LEAST_WORK if order == "least-work" else L.VT_SERVE_ARRIVAL,
+                 quick_paths=quick_paths, round_paths_cap=round_cap, round_paths=round_paths)
+    scenes, scene_of, upload_s = [], [], {}
+    large = big = None
+    if alongside:
         # config 5 served alongside the stream: the voxelized icosphere at
         # 2048^2 x 1024 spp, 8 bounces, submitted when the stream starts
         v, f = S.fbm_displaced_icosphere(level=8)
         big = Scene.voxelize(ctx, np.ascontiguousarray(v, np.float32), np.ascontiguousarray(f, np.uint32),
                              (1024, 1024, 1024), mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
                              palette=[S.lambert(0.7)])
-        scenes.append(big)
         bcfg = S.config1(edge=8, width=2048, height=2048, spp=1024)
         bcfg.settings.max_bounces = 8
+    tickets = []
+    pool_of = []            # the pool entry behind each resident scene index
     t_start = time.perf_counter()
-    if args.alongside:
+    if alongside:
         large = srv.submit(big, None, bcfg.camera, bcfg.settings, 2048, 2048, 1024)
-    for k, (res, spp, reuse, pick, cam) in enumerate(reqs):
-        wait = arrivals[k] - (time.perf_counter() - t_start)
+    for k, r in enumerate(reqs):
+        wait = r["arrival"] - (time.perf_counter() - t_start)
         if wait > 0:
             time.sleep(wait)
-        if reuse:
-            sc = scenes[pick]
+        # the server keeps each volume resident under its key (the pool index);
+        # a reused one is submitted without its voxels
+        if r["reuse"]:
+            si = r["pick"]
+            vox = None
         else:
-            sc = Scene.dense(ctx, pool[pick], [S.lambert(0.7)])
-            scenes.append(sc)
-        t_sub = time.perf_counter() - t_start
-        tickets.append((srv.submit(sc, None, cam, settings, res, res, spp), t_sub - arrivals[k], res * res * spp))
-    lat = []
-    for t, delay, _p in tickets:
+            pool_of.append(r["pick"])
+            si = len(pool_of) - 1
+            vox = pool[r["pick"]]
+        scene_of.append(si)
+        t0 = time.perf_counter()
+        t = srv.submit_dense(si, vox, [S.lambert(0.7)], r["cam"], settings, r["res"], r["res"], r["spp"])
+        t_ret = time.perf_counter()
+        if vox is not None:
+            upload_s[si] = t_ret - t0
+        tickets.append((t, t_ret - t_start - r["arrival"]))
+    lat, digests = [], []
+    for (t, delay), r in zip(tickets, reqs):
         rc = srv.wait(t, 3600.0)
         if rc != 0:
             raise RuntimeError(f"request {t} failed: {rc}")
-        lat.append(delay + srv_latency(srv, t))
+        img, secs = srv.result(t, r["res"], r["res"])
+        lat.append(delay + secs)
+        digests.append(image_digest(img))
     large_ms = None
     if large is not None:
         rc = srv.wait(large, 3600.0)
         if rc != 0:
             raise RuntimeError(f"the large request failed: {rc}")
         large_ms = srv_latency(srv, large) * 1e3
-        tickets.append((large, 0.0, 2048 * 2048 * 1024))
     t_end = time.perf_counter() - t_start
-    lat = np.array(lat)
     stats = srv.stats()
-    paths = sum(p for _t, _d, p in tickets)
     srv.close()
+    # caller-owned copies of the scenes for the one-at-a-time replays
+    scenes = [Scene.dense(ctx, pool[i], [S.lambert(0.7)]) for i in pool_of] if (replay and not alongside) else []
+    paths = sum(r["res"] * r["res"] * r["spp"] for r in reqs) + (2048 * 2048 * 1024 if alongside else 0)
+    lat = np.array(lat)
+    rec = {"requests": len(reqs), "rate_req_s": rate, "duration_s": duration,
+           "offered_mpaths_s": sum(r["res"] * r["res"] * r["spp"] for r in reqs) / duration / 1e6,
+           "served": {"mpaths_s": paths / t_end / 1e6, "makespan_s": t_end,
+                      "time_to_spp_ms": {"p50": float(np.percentile(lat, 50) * 1e3),
+                                         "p99": float(np.percentile(lat, 99) * 1e3), "max": float(lat.max() * 1e3)},
+                      "completed": int(stats.completed), "failed": int(stats.failed), "rounds": int(stats.rounds),
+                      "scene_uploads": int(stats.scene_uploads), "scene_hits": int(stats.scene_hits),
+                      "scene_evictions": int(stats.scene_evictions)},
+           "settings": {"order": order, "quick_paths": quick_paths, "round_cap": round_cap,
+                        "round_paths": round_paths or (1 << 26),
+                        "hbm_budget_bytes": 60 << 30, "passes_per_round": 4, "max_active_jobs": 64,
+                        "residency": "volumes kept resident by the server under their pool index "
+                                     "(vt_server_submit_dense), uploaded at their first request"},
+           "h2d_bytes": int(sum(pool[r["pick"]].nbytes for r in reqs if not r["reuse"]))}
+    if alongside:
+        rec["alongside"] = {"request": "voxelized icosphere (1.3M triangles, 1024^3) at 2048^2 x 1024 spp, 8 bounces, "
+                                       "submitted with the first request of the stream", "time_to_spp_ms": large_ms}
+    if replay and not alongside:
+        same = True
+        for name, kernel in (("plain", 1), ("per_request_wavefront", 2)):
+            ctx.set_kernel(kernel)
+            t_free, lats, busy = 0.0, [], 0.0
+            first_use = set()
+            for r, si, dg in zip(reqs, scene_of, digests):
+                t0 = time.perf_counter()
+                job = Job(ctx, scenes[si], None, r["cam"], settings, r["res"], r["res"])
+                job.render(r["spp"])
+                img = job.readback()
+                dt = time.perf_counter() - t0
+                job.close()
+                if si not in first_use:     # the scene's upload, measured when it was served
+                    first_use.add(si)
+                    dt += upload_s.get(si, 0.0)
+                start = max(r["arrival"], t_free)
+                t_free = start + dt
+                busy += dt
+                lats.append(t_free - r["arrival"])
+                same = same and image_digest(img) == dg
+            lats = np.array(lats)
+            rec[name] = {"mpaths_s": paths / t_free / 1e6, "makespan_s": t_free, "busy_s": busy,
+                         "time_to_spp_ms": {"p50": float(np.percentile(lats, 50) * 1e3),
+                                            "p99": float(np.percentile(lats, 99) * 1e3),
+                                            "max": float(lats.max() * 1e3)}}
+        ctx.set_kernel(2)
+        rec["served_vs_plain"] = rec["plain"]["makespan_s"] / rec["served"]["makespan_s"]
+        rec["served_vs_per_request_wavefront"] = rec["per_request_wavefront"]["makespan_s"] / rec["served"]["makespan_s"]
+        rec["identical_images"] = bool(same)
     for sc in scenes:
         sc.close()
+    if big is not None:
+        big.close()
+    return rec
+
+
+def run_serving(args, world, rank, local):
+    """Poisson request stream through vt_server (see serving_record)."""
+    from voxeltoy_gb300 import Context
+    ctx = Context(local)
+    r = serving_record(ctx, args.rate, args.duration, order=args.order, quick_paths=args.quick_paths,
+                       round_cap=args.round_cap, alongside=args.alongside, replay=args.replay,
+                       round_paths=args.round_paths)
     ctx.close()
-    return {"metric": METRIC, "value": paths / t_end / 1e6, "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
-            "ms_per_step": t_end * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+    s = r["served"]
+    return {"metric": METRIC, "value": s["mpaths_s"], "unit": UNIT, "n_gpus": world, "steps": 1, "warmup": 0,
+            "ms_per_step": s["makespan_s"] * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic (seeded request stream)",
-            "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s ({n} requests), "
-                                   f"sphere-union scenes edge 64-512 (pool of {pool_n}), reuse 0.5, resolution "
+            "config": {"workload": f"serving: Poisson {args.rate:g} req/s for {args.duration:g} s ({r['requests']} "
+                                   f"requests), sphere-union scenes edge 64-512 (pool of 16), reuse 0.5, resolution "
                                    f"256^2-1024^2, 16-1024 spp log-uniform, 4 bounces, 60 GB admission budget, "
                                    f"admission order {args.order}, quick paths {args.quick_paths}, "
                                    f"round cap {args.round_cap}",
-                       "requests": n, "offered_mpaths_s": paths / args.duration / 1e6},
-            "time_to_spp_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
-                               "max": float(lat.max() * 1e3)},
-            "server": {"completed": int(stats.completed), "failed": int(stats.failed)},
-            "alongside": None if large_ms is None else
-            {"request": "voxelized icosphere (1.3M triangles, 1024^3) at 2048^2 x 1024 spp, 8 bounces, "
-                        "submitted with the first request of the stream", "time_to_spp_ms": large_ms},
-            "e2e": {"value": paths / t_end / 1e6, "unit": UNIT,
-                    "h2d_bytes_per_step": int(sum(pool[r[3]].nbytes for r in reqs if not r[2])),
-                    "d2h_bytes_per_step": 0}}
+                       "requests": r["requests"], "offered_mpaths_s": r["offered_mpaths_s"]},
+            "e2e": {"value": s["mpaths_s"], "unit": UNIT, "h2d_bytes_per_step": r["h2d_bytes"],
+                    "d2h_bytes_per_step": 0}, **r}
 
 
 def srv_latency(srv, ticket) -> float:
@@ -478,19 +593,24 @@ def srv_latency(srv, ticket) -> float:
     return secs.value
 
 
-def run_voxelize(args, world, rank, local):
-    """1.3M-triangle fBm-displaced icosphere, conservative voxelization into
-    1024^3, then a 2048^2 render with config-1 materials and sky, 8 bounces."""
+def config5_record(ctx, spp: int = 1024, steps: int = 3, check: bool = False, rmse_rows: int = 2) -> dict:
+    """Config 5: the fBm-displaced icosphere (1,310,720 triangles) voxelized
+    conservatively into 1024^3 (timed end to end, host mesh to resident
+    scene), then rendered at 2048^2 x spp with config-1 materials and sky,
+    8 bounces (CUDA events); relative RMSE of `rmse_rows` centre rows against
+    the FP64 oracle, and optionally the occupancy against the oracle's."""
     import torch
-    from voxeltoy_gb300 import Context, Job, Scene, scenes as S
+    from voxeltoy_gb300 import Job, Scene, scenes as S
     from voxeltoy_gb300 import _lib as L
     v, f = S.fbm_displaced_icosphere(level=8)
     v = np.ascontiguousarray(v, np.float32)
     f = np.ascontiguousarray(f, np.uint32)
     res = (1024, 1024, 1024)
-    ctx = Context(local)
     vox_ms = []
-    for k in range(args.steps + 1):
+    sc = None
+    for k in range(steps + 1):
+        if sc is not None:
+            sc.close()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sc = Scene.voxelize(ctx, v, f, res, mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
@@ -499,19 +619,10 @@ def run_voxelize(args, world, rank, local):
         torch.cuda.synchronize()
         if k:
             vox_ms.append((time.perf_counter() - t0) * 1e3)
-        if k < args.steps:
-            sc.close()
-    check = None
-    if args.check:
-        from oracle import binding as orc
-        want = orc.voxelize(v, f, res, L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE)
-        got = sc.voxels()
-        check = {"bit_exact": bool(np.array_equal(want > 0, got > 0)), "occupied": int(np.count_nonzero(got))}
-    spp = args.spp if args.spp != 256 else 1024
     cfg = S.config1(edge=8, width=2048, height=2048, spp=spp)
     cfg.settings.max_bounces = 8
     job = Job(ctx, sc, None, cfg.camera, cfg.settings, 2048, 2048)
-    timer = EventTimer(ctx, local)
+    timer = EventTimer(ctx, ctx_device(ctx))
     job.render(4)
     job.reset()
     torch.cuda.synchronize()
@@ -519,18 +630,53 @@ def run_voxelize(args, world, rank, local):
         job.render(spp)
     paths = 2048 * 2048 * spp
     img = job.readback()
-    job.close(); sc.close(); ctx.close()
-    return {"metric": METRIC, "value": paths / (timer.ms * 1e-3) / 1e6, "unit": UNIT, "n_gpus": world, "steps": 1,
-            "warmup": 1, "ms_per_step": timer.ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded icosphere mesh)",
-            "config": {"workload": f"voxelize: fBm-displaced icosphere level 8 ({len(f)} triangles) -> 1024^3 "
+    job.close()
+    cfg.voxels = sc.voxels()
+    cfg.palette = [S.lambert(0.7)]
+    sc.close()
+    rec = {"triangles": int(len(f)), "grid": list(res), "spp": spp,
+           "voxelize_ms": {"median": float(np.median(vox_ms)), "min": float(min(vox_ms))},
+           "voxelize_mtris_s": len(f) / (np.median(vox_ms) * 1e-3) / 1e6,
+           "render_ms": timer.ms, "render_mpaths_s": paths / (timer.ms * 1e-3) / 1e6,
+           "image_finite": bool(np.isfinite(img).all())}
+    if rmse_rows > 0:
+        r0 = (2048 - rmse_rows) // 2
+        rec["rmse_vs_fp64"] = rmse_vs_fp64(cfg, img, spp, (r0, r0 + rmse_rows))
+    if check:
+        from oracle import binding as orc
+        want = orc.voxelize(v, f, res, L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE)
+        rec["occupancy_check"] = {"bit_exact": bool(np.array_equal(want, cfg.voxels)),
+                                  "occupied": int(np.count_nonzero(cfg.voxels))}
+    return rec
+
+
+def config1_rmse(ctx) -> dict:
+    """Config 1 at its full size (256^2 x 16 spp) against the FP64 oracle."""
+    from voxeltoy_gb300 import Job, Scene, scenes as S
+    cfg = S.config1()
+    sc = Scene.dense(ctx, cfg.voxels, cfg.palette)
+    job = Job(ctx, sc, None, cfg.camera, cfg.settings, cfg.width, cfg.height)
+    job.render(cfg.spp)
+    img = job.readback()
+    job.close(); sc.close()
+    return rmse_vs_fp64(cfg, img, cfg.spp, (0, cfg.height))
+
+
+def run_voxelize(args, world, rank, local):
+    """1.3M-triangle fBm-displaced icosphere, conservative voxelization into
+    1024^3, then a 2048^2 render with config-1 materials and sky, 8 bounces."""
+    from voxeltoy_gb300 import Context
+    ctx = Context(local)
+    spp = args.spp if args.spp != 256 else 1024
+    r = config5_record(ctx, spp=spp, steps=args.steps, check=args.check, rmse_rows=2 if args.check else 0)
+    ctx.close()
+    return {"metric": METRIC, "value": r["render_mpaths_s"], "unit": UNIT, "n_gpus": world, "steps": 1,
+            "warmup": 1, "ms_per_step": r["render_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded icosphere mesh)",
+            "config": {"workload": f"voxelize: fBm-displaced icosphere level 8 ({r['triangles']} triangles) -> 1024^3 "
                                    f"conservative, then 2048^2 pinhole, Lambert 0.7, white sky, 8 bounces, {spp} spp",
-                       "triangles": int(len(f))},
-            "voxelize_ms": {"median": float(np.median(vox_ms)), "min": float(min(vox_ms))},
-            "voxelize_mtris_s": len(f) / (np.median(vox_ms) * 1e-3) / 1e6,
-            "occupancy_check": check, "image_finite": bool(np.isfinite(img).all()),
-            "e2e": {"value": paths / (timer.ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(v.nbytes + f.nbytes),
-                    "d2h_bytes_per_step": int(img.nbytes)}}
+                       "triangles": r["triangles"]},
+            **r}
 
 
 def main():
@@ -562,6 +708,8 @@ def main():
                     help="serving: admission order of queued requests")
     ap.add_argument("--round-cap", type=int, default=0,
                     help="serving: at most this many paths of one request per round (0 = off)")
+    ap.add_argument("--round-paths", type=int, default=0,
+                    help="serving: paths traced per round (0 = the server's default, 2^26)")
     ap.add_argument("--alongside", action="store_true",
                     help="serving: also serve the voxelized 1.3M-triangle icosphere at 2048^2 x 1024 spp")
     ap.add_argument("--quick-paths", type=int, default=1 << 24,
@@ -569,6 +717,13 @@ def main():
     ap.add_argument("--check", action="store_true", help="voxelize: compare the occupancy with the oracle")
     ap.add_argument("--profile", action="store_true",
                     help="only warm-up and timed renders of the resident frame (for ncu captures)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline line only: no RMSE check against the FP64 oracle and no batching, serving and "
+                         "config-5 records")
+    ap.add_argument("--extras-rate", type=float, default=16.0, help="request rate of the serving record")
+    ap.add_argument("--extras-duration", type=float, default=5.0, help="seconds of arrivals of the serving record")
+    ap.add_argument("--no-replay", dest="replay", action="store_false",
+                    help="serving: skip the one-at-a-time replays of the stream")
     args = ap.parse_args()
     small = args.workload == "config1"
     args.edge = args.edge or (64 if small else 256)
@@ -578,6 +733,7 @@ def main():
     if args.impl == "gb300" and not args.profile:
         args.warmup = max(args.warmup, 3)
     world, rank, local = dist_setup()
+    extras = not args.no_extras and world == 1 and args.workload in ("config2", "config1")
     if args.impl == "reference":
         return run_reference(args, world, rank)
 
@@ -663,7 +819,8 @@ def main():
     value = world * paths / (ms * 1e-3) / 1e6
     launch_ms = float(np.mean(times))
     achieved = alg_bytes / (launch_ms * 1e-3) / 1e9
-    l2_gbs = l2_copy_gbs(local)
+    l2 = l2_read_gbs(ctx)
+    frame_img = job.readback() if (rank == 0 and extras) else None   # the last timed frame, for the RMSE check
 
     # end to end through the C ABI from pinned host memory
     vox_h = torch.from_numpy(np.ascontiguousarray(cfg.voxels)).pin_memory().numpy()
@@ -721,21 +878,48 @@ def main():
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "bytes_model": "1 B/DDA cell + 16 B/palette record + 8 B/env texel eval + 4 B/CDF probe + "
                                     "4 B/emissive read + 64 B/path framebuffer",
-                     "l2": {"achieved": achieved, "peak": l2_gbs, "unit": "GB/s", "frac": achieved / l2_gbs,
-                            "peak_source": "L2-resident copy (8-32 MiB buffers) measured in this run (torch copy_)"}},
+                     "l2": {"achieved": achieved, "peak": l2["gbs"], "unit": "GB/s", "frac": achieved / l2["gbs"],
+                            "peak_source": l2["source"]}},
         "rates": {"gsegments_per_s": world * float(cnt[6]) / (ms * 1e-3) / 1e9,
                   "gdda_cells_per_s": world * float(cnt[1]) / (ms * 1e-3) / 1e9},
         "counters_per_frame": {"paths": int(cnt[0]), "dda_cells": int(cnt[1]), "palette": int(cnt[2]),
                                "env_evals": int(cnt[3]), "cdf_probes": int(cnt[4]), "emissive_reads": int(cnt[5]),
                                "segments": int(cnt[6]), "empty_brick_cells": int(cnt[7])},
-        "time_to_spp_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99))},
+        "frame_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99)),
+                     "note": "device time of each timed frame (one resident job from reset to its spp target)"},
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "tuning": tuning,
     }
-    for o in (job, env, scene, ctx):
+    emissive = scene.emissive()
+    for o in (job, env, scene):
         if o is not None:
             o.close()
+    if rank == 0 and extras:
+        # checker and side records, outside every timed region above
+        t_x = time.perf_counter()
+        # the whole timed frame against the FP64 oracle at the same sample count
+        rmse = {args.workload: rmse_vs_fp64(cfg, frame_img, cfg.spp, (0, cfg.height), emissive=emissive)}
+        del frame_img
+        if args.workload == "config2":
+            rmse["config1"] = config1_rmse(ctx)
+            b = batching_record(ctx, args.scenes, 3, e2e=False)
+            rmse["config3"] = b.pop("rmse_vs_fp64")
+            c5 = config5_record(ctx, spp=1024, steps=2, rmse_rows=2)
+            rmse["config5"] = c5.pop("rmse_vs_fp64")
+            srv = serving_record(ctx, args.extras_rate, args.extras_duration)
+            line["batching"] = b
+            line["serving"] = srv
+            line["config5"] = c5
+            line["batched_vs_plain"] = b["batched_vs_plain"]
+            line["served_vs_plain"] = srv["served_vs_plain"]
+            line["time_to_spp_ms"] = dict(srv["served"]["time_to_spp_ms"],
+                                          stream=f"Poisson {args.extras_rate:g} req/s for {args.extras_duration:g} s")
+        line["rmse_vs_fp64"] = rmse
+        recs = [r for v in rmse.values() for r in (v if isinstance(v, list) else [v])]
+        line["rmse_max"] = max(r["rel_rmse"] for r in recs)
+        line["extras_s"] = round(time.perf_counter() - t_x, 1)
+    ctx.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -107,11 +107,16 @@ typedef struct vt_material {
  * (.hdr, flat or run-length scanlines) into RGB floats, rows top first as
  * vt_env_create_image takes them; with rgb NULL it returns only the size.
  * vt_image_encode_pfm writes a colour PFM from RGB or RGBA floats whose rows
- * are bottom first (vt_job_readback's order, which PFM also uses); with out
- * NULL it returns only the size.  Neither needs a GPU. */
+ * are bottom first (vt_job_readback's order, which PFM also uses);
+ * vt_image_encode_hdr writes the same pixels as a flat Radiance RGBE file
+ * (rows top first, as "-Y h +X w" orders them; negative and NaN channels
+ * become 0).  With out NULL they return only the size.  None needs a GPU. */
 VT_API int vt_image_decode(const uint8_t* data, size_t size, float* rgb,
                            size_t rgb_bytes, int32_t* width, int32_t* height);
 VT_API int vt_image_encode_pfm(const float* pixels, int32_t width, int32_t height,
+                               int32_t channels, uint8_t* out, size_t out_bytes,
+                               size_t* written);
+VT_API int vt_image_encode_hdr(const float* pixels, int32_t width, int32_t height,
                                int32_t channels, uint8_t* out, size_t out_bytes,
                                size_t* written);
 
@@ -133,6 +138,17 @@ VT_API int vt_scene_create(vt_context* ctx, int32_t rx, int32_t ry, int32_t rz,
                            const uint8_t* voxels, const vt_material* palette,
                            int32_t n_palette, const int32_t* emissive_indices,
                            int64_t n_emissive, uint32_t flags, vt_scene** out);
+
+/* Shape of the scene's occupancy bricks, the 64-bit words the DDA tests
+ * (one word per block of 2^sx x 2^sy x 2^sz voxels, each of sx, sy, sz in
+ * [1, 4] and sx + sy + sz = 6; scenes are created with 4x4x4, i.e. 2, 2, 2).  Changing it rebuilds the
+ * bricks from the volume on the device; jobs on the scene pick the new
+ * shape up before their next pass.  Images are identical for every shape:
+ * the shape only changes how often the DDA loads a new word and how the
+ * words share cache lines, which the autotuner measures.  No counterpart in
+ * the reference, which tests a 3D integer texture per step (dda.h:41-45). */
+VT_API int vt_scene_set_brick_shape(vt_scene* scene, int32_t sx, int32_t sy, int32_t sz);
+VT_API int vt_scene_get_brick_shape(const vt_scene* scene, int32_t* shape);
 
 /* Upload a volume in the reference's own layout: one int32 material-table
  * offset per voxel (-1 = empty) and a flat float material table of
@@ -253,8 +269,23 @@ VT_API int vt_scene_destroy(vt_scene* scene);
  * (src/renderer/renderer.cpp:947-1055, src/renderer/image.cpp:68-389). */
 VT_API int vt_env_create_image(vt_context* ctx, const float* rgb, int32_t width,
                                int32_t height, vt_env** out);
-/* Copy back the CDFs: cdf_u (width+1)*height floats, cdf_v height+1 floats
- * and the radiance integral (image.cpp:349-389).  Any output may be NULL. */
+/* vt_env_create_image with options.  VT_ENV_CDF_REFERENCE_SIZE builds the
+ * CDFs and the integral from the image shrunk to at most 512 texels on its
+ * long axis, as calculateCDF does (image.cpp:14, 308-320: the size from its
+ * float arithmetic), while radiance is still looked up in the full-size
+ * texels; samples then follow the shrunk image's distribution and their pdf
+ * is the full-size luminance over the shrunk image's integral, as in the
+ * reference.  The shrink is an area-weighted box average: the reference's
+ * OpenImageIO resize filter is not restated (its weights are unpinned). */
+enum { VT_ENV_CDF_REFERENCE_SIZE = 1u << 0 };
+VT_API int vt_env_create_image_ex(vt_context* ctx, const float* rgb, int32_t width,
+                                  int32_t height, uint32_t flags, vt_env** out);
+/* size[0..3] = image width, height, and the width and height of the image
+ * the CDFs describe (the same, or the shrunk size). */
+VT_API int vt_env_get_info(const vt_env* env, int32_t* size);
+/* Copy back the CDFs: cdf_u (cdf_width+1)*cdf_height floats, cdf_v
+ * cdf_height+1 floats and the radiance integral (image.cpp:349-389).  Any
+ * output may be NULL. */
 VT_API int vt_env_read_cdf(const vt_env* env, float* cdf_u, size_t cdf_u_bytes,
                            float* cdf_v, size_t cdf_v_bytes, float* integral);
 VT_API int vt_env_destroy(vt_env* env);
@@ -409,6 +440,20 @@ enum {
  * memory.  Replaces the glGetTexImage of Renderer::saveImage
  * (renderer.cpp:1108-1140). */
 VT_API int vt_job_readback(vt_job* job, float* rgba, size_t bytes, uint32_t flags);
+
+/* Accumulation state of a job: the Kahan-compensated running sums of its
+ * samples (sum) and their compensation terms (comp), width*height*4 floats
+ * each, and the number of samples they hold.  No counterpart in the
+ * reference, whose resetRender (renderer.cpp:941-945) discards the
+ * accumulation: a job restored from a snapshot into a job of the same
+ * scene, camera, settings and size continues with the samples that come
+ * next (the random streams are keyed by pixel and sample index), so its
+ * image equals that of a job that was never interrupted, bit for bit.
+ * Used to evict a long-running frame from device memory and resume it. */
+VT_API int vt_job_snapshot(const vt_job* job, float* sum, float* comp, size_t bytes_each,
+                           int32_t* samples);
+VT_API int vt_job_restore(vt_job* job, const float* sum, const float* comp, size_t bytes_each,
+                          int32_t samples);
 /* Device pointer of the float4 accumulation sums and the sample count, for
  * zero-copy consumers (valid until the next render/reset/destroy). */
 VT_API int vt_job_device_buffer(vt_job* job, void** sums, int32_t* samples);
@@ -483,9 +528,12 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
  * frame times, such as an interactive viewer, because cudaMalloc and
  * cudaFree can synchronise the whole device.  Instead, this call takes all
  * of its working memory from one array compiled into the library
- * (VT_FIXED_SCRATCH_BYTES, about 46 MB, not counted against any budget),
- * reserved on a device when the CUDA runtime loads the library's code for
- * that device.
+ * (VT_FIXED_SCRATCH_BYTES, about 44 MB, not counted against any budget).
+ * The CUDA runtime reserves it on a device when it loads the code that
+ * holds it, which vt_create triggers for its device, so the reservation
+ * (and a failure to make it) happens when the context is created, not in
+ * the caller's frame loop; the array stays reserved until the process
+ * exits.
  *
  * Limits, each rejected with VT_EINVAL and a message naming the limit:
  *   n_jobs        <= VT_FIXED_MAX_JOBS
@@ -494,9 +542,13 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
  *                    most that many samples per launch and splits the rest
  *                    into further launches.
  *
- * The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) once, with that device current; make that first
- * call before any stream capture begins on the device.  Each launch clears
+ * vt_create looks up the array's device address (cudaGetSymbolAddress)
+ * with its device current; if that failed, the first call on the device
+ * tries again, so make that first call before any stream capture begins on
+ * the device.  A call that fails after queuing work waits for that work
+ * before it returns; the jobs of a failed call may hold part of their
+ * passes, so reset them (vt_job_reset) before rendering them again.  Each
+ * launch clears
  * the words that must start at zero (queue and hit-list counters, the path
  * stream's length, the item counter); everything else in the array is
  * written before it is read.  There is one array per device, shared by
@@ -507,7 +559,7 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
 #define VT_FIXED_MAX_JOBS 16
 #define VT_FIXED_MAX_PATH_SLOTS 65536
 #define VT_FIXED_MAX_SAMPLES (1 << 20)
-#define VT_FIXED_SCRATCH_BYTES 45625088
+#define VT_FIXED_SCRATCH_BYTES 43528960
 VT_API int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs,
                                  int32_t n_jobs, int32_t passes,
                                  int32_t path_slots, int32_t* results);
@@ -530,6 +582,13 @@ typedef struct vt_server_opts {
   uint64_t round_paths_cap;    /* at most this many paths of one request per round
                                   (at least one pass), so that a large request
                                   does not lengthen every round; 0 = off          */
+  uint64_t round_paths;        /* paths traced per round: every active request
+                                  first gets passes_per_round passes (or what it
+                                  has left), then the rest of this budget goes to
+                                  the requests with the fewest paths left first,
+                                  as many passes as fit; 0 = 2^26.  Rounds of
+                                  many paths keep the GPU's path slots full;
+                                  a request that arrives waits at most one round */
 } vt_server_opts;
 
 enum { VT_SERVE_ARRIVAL = 0, VT_SERVE_LEAST_WORK = 1 };
@@ -543,19 +602,46 @@ typedef struct vt_server_stats {
   uint64_t submitted, completed, cancelled, failed;
   uint64_t paths_traced;
   uint64_t rounds;
-  uint64_t bytes_in_use;
+  uint64_t bytes_in_use;       /* job buffers and resident scenes, against the budget */
   int32_t active, queued;
+  uint64_t scene_uploads;      /* scenes uploaded by vt_server_submit_dense           */
+  uint64_t scene_hits;         /* submissions that found their scene resident         */
+  uint64_t scene_evictions;    /* resident scenes evicted to make room                */
+  int32_t scenes_resident;
+  int32_t pad;
 } vt_server_stats;
 
 /* Start a request loop thread that admits jobs as slots and budget free up
  * and traces all admitted jobs together each round. */
 VT_API int vt_server_create(vt_context* ctx, const vt_server_opts* opts,
                             vt_server** out);
-/* Submit a render request; the scene and env must outlive it. */
+/* Submit a render request on a scene the caller created and owns; the
+ * scene and env must outlive the request (destroying either while the
+ * request is queued or running is undefined).  Its memory is the caller's
+ * and is not counted against the server's budget. */
 VT_API int vt_server_submit(vt_server* srv, const vt_scene* scene, const vt_env* env,
                             const vt_camera* cam, const vt_render_settings* settings,
                             int32_t width, int32_t height, int32_t spp_target,
                             uint64_t* ticket);
+/* Submit a render request on a volume the server keeps resident, named by
+ * the caller's scene_key (for example a content hash).  If the key is not
+ * resident, the volume (voxels: rx*ry*rz palette entries + 1, 0 empty, x
+ * fastest; palette; flags as vt_scene_create) is uploaded during this call,
+ * after evicting unused resident scenes, least recently used first, until
+ * it fits the budget (VT_EBUDGET if it cannot); if the key is resident the
+ * volume arguments may be NULL / 0 and are not read.  Host pointers are
+ * borrowed for the duration of the call.  A resident scene stays on the
+ * device while requests use it and afterwards, until evicted (also to make
+ * room for a request's job buffers) or the server is destroyed.  The env
+ * stays the caller's and must outlive the request.  No counterpart in the
+ * reference, which keeps exactly one volume (createVoxelDataTexture,
+ * renderer.cpp:833-940). */
+VT_API int vt_server_submit_dense(vt_server* srv, uint64_t scene_key, int32_t rx, int32_t ry,
+                                  int32_t rz, const uint8_t* voxels, const vt_material* palette,
+                                  int32_t n_palette, uint32_t scene_flags, const vt_env* env,
+                                  const vt_camera* cam, const vt_render_settings* settings,
+                                  int32_t width, int32_t height, int32_t spp_target,
+                                  uint64_t* ticket);
 VT_API int vt_server_poll(vt_server* srv, uint64_t ticket, int32_t* state,
                           int32_t* samples_done);
 /* Wait until the request is done, failed or cancelled (timeout in seconds,

@@ -80,6 +80,40 @@ VT_API int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int32_t
 VT_API int vt_diag_set_tuning(vt_context* ctx, int64_t path_slots, int32_t trace_blocks_per_sm,
                               int32_t trace_steps, int64_t max_items);
 
+/* The scene's occupancy bit-bricks: one 64-bit word per brick of
+ * 2^sx x 2^sy x 2^sz voxels (vt_scene_get_brick_shape; bit
+ * (x & (2^sx-1)) | (y & (2^sy-1)) << sx | (z & (2^sz-1)) << (sx+sy), set =
+ * occupied or outside the volume), on the brick grid padded by one brick on
+ * every side, x fastest: (bx+2)*(by+2)*(bz+2) words, bx = ceil(rx/2^sx) ...
+ * *n_words receives that count; out (nullable) receives the words. */
+VT_API int vt_diag_scene_bricks(const vt_scene* scene, uint64_t* out, size_t bytes, int64_t* n_words);
+
+/* Bounds-checked build (libvoxeltoy_checked.so, compiled with VT_CHECKED):
+ * every data-dependent gather of the path tracer checks its index, and a
+ * failed check ORs a bit into a device word and reads a neutral value
+ * instead, without trapping: 1 brick word, 2 voxel, 4 palette entry,
+ * 8 emissive-list entry, 16 environment texel, 32 CDF entry, 64 sample-
+ * buffer item, 128 noise texel.  *word receives the bits set since the
+ * last call (the word is then cleared; the context's stream is synchronised
+ * first); *enabled is 1 in the checked build and 0 (word 0) otherwise. */
+VT_API int vt_diag_check_word(vt_context* ctx, uint32_t* word, int32_t* enabled);
+
+/* L2 read bandwidth of this GPU in GB/s: one launch of `reps` sweeps over a
+ * device buffer of `bytes` bytes (multiple of 16, 1 MiB to 1 GiB; choose it
+ * well below the L2 size) with loads that bypass L1, after one warm sweep;
+ * timed with CUDA events on the context's stream.  The buffer is allocated
+ * and freed by the call. */
+VT_API int vt_diag_l2_read_bandwidth(vt_context* ctx, int64_t bytes, int32_t reps, double* gbs);
+
+/* Tuning of the wavefront form's DDA kernel (values <= 0, and refill_min
+ * < 0, keep their setting): queue_chunk queue records a warp takes with one
+ * atomic (a multiple of 32 in [32, 1024], default 128); refill_min: a warp
+ * stops stepping and starts its lanes' next segments as soon as fewer than
+ * refill_min of its lanes still step (checked every fourth step; 0, the
+ * default, refills only every trace_steps steps).  Results are identical
+ * for every setting. */
+VT_API int vt_diag_set_trace_tuning(vt_context* ctx, int32_t queue_chunk, int32_t refill_min);
+
 /* Number of rendering kernels (plain, wavefront shade/trace/accumulate) the
  * context has launched so far. */
 VT_API int vt_diag_launch_count(const vt_context* ctx, uint64_t* launches);

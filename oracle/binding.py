@@ -42,16 +42,19 @@ class OrcScene(C.Structure):
 
 class OrcEnv(C.Structure):
     _fields_ = [("w", C.c_int32), ("h", C.c_int32), ("texels", C.c_void_p), ("cdf_u", C.c_void_p),
-                ("cdf_v", C.c_void_p), ("integral", C.c_float)]
+                ("cdf_v", C.c_void_p), ("integral", C.c_float), ("cdf_w", C.c_int32), ("cdf_h", C.c_int32)]
 
 
 _LIB = None
 
 
 def lib() -> C.CDLL:
+    """The oracle library (VT_ORACLE_SANITIZED=1 selects the AddressSanitizer /
+    UndefinedBehaviorSanitizer build, which needs libasan preloaded)."""
     global _LIB
     if _LIB is None:
-        path = _build.build()
+        import os
+        path = _build.build(sanitize=os.environ.get("VT_ORACLE_SANITIZED") == "1")
         L = C.CDLL(str(path))
         P = C.c_void_p
         sig = {
@@ -69,6 +72,9 @@ def lib() -> C.CDLL:
             "orc_pick": ([C.POINTER(OrcCamera), C.POINTER(OrcSettings), C.POINTER(OrcScene), P, C.c_int32, C.c_int32,
                           C.c_float, C.c_float, C.POINTER(C.c_float), P], C.c_int),
             "orc_build_env": ([P, C.c_int32, C.c_int32, C.c_int32, P, P, P, C.POINTER(C.c_float)], C.c_int),
+            "orc_build_env_ex": ([P, C.c_int32, C.c_int32, C.c_int32, C.c_uint32, P, P, P, C.POINTER(C.c_float), P],
+                                 C.c_int),
+            "orc_cdf_size": ([C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32)], None),
             "orc_cdf_from_function": ([P, C.c_int32, C.c_int32, C.c_int32, P, P, C.POINTER(C.c_float)], C.c_int),
             "orc_cdf_reference_float": ([P, C.c_int32, C.c_int32, P, P], C.c_int),
             "orc_binary_search": ([P, C.c_int32, C.c_float], C.c_int32),
@@ -185,26 +191,41 @@ class Scene:
                           C.c_void_p(self.em.ctypes.data), n_em)
 
 
+def cdf_size(w: int, h: int) -> tuple:
+    """The reference's CDF image size for a w x h environment (image.cpp:314-317)."""
+    cw, ch = C.c_int32(), C.c_int32()
+    lib().orc_cdf_size(w, h, C.byref(cw), C.byref(ch))
+    return cw.value, ch.value
+
+
 class Env:
+    """flags bit 0 (reference_size): CDFs and integral from the image shrunk to
+    at most 512 texels on its long axis, texels full size."""
+
     def __init__(self, rgb: np.ndarray | None = None, texels=None, cdf_u=None, cdf_v=None, integral=None,
-                 chunk: int = 32):
+                 chunk: int = 32, flags: int = 0):
         if rgb is None:
-            self.e = OrcEnv(0, 0, None, None, None, 0.0)
+            self.e = OrcEnv(0, 0, None, None, None, 0.0, 0, 0)
             return
         rgb = np.ascontiguousarray(rgb, dtype=np.float32)
         h, w = rgb.shape[:2]
         if texels is None:
+            cw, ch = cdf_size(w, h) if flags & 1 else (w, h)
             texels = np.empty((h, w, 4), np.uint16)
-            cdf_u = np.empty((h, w + 1), np.float32)
-            cdf_v = np.empty(h + 1, np.float32)
+            cdf_u = np.empty((ch, cw + 1), np.float32)
+            cdf_v = np.empty(ch + 1, np.float32)
             iv = C.c_float()
-            lib().orc_build_env(_p(rgb), w, h, chunk, _p(texels), _p(cdf_u), _p(cdf_v), C.byref(iv))
+            size = np.zeros(2, np.int32)
+            lib().orc_build_env_ex(_p(rgb), w, h, chunk, flags, _p(texels), _p(cdf_u), _p(cdf_v), C.byref(iv),
+                                   _p(size))
+            assert tuple(size) == (cw, ch)
             integral = iv.value
         self.texels = np.ascontiguousarray(texels, dtype=np.uint16)
         self.cdf_u = np.ascontiguousarray(cdf_u, dtype=np.float32)
         self.cdf_v = np.ascontiguousarray(cdf_v, dtype=np.float32)
         self.integral = float(integral)
-        self.e = OrcEnv(w, h, _p(self.texels), _p(self.cdf_u), _p(self.cdf_v), self.integral)
+        self.e = OrcEnv(w, h, _p(self.texels), _p(self.cdf_u), _p(self.cdf_v), self.integral,
+                        self.cdf_u.shape[1] - 1, self.cdf_u.shape[0])
 
 
 def noise_table() -> np.ndarray:

@@ -621,7 +621,7 @@ struct Tracer {
   // sampleEnvironmentRadiance (lights.h:36-55) / sampleEnvironmentTexture (envMapSample.h:23-65)
   vec3 sample_env(const Basis& b, R u0, R u1, vec3* dir, R* pdf, Counters& C) const {
     if (env && env->texels) {
-      const int su = env->w + 1, sv = env->h + 1;
+      const int su = (env->cdf_w ? env->cdf_w : env->w) + 1, sv = (env->cdf_h ? env->cdf_h : env->h) + 1;
       const int row = search(env->cdf_v, sv - 1, u1, C);
       const float* cu = env->cdf_u + (size_t)row * su;
       const int col = search(cu, su - 1, u0, C);
@@ -1268,18 +1268,57 @@ int orc_pick(const orc_camera* cam, const orc_settings* s, const orc_scene* scen
   return 0;
 }
 
-int orc_build_env(const float* rgb, int32_t w, int32_t h, int32_t chunk, uint16_t* texels, float* cdf_u,
-                  float* cdf_v, float* integral) {
+void orc_cdf_size(int32_t w, int32_t h, int32_t* cw, int32_t* ch) {
+  const unsigned m = (unsigned)std::max(w, h);
+  if (m <= 512u) { *cw = w; *ch = h; return; }
+  // (unsigned)((float)imageWidth / std::max(imageWidth, imageHeight) * MAX_CDF_SIZE)
+  *cw = (int32_t)(unsigned)((float)(unsigned)w / (float)m * 512.0f);
+  *ch = (int32_t)(unsigned)((float)(unsigned)h / (float)m * 512.0f);
+}
+
+int orc_build_env_ex(const float* rgb, int32_t w, int32_t h, int32_t chunk, uint32_t flags, uint16_t* texels,
+                     float* cdf_u, float* cdf_v, float* integral, int32_t* cdf_size) {
   const size_t n = (size_t)w * h;
   std::vector<float> lum(n), tmp(n), func(n);
+  std::vector<uint16_t> half(3 * n);
   for (size_t i = 0; i < n; ++i) {
     // texels are stored as IEEE halves, clamped to the finite half range
     const uint16_t r = vtb::f2h(vtb::clamp_half(rgb[3 * i])), g = vtb::f2h(vtb::clamp_half(rgb[3 * i + 1])),
                    b = vtb::f2h(vtb::clamp_half(rgb[3 * i + 2]));
     if (texels) { texels[4 * i] = r; texels[4 * i + 1] = g; texels[4 * i + 2] = b; texels[4 * i + 3] = 0x3c00; }
+    half[3 * i] = r; half[3 * i + 1] = g; half[3 * i + 2] = b;
     // channel_sum with Rec.709 weights (image.cpp:326-335)
     lum[i] = (vtb::h2f(r) * 0.2126f + vtb::h2f(g) * 0.7152f) + vtb::h2f(b) * 0.0722f;
   }
+  int32_t ow = w, oh = h;
+  if (flags & 1u) orc_cdf_size(w, h, &ow, &oh);
+  if (ow != w || oh != h) {
+    // shrink (image.cpp:308-320): area-weighted average of the texels each
+    // output texel covers, in double, rows then columns in index order;
+    // then the luminance of the average
+    const double sx = (double)w / (double)ow, sy = (double)h / (double)oh;
+    for (int oy = 0; oy < oh; ++oy) {
+      const double y0 = (double)oy * sy, y1 = (double)(oy + 1) * sy;
+      for (int ox = 0; ox < ow; ++ox) {
+        const double x0 = (double)ox * sx, x1 = (double)(ox + 1) * sx;
+        double acc[3] = {0.0, 0.0, 0.0};
+        for (int j = (int)std::floor(y0); j < (int)std::ceil(y1) && j < h; ++j) {
+          const double wy = std::min(y1, (double)(j + 1)) - std::max(y0, (double)j);
+          for (int i = (int)std::floor(x0); i < (int)std::ceil(x1) && i < w; ++i) {
+            const double wx = std::min(x1, (double)(i + 1)) - std::max(x0, (double)i);
+            const double wgt = wx * wy;
+            for (int c = 0; c < 3; ++c) acc[c] = acc[c] + wgt * (double)vtb::h2f(half[3 * ((size_t)j * w + i) + c]);
+          }
+        }
+        const double area = sx * sy;
+        const float fr = (float)(acc[0] / area), fg = (float)(acc[1] / area), fb = (float)(acc[2] / area);
+        lum[(size_t)oy * ow + ox] = (fr * 0.2126f + fg * 0.7152f) + fb * 0.0722f;
+      }
+    }
+    w = ow;
+    h = oh;
+  }
+  if (cdf_size) { cdf_size[0] = w; cdf_size[1] = h; }
   // 3x3 Gaussian, sigma 0.75, clamp to edge (image.cpp:337-342)
   const float ws = 0.225610111284051620f, wm = 0.548779777431896800f;
   for (int y = 0; y < h; ++y)
@@ -1298,6 +1337,11 @@ int orc_build_env(const float* rgb, int32_t w, int32_t h, int32_t chunk, uint16_
   }
   cdf_fp64(func.data(), w, h, chunk, cdf_u, cdf_v, integral);
   return 0;
+}
+
+int orc_build_env(const float* rgb, int32_t w, int32_t h, int32_t chunk, uint16_t* texels, float* cdf_u,
+                  float* cdf_v, float* integral) {
+  return orc_build_env_ex(rgb, w, h, chunk, 0u, texels, cdf_u, cdf_v, integral, nullptr);
 }
 
 int orc_cdf_from_function(const float* func, int32_t w, int32_t h, int32_t chunk, float* cdf_u, float* cdf_v,

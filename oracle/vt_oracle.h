@@ -85,15 +85,27 @@ typedef struct orc_scene {
 typedef struct orc_env {
   int32_t w, h;
   const uint16_t* texels;   /* w*h*4 IEEE halves (RGBA) */
-  const float* cdf_u;       /* (w+1)*h */
-  const float* cdf_v;       /* h+1 */
+  const float* cdf_u;       /* (cdf_w+1)*cdf_h */
+  const float* cdf_v;       /* cdf_h+1 */
   float integral;
+  int32_t cdf_w, cdf_h;     /* size of the image the CDFs were built from; 0 = w, h */
 } orc_env;
 
 /* Camera uniforms of Renderer::updateCamera (renderer.cpp:343-397):
  * out[0:16] proj, [16:32] inverse proj, [32:48] inverse model-view (row-major),
  * [48:52] viewport. */
 int orc_camera_uniforms(const orc_camera* cam, int32_t width, int32_t height, float* out);
+
+/* Environment build with options: flags bit 0 builds the CDFs and the
+ * integral from the image shrunk to at most 512 texels on its long axis
+ * (calculateCDF, image.cpp:14, 308-320; the size from the reference's float
+ * arithmetic, an area-weighted box filter over the FP16 texels standing in
+ * for OpenImageIO's resize), while the texels stay full size.  cdf_size
+ * receives the CDF image's width and height. */
+int orc_build_env_ex(const float* rgb, int32_t w, int32_t h, int32_t chunk, uint32_t flags, uint16_t* texels,
+                     float* cdf_u, float* cdf_v, float* integral, int32_t* cdf_size);
+/* The reference's CDF image size for a w x h environment (image.cpp:314-317). */
+void orc_cdf_size(int32_t w, int32_t h, int32_t* cw, int32_t* ch);
 
 /* CameraParameters defaults (cameraParameters.cpp:7-17): target 0, eye at
  * distance 100 on -Z, near 0.1, far 10000, 50 mm on a 36 mm film, pinhole,

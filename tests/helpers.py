@@ -61,3 +61,21 @@ def close_all(*objs):
     for o in objs:
         if o is not None:
             o.close()
+
+
+def bricks_from_voxels(vox: np.ndarray, shape=(2, 2, 2)) -> np.ndarray:
+    """The occupancy bit-bricks of a [z, y, x] volume as the library lays them
+    out: one uint64 per brick of 2^sx x 2^sy x 2^sz voxels (shape = (sx, sy,
+    sz)), bit (x & (2^sx-1)) | (y & (2^sy-1)) << sx | (z & (2^sz-1)) << (sx+sy),
+    set for occupied voxels and for voxels outside the volume, on the brick
+    grid padded by one all-set brick on every side."""
+    sx, sy, sz = shape
+    ex, ey, ez = 1 << sx, 1 << sy, 1 << sz
+    rz, ry, rx = vox.shape
+    bz, by, bx = -(-rz // ez), -(-ry // ey), -(-rx // ex)
+    occ = np.ones(((bz + 2) * ez, (by + 2) * ey, (bx + 2) * ex), bool)
+    occ[ez:ez + rz, ey:ey + ry, ex:ex + rx] = vox != 0
+    blocks = occ.reshape(bz + 2, ez, by + 2, ey, bx + 2, ex).transpose(0, 2, 4, 1, 3, 5)   # [BZ,BY,BX,dz,dy,dx]
+    bits = blocks.reshape(bz + 2, by + 2, bx + 2, 64).astype(np.uint64)
+    weights = np.left_shift(np.uint64(1), np.arange(64, dtype=np.uint64))
+    return (bits * weights).sum(-1, dtype=np.uint64)

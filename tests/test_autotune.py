@@ -13,11 +13,21 @@ class FakeInfo:
 
 
 class FakeScene:
-    def __init__(self, res):
+    def __init__(self, res, ctx=None):
         self._res = res
+        self.ctx = ctx
+        self.shape = (2, 2, 2)
 
     def info(self):
         return FakeInfo(self._res)
+
+    def brick_shape(self):
+        return self.shape
+
+    def set_brick_shape(self, shape):
+        self.shape = tuple(shape)
+        if self.ctx is not None:
+            self.ctx.setting["brick_shape"] = self.shape
 
 
 class FakeCtx:
@@ -32,6 +42,9 @@ class FakeCtx:
     def set_lanes(self, lanes):
         self.setting["lanes"] = lanes
 
+    def set_trace_tuning(self, queue_chunk, refill_min):
+        self.setting.update(queue_chunk=queue_chunk, refill_min=refill_min)
+
     def render_batch(self, jobs, passes):
         for j in jobs:
             j.render(passes)
@@ -39,12 +52,13 @@ class FakeCtx:
 
 class FakeJob:
     """Render 'time' is spent in a fake clock: the best setting is 8M slots,
-    3 blocks per SM, 16 steps and two lanes."""
+    3 blocks per SM, 16 steps, two lanes, 8x4x2 bricks, queue chunks of 64
+    and a refill threshold of 12."""
 
     def __init__(self, ctx, clock, w=64, h=48, res=(32, 32, 32), unit=1.0):
         self.ctx, self.clock, self.unit = ctx, clock, unit
         self.width, self.height = w, h
-        self.scene = FakeScene(res)
+        self.scene = FakeScene(res, ctx)
         self.renders = 0
 
     def reset(self):
@@ -60,6 +74,9 @@ class FakeJob:
         cost += 0.05 * abs(s.get("trace_blocks_per_sm", 0) - 3)
         cost += 0.03 * abs(s.get("trace_steps", 16) - 16) / 8
         cost += 0.07 * abs(s.get("lanes", 2) - 2)
+        cost += 0.01 * abs(s.get("queue_chunk", 128) - 64) / 64
+        cost += 0.002 * abs(s.get("refill_min", 0) - 12)
+        cost += 0.0 if self.scene.shape == (3, 2, 1) else 0.004
         self.clock[0] += cost * passes * self.unit
         self.renders += 1
 
@@ -76,12 +93,15 @@ def test_sweep_picks_the_fastest_setting(fake_time, tmp_path, monkeypatch):
     ctx = FakeCtx()
     job = FakeJob(ctx, fake_time, w=4096, h=4096)    # enough samples that no slot count collapses
     best = autotune.tune(ctx, [job], passes=16, repeats=1, use_cache=False)
-    assert (best["path_slots"], best["trace_blocks_per_sm"], best["trace_steps"], best["lanes"]) == \
-        (1 << 23, 3, 16, 2)
-    assert ctx.setting == {"path_slots": 1 << 23, "trace_blocks_per_sm": 3, "trace_steps": 16, "lanes": 2}
+    assert (best["path_slots"], best["trace_blocks_per_sm"], best["trace_steps"], best["lanes"],
+            best["brick_shape"], best["queue_chunk"], best["refill_min"]) == (1 << 23, 3, 16, 2, (3, 2, 1), 64, 12)
+    assert ctx.setting == {"path_slots": 1 << 23, "trace_blocks_per_sm": 3, "trace_steps": 16, "lanes": 2,
+                           "brick_shape": (3, 2, 1), "queue_chunk": 64, "refill_min": 12}
+    assert job.scene.shape == (3, 2, 1)
     g = autotune.DEFAULT_GRID
+    # the launch-shape grid, then bricks and the DDA kernel's knobs at the best launch shape
     assert len(best["sweep"]) == len(g["path_slots"]) * len(g["trace_blocks_per_sm"]) * len(g["trace_steps"]) * \
-        len(g["lanes"])
+        len(g["lanes"]) + len(g["brick_shape"]) * len(g["queue_chunk"]) * len(g["refill_min"]) - 1
     assert not (tmp_path / "tune.json").exists()
 
 
@@ -116,4 +136,5 @@ def test_workload_key_classes():
     c = FakeJob(ctx, clock, w=512, h=512, res=(1024, 64, 64))
     assert autotune.workload_key([a]) == autotune.workload_key([b])
     assert autotune.workload_key([a]) != autotune.workload_key([c])
-    assert autotune.workload_key([a, b]).endswith("_jobs2")
+    assert "_jobs2_" in autotune.workload_key([a, b])
+    assert autotune.workload_key([a]).endswith(autotune.KNOBS)     # entries of an older knob set do not apply

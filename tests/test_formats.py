@@ -60,10 +60,14 @@ def test_vox_default_palette_and_versions():
         F.vox_decode(b"VOX " + struct.pack("<i", 150))              # truncated
 
 
-REF_VOX = "/root/reference/resources/scene_fall.vox"
+# The reference's sample inputs, found through VOXELTOY_REFERENCE_RESOURCES
+# (its resources/ directory); the tests skip when that is unset or absent.
+REF_RESOURCES = os.environ.get("VOXELTOY_REFERENCE_RESOURCES", "")
+REF_VOX = os.path.join(REF_RESOURCES, "scene_fall.vox") if REF_RESOURCES else ""
 
 
-@pytest.mark.skipif(not os.path.exists(REF_VOX), reason="the reference's sample scene is not on this machine")
+@pytest.mark.skipif(not REF_VOX or not os.path.exists(REF_VOX),
+                    reason="VOXELTOY_REFERENCE_RESOURCES does not point at the reference's sample scene")
 def test_vox_reference_sample_scene():
     data = open(REF_VOX, "rb").read()
     grid, pal = F.vox_decode(data)
@@ -188,11 +192,36 @@ def test_radiance_hdr_flat_and_rle():
         F.image_decode(b"#?RADIANCE\nFORMAT=32-bit_rle_xyze\n\n-Y 1 +X 1\n\x00\x00\x00\x00")
 
 
-REF_OBJ = "/root/reference/resources/bunny.obj"
+REF_OBJ = os.path.join(REF_RESOURCES, "bunny.obj") if REF_RESOURCES else ""
 
 
-@pytest.mark.skipif(not os.path.exists(REF_OBJ), reason="the reference's sample mesh is not on this machine")
+@pytest.mark.skipif(not REF_OBJ or not os.path.exists(REF_OBJ),
+                    reason="VOXELTOY_REFERENCE_RESOURCES does not point at the reference's sample mesh")
 def test_obj_reference_sample_mesh():
     v, i = F.obj_decode(REF_OBJ)
     assert len(v) > 1000 and len(i) > 1000
     assert i.max() < len(v) and np.isfinite(v).all()
+
+
+def test_hdr_encode_round_trip():
+    """vt_image_encode_hdr: rows bottom first in, top first in the file (the
+    decoder returns them top first), RGBE precision (8 bits of mantissa under
+    the largest channel), zeros, and negative / NaN / infinite channels."""
+    rng = np.random.default_rng(8)
+    h, w = 7, 11
+    img = (rng.random((h, w, 4)) * np.exp2(rng.integers(-10, 12, (h, w, 1)))).astype(np.float32)
+    img[0, 0, :3] = 0.0
+    img[1, 2, :3] = [-1.0, np.nan, 2.0]
+    img[2, 3, :3] = [np.inf, 1.0, 0.5]
+    data = F.encode_hdr(img)
+    assert data.startswith(b"#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y 7 +X 11\n")
+    got = F.image_decode(data)[::-1]                       # back to rows bottom first
+    rgb = np.nan_to_num(np.clip(img[..., :3], 0.0, None), nan=0.0, posinf=1.0e38).astype(np.float64)
+    ok = np.ones((h, w), bool)
+    ok[2, 3] = False
+    scale = rgb.max(axis=-1, keepdims=True)
+    assert np.all(np.abs(got - rgb)[ok] <= (scale / 128)[ok] + 1e-30)
+    assert np.all(got[0, 0] == 0.0)
+    # a zero mantissa beside a larger channel reads back as half a quantum of that channel
+    assert got[1, 2, 0] <= 2.0 / 256 and got[1, 2, 1] <= 2.0 / 256 and abs(got[1, 2, 2] - 2.0) <= 2.0 / 128
+    assert got[2, 3, 0] > 0.99e38

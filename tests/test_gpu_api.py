@@ -482,3 +482,102 @@ def test_server_teardown_returns_device_memory(ctx):
     finally:
         close_all(job, scene, env)
 
+
+
+def test_snapshot_restore_resumes_bit_identically(ctx):
+    """A job interrupted after 5 samples, snapshotted, destroyed and restored
+    into a new job reaches 12 samples with the same bits as a job that was
+    never interrupted (sums, compensations and the resolved image)."""
+    cfg = small_config2(edge=32, w=40, h=28, seed=21)
+    cfg.settings.max_samples = 1 << 20
+    scene, env, whole = gpu_setup(ctx, cfg)
+    part = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
+    resumed = None
+    try:
+        whole.render(12)
+        part.render(5)
+        snap = part.snapshot()
+        assert snap[2] == 5
+        part.close()
+        part = None
+        resumed = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
+        resumed.restore(*snap)
+        assert resumed.samples() == 5
+        resumed.render(7)
+        assert resumed.samples() == 12
+        a, b = whole.snapshot(), resumed.snapshot()
+        assert a[2] == b[2] == 12
+        assert np.array_equal(a[0].view(np.uint32), b[0].view(np.uint32))
+        assert np.array_equal(a[1].view(np.uint32), b[1].view(np.uint32))
+        assert np.array_equal(whole.readback().view(np.uint32), resumed.readback().view(np.uint32))
+        with pytest.raises(L.VtError) as e:
+            resumed.restore(snap[0], snap[1], -1)
+        assert e.value.code == L.VT_EINVAL
+        with pytest.raises(L.VtError) as e:
+            resumed.restore(snap[0][:10], snap[1][:10], 5)       # too small for the frame
+        assert e.value.code == L.VT_EINVAL
+        assert resumed.samples() == 12
+    finally:
+        close_all(*(j for j in (part, resumed) if j is not None), whole, scene, env)
+
+
+def test_server_keeps_scenes_resident_and_evicts_lru(ctx):
+    """vt_server_submit_dense: a volume is uploaded once per key, reused by
+    later requests (no volume passed), evicted least recently used first
+    when a new scene needs the budget, and its images equal renders of a
+    caller-owned scene."""
+    cfgs = [small_config1(edge=48, w=24, h=20, seed=71), small_config1(edge=40, w=24, h=20, seed=72),
+            small_config1(edge=44, w=24, h=20, seed=73)]
+    alone = []
+    for c in cfgs:
+        sc = Scene.dense(ctx, c.voxels, c.palette)
+        j = Job(ctx, sc, None, c.camera, c.settings, c.width, c.height)
+        j.render(3)
+        alone.append(j.readback().copy())
+        close_all(j, sc)
+    job_bytes = 24 * 20 * 16 * 3
+    scene_bytes = [c.voxels.size + 8 * ((c.voxels.shape[0] + 3) // 4 + 2) ** 3 + 16 + 4 for c in cfgs]
+    # room for two of the scenes and a job, not for three
+    budget = scene_bytes[0] + scene_bytes[2] + job_bytes + 4096
+    srv = Server(ctx, hbm_budget_bytes=budget, max_active_jobs=1, passes_per_round=1)
+    try:
+        def run(key, cfg, with_volume):
+            t = srv.submit_dense(key, cfg.voxels if with_volume else None, cfg.palette, cfg.camera, cfg.settings,
+                                 cfg.width, cfg.height, 3)
+            assert srv.wait(t, 60.0) == L.VT_OK
+            return srv.result(t, cfg.width, cfg.height)[0]
+
+        for img, want in [(run(10, cfgs[0], True), alone[0]), (run(10, cfgs[0], False), alone[0]),
+                          (run(11, cfgs[1], True), alone[1])]:
+            np.testing.assert_array_equal(img.view(np.uint32), want.view(np.uint32))
+        st = srv.stats()
+        assert (st.scene_uploads, st.scene_hits, st.scene_evictions, st.scenes_resident) == (2, 1, 0, 2)
+        np.testing.assert_array_equal(run(10, cfgs[0], False).view(np.uint32), alone[0].view(np.uint32))
+        # a third scene evicts the least recently used one (key 11), not key 10
+        np.testing.assert_array_equal(run(12, cfgs[2], True).view(np.uint32), alone[2].view(np.uint32))
+        st = srv.stats()
+        assert (st.scene_uploads, st.scene_evictions, st.scenes_resident) == (3, 1, 2)
+        with pytest.raises(L.VtError) as e:                       # key 11 is gone and no volume is given
+            srv.submit_dense(11, None, cfgs[1].palette, cfgs[1].camera, cfgs[1].settings, 24, 20, 3)
+        assert e.value.code == L.VT_EINVAL
+        np.testing.assert_array_equal(run(10, cfgs[0], False).view(np.uint32), alone[0].view(np.uint32))
+        assert srv.stats().bytes_in_use <= budget
+    finally:
+        srv.close()
+
+
+def test_server_does_not_charge_caller_owned_scenes(ctx):
+    """A scene the caller created is the caller's memory: a server whose
+    budget is far below the scene's size still admits requests on it (only
+    the job's buffers count)."""
+    cfg = small_config1(edge=128, w=16, h=16, seed=74)
+    sc = Scene.dense(ctx, cfg.voxels, cfg.palette)
+    srv = Server(ctx, hbm_budget_bytes=64 << 10, max_active_jobs=2, passes_per_round=2)
+    try:
+        assert sc.info().device_bytes > 2 << 20
+        t = srv.submit(sc, None, cfg.camera, cfg.settings, 16, 16, 2)
+        assert srv.wait(t, 60.0) == L.VT_OK
+        assert srv.stats().bytes_in_use == 0
+    finally:
+        srv.close()
+        sc.close()

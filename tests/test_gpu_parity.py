@@ -11,7 +11,8 @@ import time
 import numpy as np
 import pytest
 
-from helpers import close_all, gpu_setup, oracle_setup, reference_config, small_config1, small_config2
+from helpers import (bricks_from_voxels, close_all, gpu_setup, oracle_setup, reference_config, small_config1,
+                     small_config2)
 from voxeltoy_gb300 import Env, Job, Scene, Server
 from voxeltoy_gb300 import _lib as L
 from voxeltoy_gb300 import scenes as S
@@ -110,6 +111,50 @@ def test_env_build_bitexact(ctx, orc):
         assert np.all(np.abs(cu - seq.cdf_u) <= np.spacing(np.float32(1.0)))
     finally:
         env.close()
+
+
+@pytest.mark.parametrize("size", [(1100, 550), (777, 333), (300, 900)])
+def test_env_reference_size_cdf_bitexact(ctx, orc, size):
+    """VT_ENV_CDF_REFERENCE_SIZE: full-size texels, CDFs and integral of the
+    image shrunk to at most 512 texels on its long axis, equal to the
+    oracle's build of the same mode bit for bit."""
+    w, h = size
+    rgb = np.ascontiguousarray(S.sky_sun_env(w, h, peak=300.0))
+    env = Env(ctx, rgb, flags=L.VT_ENV_CDF_REFERENCE_SIZE)
+    try:
+        ref = orc.Env(rgb, chunk=32, flags=1)
+        assert (env.cdf_w, env.cdf_h) == orc.cdf_size(w, h)
+        assert max(env.cdf_w, env.cdf_h) == 512
+        cu, cv, integral = env.cdf()
+        np.testing.assert_array_equal(env.texels(), ref.texels)
+        np.testing.assert_array_equal(cu, ref.cdf_u)
+        np.testing.assert_array_equal(cv, ref.cdf_v)
+        assert integral == np.float32(ref.integral)
+    finally:
+        env.close()
+
+
+def test_samples_bitexact_reference_size_env(ctx, orc):
+    """Per-sample radiance and first hits with importance sampling through
+    the shrunk CDFs (pdf from the full-size texels) equal the oracle's."""
+    cfg = small_config2(edge=32, w=32, h=28, seed=5)
+    cfg.env_rgb = S.sky_sun_env(1040, 520, peak=400.0)
+    scene = Scene.dense(ctx, cfg.voxels, cfg.palette, flags=cfg.scene_flags)
+    env = Env(ctx, cfg.env_rgb, flags=L.VT_ENV_CDF_REFERENCE_SIZE)
+    job = Job(ctx, scene, env, cfg.camera, cfg.settings, cfg.width, cfg.height)
+    try:
+        assert (env.cdf_w, env.cdf_h) == (512, 256)
+        osc = orc.Scene(cfg.voxels, cfg.palette, scene.emissive())
+        oenv = orc.Env(cfg.env_rgb, flags=1)
+        for smp in (0, 3):
+            g_rgba, g_hits, g_cnt = job.samples_diag(smp)
+            o_rgba, o_hits, o_cnt = orc.render_samples(cfg.camera, cfg.settings, osc, oenv, cfg.width, cfg.height,
+                                                       smp, 32)
+            np.testing.assert_array_equal(g_hits, o_hits)
+            assert same_bits(g_rgba, o_rgba).all()
+            assert g_cnt[4] > 0                      # the CDFs were probed
+    finally:
+        close_all(job, scene, env)
 
 
 def test_gpu_cdf_known_answers(ctx):
@@ -400,7 +445,8 @@ def test_server_results_equal_alone(ctx):
             small_config1(edge=32, w=40, h=10, seed=10)]
     spps = [5, 7, 3]
     made = [gpu_setup(ctx, c) for c in cfgs]
-    srv = Server(ctx, hbm_budget_bytes=1 << 30, max_active_jobs=2, passes_per_round=2)
+    # round_paths=1: no budget beyond the two passes each active request gets per round
+    srv = Server(ctx, hbm_budget_bytes=1 << 30, max_active_jobs=2, passes_per_round=2, round_paths=1)
     try:
         alone = []
         for (_s, _e, j), spp in zip(made, spps):
@@ -416,6 +462,36 @@ def test_server_results_equal_alone(ctx):
             np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
         st = srv.stats()
         assert st.completed == 3 and st.failed == 0
+    finally:
+        srv.close()
+        for m in made:
+            close_all(m[2], m[0], m[1])
+
+
+def test_server_round_budget_goes_to_the_least_work_first(ctx):
+    """A round's path budget: one pass each, then the rest to the request
+    with the fewest paths left.  A 16x16x8 request and a 64x64x64 one share
+    a budget of 64*64*8 + 16*16*8 paths: the small one finishes in the first
+    round, the large one takes 8 passes a round, 8 rounds in all; both
+    images equal the ones rendered alone."""
+    cfgs = [small_config1(edge=32, w=16, h=16, seed=64), small_config1(edge=32, w=64, h=64, seed=65)]
+    spps = [8, 64]
+    made = [gpu_setup(ctx, c) for c in cfgs]
+    srv = Server(ctx, max_active_jobs=4, passes_per_round=1, round_paths=64 * 64 * 8 + 16 * 16 * 8)
+    try:
+        alone = []
+        for (_s, _e, j), spp in zip(made, spps):
+            j.render(spp)
+            alone.append(j.readback().copy())
+        srv_paused = [srv.submit(s, e, c.camera, c.settings, c.width, c.height, spp)
+                      for (s, e, _j), c, spp in zip(made, cfgs, spps)]
+        for t, want, c in zip(srv_paused, alone, cfgs):
+            assert srv.wait(t, 60.0) == L.VT_OK
+            got, _ = srv.result(t, c.width, c.height)
+            np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+        # both requests may land in the first round or the second one in the
+        # next: 8 rounds, or 9 when the small one ran alone first
+        assert srv.stats().rounds in (8, 9)
     finally:
         srv.close()
         for m in made:
@@ -524,16 +600,63 @@ def _tri_soup(seed, n_small=3000, n_large=40, res=(96, 80, 64)):
                                   L.VT_VOXELIZE_THIN | L.VT_VOXELIZE_REFERENCE_BOUNDS,
                                   L.VT_VOXELIZE_FAT | L.VT_VOXELIZE_REFERENCE_BOUNDS])
 def test_voxelize_bitexact_triangle_soup(ctx, orc, mode):
-    res = (96, 80, 64)
     v, idx = _tri_soup(3)
-    sc = Scene.voxelize(ctx, v, idx, res, mode=mode, placement=L.VT_MESH_VOXEL_SPACE)
+    for res in [(96, 80, 64), (97, 81, 66)]:            # the second one ends in partial bricks
+        sc = Scene.voxelize(ctx, v, idx, res, mode=mode, placement=L.VT_MESH_VOXEL_SPACE)
+        try:
+            got = sc.voxels()
+            want = orc.voxelize(v, idx, res, mode, placement=0)
+            np.testing.assert_array_equal(got, want)
+            assert want.sum() > 1000
+            # the voxelizer sets the brick bits itself: they equal the layout's bricks of its voxels
+            np.testing.assert_array_equal(sc.bricks(), bricks_from_voxels(want))
+        finally:
+            sc.close()
+
+
+@pytest.mark.parametrize("shape", [(2, 2, 2), (3, 2, 1), (1, 3, 2), (1, 1, 4), (4, 1, 1)])
+def test_brick_shapes_trace_identically(ctx, shape):
+    """Every brick shape: the bricks follow the layout of that shape, and a
+    sample pass (first hits, per-sample radiance) and an accumulated frame are
+    the same bits as with 4x4x4 bricks; edits keep the shape's bits."""
+    cfg = small_config2(edge=37, w=40, h=32, seed=41)      # 37^3: partial bricks on every axis
+    scene, env, job = gpu_setup(ctx, cfg)
     try:
-        got = sc.voxels()
-        want = orc.voxelize(v, idx, res, mode, placement=0)
-        np.testing.assert_array_equal(got, want)
-        assert want.sum() > 1000
+        base_rgba, base_hits, _ = job.samples_diag(0)
+        job.render(3)
+        base_img = job.readback().view(np.uint32).copy()
+        scene.set_brick_shape(shape)
+        assert scene.brick_shape() == tuple(shape)
+        np.testing.assert_array_equal(scene.bricks(), bricks_from_voxels(cfg.voxels, shape))
+        job.reset()
+        rgba, hits, _ = job.samples_diag(0)
+        assert np.array_equal(hits, base_hits)
+        assert np.array_equal(rgba.view(np.uint32), base_rgba.view(np.uint32))
+        job.render(3)
+        assert np.array_equal(job.readback().view(np.uint32), base_img)
+        scene.set_voxel(3, 4, 5, 0)
+        scene.set_voxel(36, 36, 36, 1)
+        want = cfg.voxels.copy()
+        want[5, 4, 3] = 0
+        want[36, 36, 36] = 1
+        np.testing.assert_array_equal(scene.bricks(), bricks_from_voxels(want, shape))
+        for bad in [(3, 3, 3), (3, 3, 0), (0, 2, 4), (5, 1, 0)]:
+            with pytest.raises(L.VtError):
+                scene.set_brick_shape(bad)
+        assert scene.brick_shape() == tuple(shape)
     finally:
-        sc.close()
+        close_all(job, scene, env)
+
+
+def test_dense_scene_bricks_match_the_layout(ctx):
+    rng = np.random.default_rng(5)
+    for shape in [(64, 64, 64), (13, 30, 7), (5, 4, 9)]:
+        g = (rng.random(shape) < 0.3).astype(np.uint8) * rng.integers(1, 3, size=shape, dtype=np.uint8)
+        sc = Scene.dense(ctx, g, [S.lambert(0.5), S.lambert(0.2)])
+        try:
+            np.testing.assert_array_equal(sc.bricks(), bricks_from_voxels(g))
+        finally:
+            sc.close()
 
 
 @pytest.mark.parametrize("mode", [L.VT_VOXELIZE_THIN, L.VT_VOXELIZE_FAT])
@@ -546,6 +669,39 @@ def test_voxelize_bitexact_icosphere(ctx, orc, mode):
         want = orc.voxelize(v, f, res, mode, placement=1)
         np.testing.assert_array_equal(got, want)
     finally:
+        sc.close()
+
+
+def test_voxelize_config5_full_size(ctx, orc):
+    """The large-grid workload at its full size: the fBm-displaced icosphere
+    of 1,310,720 triangles voxelized conservatively into 1024^3 equals the
+    oracle bit for bit, and one sample per pixel of a 256^2 view of that
+    volume (8 bounces) equals the oracle's per-sample radiance and first hits."""
+    v, f = S.fbm_displaced_icosphere(level=8, seed=4)
+    assert len(f) == 1310720
+    res = (1024, 1024, 1024)
+    sc = Scene.voxelize(ctx, v, f, res, mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
+                        palette=[S.lambert(0.7)])
+    job = None
+    try:
+        got = sc.voxels()
+        want = orc.voxelize(v, f, res, L.VT_VOXELIZE_FAT, placement=1)
+        assert np.array_equal(got, want)
+        assert 4_000_000 < np.count_nonzero(want) < 6_000_000
+        del want
+        assert np.array_equal(sc.bricks(), bricks_from_voxels(got))
+        cfg = S.config1(edge=8, width=256, height=256, spp=1)
+        cfg.settings.max_bounces = 8
+        job = Job(ctx, sc, None, cfg.camera, cfg.settings, 256, 256)
+        rgba, hits, _ = job.samples_diag(0)
+        osc = orc.Scene(got, [S.lambert(0.7)], None)
+        wrgba, whits, _ = orc.render_samples(cfg.camera, cfg.settings, osc, orc.Env(), 256, 256, 0, 32)
+        assert np.array_equal(hits, whits)
+        assert np.array_equal(rgba.view(np.uint32), wrgba.view(np.uint32))
+        assert ((hits[..., 3] >> 8) & 1).sum() > 10000      # the view sees the object
+    finally:
+        if job is not None:
+            job.close()
         sc.close()
 
 

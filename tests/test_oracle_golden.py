@@ -209,3 +209,47 @@ def test_wang_hash_restatement_is_the_published_function():
         return s
     for seed in [0, 1, 61, 1024, 123456789, 2 ** 31 - 1, -1, -2 ** 31, 987654]:
         assert int(_wang_hash(seed).astype(np.uint32)) == ref(seed)
+
+
+def test_reference_cdf_size_and_box_shrink(orc):
+    """The oracle's reference-size environment build: the shrunk size by the
+    reference's float arithmetic (image.cpp:314-317), and the CDFs of the
+    area-weighted box average of the FP16 texels, restated here in numpy."""
+    for (w, h) in [(1024, 512), (777, 333), (300, 900), (512, 256), (4000, 3)]:
+        m = np.float32(max(w, h))
+        want = (w, h) if max(w, h) <= 512 else \
+            (int(np.uint32(np.float32(w) / m * np.float32(512))), int(np.uint32(np.float32(h) / m * np.float32(512))))
+        assert orc.cdf_size(w, h) == want, (w, h)
+    w, h = 777, 333
+    rgb = np.random.default_rng(4).random((h, w, 3)).astype(np.float32) * 5
+    env = orc.Env(rgb, chunk=32, flags=1)
+    cw, ch = orc.cdf_size(w, h)
+    assert env.cdf_u.shape == (ch, cw + 1) and env.cdf_v.shape == (ch + 1,)
+    half = rgb.astype(np.float16).astype(np.float64)
+    sx, sy = w / cw, h / ch
+
+    def weights(n_out, scale, n_in):
+        m = np.zeros((n_out, n_in))
+        for o in range(n_out):
+            a, b = o * scale, (o + 1) * scale
+            for i in range(int(np.floor(a)), min(int(np.ceil(b)), n_in)):
+                m[o, i] = min(b, i + 1) - max(a, i)
+        return m
+    wx, wy = weights(cw, sx, w), weights(ch, sy, h)
+    rows_avg = (wy @ half.reshape(h, w * 3)).reshape(ch, w, 3)                 # rows, then columns
+    avg = np.einsum("yic,xi->yxc", rows_avg, wx, optimize=True) / (sx * sy)
+    lum = (avg[..., 0].astype(np.float32) * np.float32(0.2126) + avg[..., 1].astype(np.float32) * np.float32(0.7152)) \
+        + avg[..., 2].astype(np.float32) * np.float32(0.0722)
+    got_cu, got_cv = env.cdf_u, env.cdf_v
+    assert np.all(np.diff(got_cu, axis=1) >= 0) and got_cu[:, -1].max() == 1.0 and got_cv[-1] == 1.0
+    # the shrunk luminance drives the marginal: compare against a direct float64 build of the CDF of lum
+    ws, wm = 0.225610111284051620, 0.548779777431896800
+    lp = np.pad(lum.astype(np.float64), 1, mode="edge")
+    bl = ws * lp[1:-1, :-2] + wm * lp[1:-1, 1:-1] + ws * lp[1:-1, 2:]
+    bp = np.pad(bl, ((1, 1), (0, 0)), mode="edge")
+    bl = ws * bp[:-2] + wm * bp[1:-1] + ws * bp[2:]
+    st = np.sin(np.pi * (np.arange(ch) + 0.5) / ch)
+    func = np.maximum(bl, 0) * st[:, None]
+    rows = func.sum(1)
+    marg = np.concatenate([[0], np.cumsum(rows)]) / rows.sum()
+    assert np.allclose(got_cv, marg, atol=2e-6)

@@ -38,6 +38,11 @@ def bits(job):
     return job.readback().view(np.uint32).copy()
 
 
+def device_free_bytes() -> int:
+    import torch
+    return torch.cuda.mem_get_info()[0]
+
+
 def test_fixed_equals_batch_and_allocates_nothing(fctx):
     cfg = small_config2(edge=32, w=40, h=28, seed=11)
     cfg.settings.max_samples = 1 << 20
@@ -46,9 +51,14 @@ def test_fixed_equals_batch_and_allocates_nothing(fctx):
     try:
         for call in range(2):                       # two calls in a row
             before = fctx.memory()
+            free_before = device_free_bytes()
             rc, res = fixed(fctx, [job], 3)
             assert rc == L.VT_OK, L.load().vt_last_error()
             assert fctx.memory() == before          # nothing drawn from the context's allocator
+            if call == 1:
+                # nor from the device: the array was reserved when the context
+                # was created (the first call may still load kernel code)
+                assert device_free_bytes() == free_before
             assert res == [L.VT_SAMPLES_PENDING]
             fctx.render_batch([ref], 3, kernel=2)
             assert job.samples() == ref.samples() == 3 * (call + 1)

@@ -23,6 +23,7 @@ VT_VOXELIZE_THIN, VT_VOXELIZE_FAT, VT_VOXELIZE_REFERENCE_BOUNDS = 0, 1, 0x100
 VT_MESH_VOXEL_SPACE, VT_MESH_FIT_UNIT_CUBE = 0, 1
 VT_LENS_PINHOLE, VT_LENS_THIN_LENS, VT_LENS_ORTHOGRAPHIC = 0, 1, 2
 VT_SERVE_ARRIVAL, VT_SERVE_LEAST_WORK = 0, 1
+VT_ENV_CDF_REFERENCE_SIZE = 1
 VT_INTEGRATOR_PATH_TRACER, VT_INTEGRATOR_EDIT_MODE = 0, 1
 VT_BUTTON_ROTATE, VT_BUTTON_PAN = 1, 2
 VT_KEY_FORWARD, VT_KEY_BACK, VT_KEY_RIGHT, VT_KEY_LEFT = 0, 1, 2, 3
@@ -85,13 +86,15 @@ class BatchOpts(C.Structure):
 class ServerOpts(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_active_jobs", C.c_int32), ("passes_per_round", C.c_int32),
                 ("path_slots", C.c_int32), ("order", C.c_int32), ("quick_paths", C.c_uint64),
-                ("round_paths_cap", C.c_uint64)]
+                ("round_paths_cap", C.c_uint64), ("round_paths", C.c_uint64)]
 
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("cancelled", C.c_uint64),
                 ("failed", C.c_uint64), ("paths_traced", C.c_uint64), ("rounds", C.c_uint64),
-                ("bytes_in_use", C.c_uint64), ("active", C.c_int32), ("queued", C.c_int32)]
+                ("bytes_in_use", C.c_uint64), ("active", C.c_int32), ("queued", C.c_int32),
+                ("scene_uploads", C.c_uint64), ("scene_hits", C.c_uint64), ("scene_evictions", C.c_uint64),
+                ("scenes_resident", C.c_int32), ("pad", C.c_int32)]
 
 
 P = C.c_void_p
@@ -117,7 +120,11 @@ SIGNATURES = {
     "vt_scene_read_material_table": [P, P, C.c_int64, C.POINTER(C.c_int64)],
     "vt_scene_write_material_table": [P, C.c_int64, P, C.c_int32],
     "vt_scene_destroy": [P],
+    "vt_scene_set_brick_shape": [P, C.c_int32, C.c_int32, C.c_int32],
+    "vt_scene_get_brick_shape": [P, C.POINTER(C.c_int32)],
     "vt_env_create_image": [P, P, C.c_int32, C.c_int32, PP],
+    "vt_env_create_image_ex": [P, P, C.c_int32, C.c_int32, C.c_uint32, PP],
+    "vt_env_get_info": [P, C.POINTER(C.c_int32)],
     "vt_env_read_cdf": [P, P, C.c_size_t, P, C.c_size_t, fp],
     "vt_env_destroy": [P],
     "vt_camera_default": [C.POINTER(Camera)],
@@ -144,6 +151,8 @@ SIGNATURES = {
     "vt_job_sample_count": [P, C.POINTER(C.c_int32)],
     "vt_job_readback": [P, P, C.c_size_t, C.c_uint32],
     "vt_job_device_buffer": [P, PP, C.POINTER(C.c_int32)],
+    "vt_job_snapshot": [P, P, P, C.c_size_t, C.POINTER(C.c_int32)],
+    "vt_job_restore": [P, P, P, C.c_size_t, C.c_int32],
     "vt_job_pick": [P, C.c_float, C.c_float, fp, C.POINTER(C.c_int32)],
     "vt_job_destroy": [P],
     "vt_render_batch": [P, C.POINTER(C.c_void_p), C.c_int32, C.c_int32, C.POINTER(BatchOpts), C.POINTER(C.c_int32)],
@@ -159,9 +168,13 @@ SIGNATURES = {
                               PP],
     "vt_image_decode": [P, C.c_size_t, P, C.c_size_t, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "vt_image_encode_pfm": [P, C.c_int32, C.c_int32, C.c_int32, P, C.c_size_t, C.POINTER(C.c_size_t)],
+    "vt_image_encode_hdr": [P, C.c_int32, C.c_int32, C.c_int32, P, C.c_size_t, C.POINTER(C.c_size_t)],
     "vt_server_create": [P, C.POINTER(ServerOpts), PP],
     "vt_server_submit": [P, P, P, C.POINTER(Camera), C.POINTER(RenderSettings), C.c_int32, C.c_int32, C.c_int32,
                          C.POINTER(C.c_uint64)],
+    "vt_server_submit_dense": [P, C.c_uint64, C.c_int32, C.c_int32, C.c_int32, P, C.POINTER(Material), C.c_int32,
+                               C.c_uint32, P, C.POINTER(Camera), C.POINTER(RenderSettings), C.c_int32, C.c_int32,
+                               C.c_int32, C.POINTER(C.c_uint64)],
     "vt_server_poll": [P, C.c_uint64, C.POINTER(C.c_int32), C.POINTER(C.c_int32)],
     "vt_server_wait": [P, C.c_uint64, C.c_double],
     "vt_server_result": [P, C.c_uint64, P, C.c_size_t, C.POINTER(C.c_double)],
@@ -179,7 +192,11 @@ SIGNATURES = {
     "vt_diag_env_texels": [P, P, C.c_size_t],
     "vt_diag_stream": [P, PP],
     "vt_diag_launch_count": [P, C.POINTER(C.c_uint64)],
+    "vt_diag_l2_read_bandwidth": [P, C.c_int64, C.c_int32, C.POINTER(C.c_double)],
+    "vt_diag_check_word": [P, C.POINTER(C.c_uint32), C.POINTER(C.c_int32)],
+    "vt_diag_scene_bricks": [P, P, C.c_size_t, C.POINTER(C.c_int64)],
     "vt_diag_set_tuning": [P, C.c_int64, C.c_int32, C.c_int32, C.c_int64],
+    "vt_diag_set_trace_tuning": [P, C.c_int32, C.c_int32],
     "vt_diag_set_noise_table": [P, P, C.c_size_t],
     "vt_diag_get_noise_table": [P, P, C.c_size_t],
 }
@@ -194,13 +211,17 @@ class VtError(RuntimeError):
 
 
 def load(build_if_missing: bool = True) -> C.CDLL:
-    """Load libvoxeltoy.so (building it first if it is missing or stale)."""
+    """Load libvoxeltoy.so (building it first if it is missing or stale);
+    with VOXELTOY_CHECKED=1 in the environment, the bounds-checked build
+    libvoxeltoy_checked.so instead."""
     global _LIB
     if _LIB is not None:
         return _LIB
-    path = _build.LIB
-    if build_if_missing and not _build.up_to_date():
-        _build.build()
+    import os
+    checked = os.environ.get("VOXELTOY_CHECKED") == "1"
+    path = _build.CHECKED_LIB if checked else _build.LIB
+    if build_if_missing and not _build.up_to_date(checked):
+        _build.build(checked=checked)
     if not Path(path).exists():
         raise RuntimeError(f"{path} is missing: run voxeltoy_gb300.build.build()")
     lib = C.CDLL(str(path))

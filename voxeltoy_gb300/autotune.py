@@ -2,15 +2,23 @@
 
 Times short renders of the caller's own jobs over a grid of
   path_slots            paths in flight per launch (state + queues per slot)
-  trace_blocks_per_sm   resident blocks of the DDA kernel
+  trace_blocks_per_sm   resident blocks of the DDA kernel (rays per block x
+                        blocks: the DDA kernel's block shape is 256 threads)
   trace_steps           DDA steps between ray-pool refills
   lanes                 wavefronts side by side on as many streams (1-3)
-and applies the fastest setting to the context.  Path-slot counts above the
-workload's samples collapse to one setting; frames shorter than a few
-milliseconds are timed several times per setting.  Results are cached in a JSON
-file keyed by a workload class (log2 of the largest grid edge, log2 of the
-pixels per pass, number of jobs) so later runs with a similar workload skip
-the sweep.
+and then, at the best of those, a second sweep of
+  brick_shape           log2 extents of the scenes' occupancy bricks (4x4x4,
+                        8x4x2, 2x8x4, 4x2x8: 64 voxels a word)
+  queue_chunk           queue records a DDA warp takes per atomic
+  refill_min            compaction threshold: a DDA warp refills its lanes as
+                        soon as fewer than this many still step (0 = only
+                        every trace_steps steps)
+and applies the fastest setting to the context.  Every setting renders the
+same bits.  Path-slot counts above the workload's samples collapse to one
+setting; frames shorter than a few milliseconds are timed several times per
+setting.  Results are cached in a JSON file keyed by a workload class (log2
+of the largest grid edge, log2 of the pixels per pass, number of jobs) and
+the set of knobs swept, so later runs with a similar workload skip the sweep.
 """
 from __future__ import annotations
 
@@ -26,7 +34,11 @@ DEFAULT_GRID = {
     "trace_blocks_per_sm": [0, 3, 5],
     "trace_steps": [8, 16, 32],
     "lanes": [2, 3, 1],
+    "brick_shape": [(2, 2, 2), (3, 2, 1), (1, 3, 2), (2, 1, 3)],
+    "queue_chunk": [128, 64, 256],
+    "refill_min": [0, 12, 20],
 }
+KNOBS = "slots,bps,steps,lanes,brick,chunk,refill"
 
 
 def cache_path() -> Path:
@@ -39,12 +51,18 @@ def cache_path() -> Path:
 def workload_key(jobs) -> str:
     edge = max(max(j.scene.info().resolution) for j in jobs)
     pixels = sum(j.width * j.height for j in jobs)
-    return f"edge{int(round(math.log2(max(edge, 1))))}_px{int(round(math.log2(max(pixels, 1))))}_jobs{len(jobs)}"
+    return (f"edge{int(round(math.log2(max(edge, 1))))}_px{int(round(math.log2(max(pixels, 1))))}_jobs{len(jobs)}"
+            f"_{KNOBS}")
 
 
-def _apply(ctx, setting: dict):
+def _apply(ctx, setting: dict, jobs=()):
     ctx.set_lanes(setting.get("lanes", 2))
     ctx.set_tuning(setting["path_slots"], setting["trace_blocks_per_sm"], setting["trace_steps"])
+    ctx.set_trace_tuning(setting.get("queue_chunk", 128), setting.get("refill_min", 0))
+    shape = tuple(setting.get("brick_shape", (2, 2, 2)))
+    for sc in {id(j.scene): j.scene for j in jobs}.values():
+        if tuple(sc.brick_shape()) != shape:
+            sc.set_brick_shape(shape)
 
 
 def _time_render(ctx, jobs, passes: int, repeats: int) -> float:
@@ -80,7 +98,7 @@ def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None
             cache = {}
     if use_cache and key in cache:
         best = dict(cache[key])
-        _apply(ctx, best)
+        _apply(ctx, best, jobs)
         best.update(key=key, cached=True)
         return best
     grid = dict(DEFAULT_GRID, **(grid or {}))
@@ -93,12 +111,24 @@ def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None
     results = []
     for lanes, slots, bps, steps in itertools.product(grid["lanes"], slot_list, grid["trace_blocks_per_sm"],
                                                       grid["trace_steps"]):
-        setting = {"path_slots": slots, "trace_blocks_per_sm": bps, "trace_steps": steps, "lanes": lanes}
-        _apply(ctx, setting)
+        setting = {"path_slots": slots, "trace_blocks_per_sm": bps, "trace_steps": steps, "lanes": lanes,
+                   "brick_shape": tuple(grid["brick_shape"][0]), "queue_chunk": grid["queue_chunk"][0],
+                   "refill_min": grid["refill_min"][0]}
+        _apply(ctx, setting, jobs)
+        results.append((_time_render(ctx, jobs, passes, reps), setting))
+    results.sort(key=lambda r: r[0])
+    # the bricks and the DDA kernel's queue chunk and compaction threshold at
+    # the best launch shape
+    first = dict(results[0][1])
+    for shape, chunk, refill in itertools.product(grid["brick_shape"], grid["queue_chunk"], grid["refill_min"]):
+        if (tuple(shape), chunk, refill) == (first["brick_shape"], first["queue_chunk"], first["refill_min"]):
+            continue
+        setting = dict(first, brick_shape=tuple(shape), queue_chunk=chunk, refill_min=refill)
+        _apply(ctx, setting, jobs)
         results.append((_time_render(ctx, jobs, passes, reps), setting))
     results.sort(key=lambda r: r[0])
     t, best = results[0]
-    _apply(ctx, best)
+    _apply(ctx, best, jobs)
     best = dict(best, seconds=t)
     for j in jobs:
         j.reset()

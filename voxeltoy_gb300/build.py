@@ -19,6 +19,7 @@ INCLUDE = PKG.parent / "include"
 OUT_DIR = PKG / "_lib"
 BUILD_DIR = PKG / "_lib" / "obj"
 LIB = OUT_DIR / "libvoxeltoy.so"
+CHECKED_LIB = OUT_DIR / "libvoxeltoy_checked.so"   # bounds-checked kernels (VT_CHECKED)
 CLI_SRC = PKG / "host" / "vt_cli.cpp"
 CLI = OUT_DIR / "vt_cli"
 
@@ -42,10 +43,11 @@ def _deps() -> list[Path]:
     return [CSRC / s for s in SOURCES] + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + sorted(INCLUDE.glob("*.h"))
 
 
-def up_to_date() -> bool:
-    if not LIB.exists():
+def up_to_date(checked: bool = False) -> bool:
+    lib = CHECKED_LIB if checked else LIB
+    if not lib.exists():
         return False
-    t = LIB.stat().st_mtime
+    t = lib.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps() + [Path(__file__)])
 
 
@@ -62,17 +64,23 @@ def build_cli(force: bool = False) -> Path:
     return CLI
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
     """Compile every CUDA source and link libvoxeltoy.so (and the C++ host
-    program vt_cli next to it); returns the library's path."""
-    if not force and up_to_date():
-        build_cli()
-        return LIB
-    BUILD_DIR.mkdir(parents=True, exist_ok=True)
+    program vt_cli next to it); returns the library's path.  checked: the
+    bounds-checked variant libvoxeltoy_checked.so (-DVT_CHECKED), for the
+    checked test pass."""
+    lib = CHECKED_LIB if checked else LIB
+    if not force and up_to_date(checked):
+        if not checked:
+            build_cli()
+        return lib
+    obj_dir = BUILD_DIR.with_name("obj_checked") if checked else BUILD_DIR
+    obj_dir.mkdir(parents=True, exist_ok=True)
     procs = []
     for src in SOURCES:
-        obj = BUILD_DIR / (Path(src).stem + ".o")
-        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+        obj = obj_dir / (Path(src).stem + ".o")
+        cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *(["-DVT_CHECKED=1"] if checked else []), "-c", str(CSRC / src),
+               "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), file=sys.stderr)
         procs.append((src, obj, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
@@ -85,15 +93,16 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             print(out.decode(errors="replace"), file=sys.stderr)
     if errors:
         raise RuntimeError("nvcc failed:\n" + "\n".join(errors))
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *[str(o) for _s, o, _p in procs], "-lpthread", "-ldl", "-lrt"]
     r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))
-    os.replace(tmp, LIB)
-    build_cli(force=True)
-    return LIB
+    os.replace(tmp, lib)
+    if not checked:
+        build_cli(force=True)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose=True))
+    print(build(force="--force" in sys.argv, verbose=True, checked="--checked" in sys.argv))

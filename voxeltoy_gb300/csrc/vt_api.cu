@@ -134,6 +134,11 @@ extern "C" int vt_create(const vt_device_opts* opts, vt_context** out) {
   if (rc == VT_OK) rc = c->alloc((void**)&c->d_error, sizeof(int32_t) * 4);
   if (rc != VT_OK) { vt_destroy(c); return rc; }
   cudaMemset(c->d_error, 0, sizeof(int32_t) * 4);
+  // vt_render_batch_fixed's device array: loaded and located now, with this
+  // device current, instead of at that entry point's first call.  A failure
+  // here is not fatal to the context; the entry point retries and reports it.
+  if (fixed_scratch_setup(dev) != VT_OK)
+    c->log("vt_render_batch_fixed's device array is not available on device %d: %s", dev, vt_last_error());
   *out = c;
   return VT_OK;
 }
@@ -217,6 +222,12 @@ vt_scene::~vt_scene() {
 }
 
 // Volume bounds of createVoxelDataTexture (renderer.cpp:845-850, 928-931).
+static BrickShape scene_shape(const vt_scene* s) {
+  BrickShape b;
+  b.sx = s->bsh[0]; b.sy = s->bsh[1]; b.sz = s->bsh[2];
+  return b;
+}
+
 static void scene_bounds(vt_scene* s) {
   const float voxel = 1000.0f / (float)std::max(s->res[0], std::max(s->res[1], s->res[2]));
   for (int i = 0; i < 3; ++i) {
@@ -224,7 +235,7 @@ static void scene_bounds(vt_scene* s) {
     s->bmin[i] = -size * 0.5f;
     s->bmax[i] = size * 0.5f;
     s->vsize[i] = (s->bmax[i] - s->bmin[i]) / (float)s->res[i];
-    s->bdim[i] = (s->res[i] + 3) / 4;
+    s->bdim[i] = (s->res[i] + (1 << s->bsh[i]) - 1) >> s->bsh[i];
   }
 }
 
@@ -347,8 +358,10 @@ static int scene_emissive(vt_context* ctx, vt_scene* s, const int32_t* emissive,
   return VT_OK;
 }
 
+// Palette, bit-bricks (unless the voxelizer built them: s->bricks set and
+// every voxel's entry known to be within the palette) and emissive list.
 static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette, int32_t n_palette,
-                        const int32_t* emissive, int64_t n_emissive, uint32_t flags) {
+                        const int32_t* emissive, int64_t n_emissive, uint32_t flags, bool bricks_built = false) {
   const int64_t nvox = (int64_t)s->res[0] * s->res[1] * s->res[2];
   // palette
   std::vector<uint4> pal(std::max(n_palette, 1));
@@ -375,17 +388,19 @@ static int scene_finish(vt_context* ctx, vt_scene* s, const vt_material* palette
           "palette upload");
   // bit-bricks
   const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
-  rc = ctx->alloc((void**)&s->bricks, sizeof(unsigned long long) * nb);
-  if (rc != VT_OK) return rc;
-  // the bricks pass also finds the largest palette entry the volume uses
-  unsigned long long* d_top = ctx->d_queue + 1;
-  VT_CUDA(cudaMemsetAsync(d_top, 0, sizeof(unsigned long long), ctx->stream), "brick build");
-  VT_CUDA(launch_build_bricks(s->grid, s->res[0], s->res[1], s->res[2], s->bricks, s->bdim[0], s->bdim[1],
-                              s->bdim[2], d_top, ctx->stream), "brick build");
-  unsigned long long top = 0;   // pageable: the read has completed when the copy returns
-  VT_CUDA(cudaMemcpyAsync(&top, d_top, sizeof(top), cudaMemcpyDeviceToHost, ctx->stream), "brick build");
-  if (top > (unsigned long long)n_palette)
-    return fail(VT_EINVAL, "voxel uses palette entry %d of %d", (int)top, n_palette);
+  if (!bricks_built) {
+    rc = ctx->alloc((void**)&s->bricks, sizeof(unsigned long long) * nb);
+    if (rc != VT_OK) return rc;
+    // the bricks pass also finds the largest palette entry the volume uses
+    unsigned long long* d_top = ctx->d_queue + 1;
+    VT_CUDA(cudaMemsetAsync(d_top, 0, sizeof(unsigned long long), ctx->stream), "brick build");
+    VT_CUDA(launch_build_bricks(s->grid, s->res[0], s->res[1], s->res[2], s->bricks, s->bdim[0], s->bdim[1],
+                                s->bdim[2], scene_shape(s), d_top, ctx->stream), "brick build");
+    unsigned long long top = 0;   // pageable: the read has completed when the copy returns
+    VT_CUDA(cudaMemcpyAsync(&top, d_top, sizeof(top), cudaMemcpyDeviceToHost, ctx->stream), "brick build");
+    if (top > (unsigned long long)n_palette)
+      return fail(VT_EINVAL, "voxel uses palette entry %d of %d", (int)top, n_palette);
+  }
   s->flags = flags;
   rc = scene_emissive(ctx, s, emissive, n_emissive, flags);
   if (rc != VT_OK) return rc;
@@ -414,6 +429,7 @@ static int scene_alloc(vt_context* ctx, int32_t rx, int32_t ry, int32_t rz, vt_s
 extern "C" int vt_scene_create(vt_context* ctx, int32_t rx, int32_t ry, int32_t rz, const uint8_t* voxels,
                                const vt_material* palette, int32_t n_palette, const int32_t* emissive_indices,
                                int64_t n_emissive, uint32_t flags, vt_scene** out) {
+  vt::Range nvtx_range("vt.scene_build");
   VT_CHECK_ARG(voxels && palette, "voxels/palette is null");
   VT_CHECK_ARG(n_palette >= 1 && n_palette <= 255, "n_palette must be in [1, 255]");
   VT_CHECK_ARG(n_emissive >= 0, "n_emissive < 0");
@@ -511,6 +527,7 @@ extern "C" int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices, in
                                       const uint32_t* indices, int64_t n_triangles, int32_t rx, int32_t ry,
                                       int32_t rz, int32_t mode, int32_t placement, const vt_material* palette,
                                       int32_t n_palette, vt_scene** out) {
+  vt::Range nvtx_range("vt.voxelize");
   VT_CHECK_ARG(ctx && out, "null argument");
   VT_CHECK_ARG(n_triangles == 0 || (vertices && indices), "vertices/indices is null");
   VT_CHECK_ARG(n_vertices >= 0 && n_triangles >= 0, "negative counts");
@@ -530,23 +547,33 @@ extern "C" int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices, in
     fit_unit_cube(vertices, n_vertices, rx, ry, rz, vs);
     vsrc = vs.data();
   }
+  // mesh and the large-triangle list through the budgeted allocator; the
+  // voxelizer sets the brick bits itself, so no separate brick pass follows
   float* d_v = nullptr;
   uint32_t* d_i = nullptr;
+  const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
   rc = ctx->alloc((void**)&d_v, sizeof(float) * 3 * std::max<int64_t>(n_vertices, 1));
   if (rc == VT_OK) rc = ctx->alloc((void**)&d_i, sizeof(uint32_t) * 3 * std::max<int64_t>(n_triangles, 1));
-  if (rc != VT_OK) { ctx->release(d_v); delete s; return rc; }
+  if (rc == VT_OK) rc = ctx->ensure_scratch(voxelize_scratch_bytes(n_triangles));
+  if (rc == VT_OK) rc = ctx->alloc((void**)&s->bricks, sizeof(unsigned long long) * nb);
+  if (rc != VT_OK) { ctx->release(d_v); ctx->release(d_i); delete s; return rc; }
   cudaError_t e = cudaMemsetAsync(s->grid, 0, (size_t)nvox, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_bricks_init(s->bricks, rx, ry, rz, s->bdim[0], s->bdim[1], s->bdim[2], scene_shape(s), ctx->stream);
   if (e == cudaSuccess && n_vertices)
     e = cudaMemcpyAsync(d_v, vsrc, sizeof(float) * 3 * n_vertices, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && n_triangles)
     e = cudaMemcpyAsync(d_i, indices, sizeof(uint32_t) * 3 * n_triangles, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = launch_voxelize(d_v, d_i, n_triangles, rx, ry, rz, mode & 1,
-                                                (mode & VT_VOXELIZE_REFERENCE_BOUNDS) != 0, s->grid, 1, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_voxelize(d_v, d_i, n_triangles, rx, ry, rz, mode & 1, (mode & VT_VOXELIZE_REFERENCE_BOUNDS) != 0,
+                        s->grid, 1, s->bricks, s->bdim[0], s->bdim[1], scene_shape(s), ctx->scratch,
+                        ctx->sm_count * 4, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   ctx->release(d_v);
   ctx->release(d_i);
   if (e != cudaSuccess) { delete s; return cuda_fail(e, "voxelization"); }
-  rc = scene_finish(ctx, s, palette, n_palette, nullptr, 0, VT_SCENE_AUTO_EMISSIVE | VT_SCENE_PRUNE_EMISSIVE);
+  rc = scene_finish(ctx, s, palette, n_palette, nullptr, 0, VT_SCENE_AUTO_EMISSIVE | VT_SCENE_PRUNE_EMISSIVE,
+                    /*bricks_built=*/true);
   if (rc != VT_OK) { delete s; return rc; }
   *out = s;
   return VT_OK;
@@ -702,36 +729,57 @@ static EnvScratch env_scratch(void* base, const size_t* offs) {
   return S;
 }
 
+// The reference's CDF image size (calculateCDF, image.cpp:14, 314-317): at
+// most 512 texels on the long axis, by its float arithmetic.
+static void reference_cdf_size(int32_t w, int32_t h, int32_t* cw, int32_t* ch) {
+  const unsigned m = (unsigned)std::max(w, h);
+  if (m <= 512u) { *cw = w; *ch = h; return; }
+  *cw = (int32_t)(unsigned)((float)(unsigned)w / (float)m * 512.0f);
+  *ch = (int32_t)(unsigned)((float)(unsigned)h / (float)m * 512.0f);
+}
+
 extern "C" int vt_env_create_image(vt_context* ctx, const float* rgb, int32_t w, int32_t h, vt_env** out) {
+  return vt_env_create_image_ex(ctx, rgb, w, h, 0u, out);
+}
+
+extern "C" int vt_env_create_image_ex(vt_context* ctx, const float* rgb, int32_t w, int32_t h, uint32_t flags,
+                                      vt_env** out) {
+  vt::Range nvtx_range("vt.env_build");
   VT_CHECK_ARG(ctx && rgb && out, "null argument");
   VT_CHECK_ARG(w > 0 && h > 0 && (int64_t)w * h < ((int64_t)1 << 28), "bad image size");
+  VT_CHECK_ARG((flags & ~(uint32_t)VT_ENV_CDF_REFERENCE_SIZE) == 0, "unknown environment flags");
   *out = nullptr;
   vt_env* env = new vt_env();
   env->ctx = ctx;
   env->w = w;
   env->h = h;
+  env->cdf_w = w;
+  env->cdf_h = h;
+  if (flags & VT_ENV_CDF_REFERENCE_SIZE) reference_cdf_size(w, h, &env->cdf_w, &env->cdf_h);
+  const int32_t cw = env->cdf_w, ch = env->cdf_h;
+  VT_CHECK_ARG(cw > 0 && ch > 0, "the shrunk CDF image is empty");
   const size_t n = (size_t)w * h;
   int rc = ctx->alloc((void**)&env->texels, sizeof(uint2) * n);
-  if (rc == VT_OK) rc = ctx->alloc((void**)&env->cdf_u, sizeof(float) * (size_t)(w + 1) * h);
-  if (rc == VT_OK) rc = ctx->alloc((void**)&env->cdf_v, sizeof(float) * (size_t)(h + 1));
+  if (rc == VT_OK) rc = ctx->alloc((void**)&env->cdf_u, sizeof(float) * (size_t)(cw + 1) * ch);
+  if (rc == VT_OK) rc = ctx->alloc((void**)&env->cdf_v, sizeof(float) * (size_t)(ch + 1));
   size_t offs[9];
   const size_t sb = env_scratch_bytes(w, h, offs);
   if (rc == VT_OK) rc = ctx->ensure_scratch(sb);   // kept by the context for the next build
   if (rc != VT_OK) { delete env; return rc; }
   void* scratch = ctx->scratch;
   EnvScratch S = env_scratch(scratch, offs);
-  // row weights sin(pi (y + 0.5) / h) as calculateImageIntegral computes them (image.cpp:366)
-  std::vector<float> sin_theta(h);
-  for (int y = 0; y < h; ++y) sin_theta[y] = (float)std::sin(M_PI * (double)((float)y + 0.5f) / (double)(float)h);
+  // row weights sin(pi (y + 0.5) / h) of the CDF image, as calculateImageIntegral computes them (image.cpp:366)
+  std::vector<float> sin_theta(ch);
+  for (int y = 0; y < ch; ++y) sin_theta[y] = (float)std::sin(M_PI * (double)((float)y + 0.5f) / (double)(float)ch);
   float* d_rgb = (float*)((char*)scratch + offs[7]);
   uint32_t* d_out = (uint32_t*)((char*)scratch + offs[8]);   // integral bits, first non-finite texel
   uint32_t res[2] = {0u, 0u};   // pageable: the read has completed when the copy returns
   cudaError_t e = cudaMemcpyAsync(d_rgb, rgb, sizeof(float) * 3 * n, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(S.sin_theta, sin_theta.data(), sizeof(float) * h, cudaMemcpyHostToDevice, ctx->stream);
+    e = cudaMemcpyAsync(S.sin_theta, sin_theta.data(), sizeof(float) * ch, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_out + 1, 0xff, sizeof(uint32_t), ctx->stream);
   if (e == cudaSuccess)
-    e = launch_env_build(d_rgb, w, h, S, env->texels, env->cdf_u, env->cdf_v, (float*)d_out, d_out + 1,
+    e = launch_env_build(d_rgb, w, h, cw, ch, S, env->texels, env->cdf_u, env->cdf_v, (float*)d_out, d_out + 1,
                          ctx->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(res, d_out, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
@@ -751,10 +799,16 @@ extern "C" int vt_env_read_cdf(const vt_env* env, float* cdf_u, size_t cu_bytes,
                                float* integral) {
   VT_CHECK_ARG(env, "env is null");
   cudaSetDevice(env->ctx->device);
-  const size_t nu = sizeof(float) * (size_t)(env->w + 1) * env->h, nv = sizeof(float) * (size_t)(env->h + 1);
+  const size_t nu = sizeof(float) * (size_t)(env->cdf_w + 1) * env->cdf_h, nv = sizeof(float) * (size_t)(env->cdf_h + 1);
   if (cdf_u) { VT_CHECK_ARG(cu_bytes >= nu, "cdf_u too small"); VT_CUDA(cudaMemcpy(cdf_u, env->cdf_u, nu, cudaMemcpyDeviceToHost), "cdf_u"); }
   if (cdf_v) { VT_CHECK_ARG(cv_bytes >= nv, "cdf_v too small"); VT_CUDA(cudaMemcpy(cdf_v, env->cdf_v, nv, cudaMemcpyDeviceToHost), "cdf_v"); }
   if (integral) *integral = env->integral;
+  return VT_OK;
+}
+
+extern "C" int vt_env_get_info(const vt_env* env, int32_t* size) {
+  VT_CHECK_ARG(env && size, "null argument");
+  size[0] = env->w; size[1] = env->h; size[2] = env->cdf_w; size[3] = env->cdf_h;
   return VT_OK;
 }
 
@@ -1055,6 +1109,7 @@ int vt::build_frame(vt_job* j) {
     F.vsize[i] = s->vsize[i];
     F.vext[i] = 1.0f / (s->bmax[i] - s->bmin[i]);
     F.bdim[i] = s->bdim[i];
+    F.bsh[i] = s->bsh[i];
   }
   const float len = std::sqrt(((float)s->res[0] * (float)s->res[0] + (float)s->res[1] * (float)s->res[1]) +
                               (float)s->res[2] * (float)s->res[2]);
@@ -1077,7 +1132,10 @@ int vt::build_frame(vt_job* j) {
   F.env_integral = j->env ? j->env->integral : 0.0f;
   F.env_w = j->env ? j->env->w : 0;
   F.env_h = j->env ? j->env->h : 0;
+  F.env_cdf_w = j->env ? j->env->cdf_w : 0;
+  F.env_cdf_h = j->env ? j->env->cdf_h : 0;
   F.n_emissive = (int32_t)s->n_emissive;
+  F.n_palette = s->n_palette;
   F.max_bounces = S.max_bounces;
   F.rr_start = S.rr_start_bounce;
   F.inv_gamma = 1.0f / S.gamma;
@@ -1217,6 +1275,7 @@ int vt::refresh_job(vt_job* j) {
 
 int vt::render_jobs(vt_context* ctx, vt_job* const* jobs, int32_t n, const int32_t* passes, int kernel,
                     int path_slots, int blocks_per_sm, bool count) {
+  vt::Range nvtx_range("vt.render");
   cudaSetDevice(ctx->device);
   for (int32_t i = 0; i < n; ++i) {
     const int rc = refresh_job(jobs[i]);
@@ -1284,6 +1343,7 @@ static int wf_reserve(vt_context* ctx, int64_t slots, int64_t items) {
 // One wavefront launch over `entries` (tile_begin = first item of each job).
 static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std::vector<Grid>& grids,
                      int64_t items, int64_t slots_cap, int blocks_per_sm, bool count) {
+  vt::Range nvtx_range("vt.wavefront_launch");
   const int64_t slots = std::max<int64_t>(32, std::min<int64_t>(items, slots_cap));
   int rc = wf_reserve(ctx, slots, items);
   if (rc != VT_OK) return rc;
@@ -1338,6 +1398,8 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     P[l].n_items = (unsigned long long)(l + 1 == lanes ? items : items / lanes * (l + 1));
     P[l].sbuf = ctx->sbuf;
     P[l].counters = count ? ctx->d_counters : nullptr;
+    P[l].trace_chunk = (uint32_t)ctx->trace_chunk;
+    P[l].refill_min = ctx->refill_min;
   }
   // control words zero (first stream empty), item counters at each lane's first item
   VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, vt_context::kMaxLanes * kCtlBytes, st), "wavefront control");
@@ -1408,6 +1470,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   // Groups run until every lane's next stream is empty (its items are done;
   // a finished lane's rounds find nothing to do).
   for (;;) {
+    vt::Range rounds_range("vt.rounds");   // eight rounds of every lane, then the live-count check
     if (ctx->use_graphs) {
       VT_CUDA(cudaGraphLaunch(ctx->rounds_exec, st), "wavefront rounds");
     } else {
@@ -1425,6 +1488,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
   }
   long long max_pixels = 0;
   for (const JobEntry& e : entries) max_pixels = std::max<long long>(max_pixels, e.n_pixels);
+  vt::Range acc_range("vt.accumulate");
   VT_CUDA(launch_wf_accumulate(ctx->d_jobs, (int)entries.size(), max_pixels, ctx->sbuf, st), "accumulate");
   ctx->launches += 1;
   return VT_OK;
@@ -1466,17 +1530,7 @@ int vt::render_wavefront(vt_context* ctx, vt_job* const* jobs, int32_t n, const 
       e.n_pixels = (int64_t)jobs[i]->w * jobs[i]->h;
       items += e.n_pixels * p;
       entries.push_back(e);
-      Grid g;
-      memset(&g, 0, sizeof(g));
-      const Frame& F = jobs[i]->frame;
-      g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
-      g.bx = F.bdim[0] + 2; g.bxy = (F.bdim[0] + 2) * (F.bdim[1] + 2);
-      g.max_steps = F.max_steps;
-      g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
-      g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
-      g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
-      g.bricks = jobs[i]->dev.bricks + 1 + g.bx + g.bxy;
-      grids.push_back(g);
+      grids.push_back(make_grid(jobs[i]->frame, jobs[i]->dev.bricks));
       done[i] += p;
     }
     if (items >= ((int64_t)1 << 32)) return fail(VT_EINVAL, "more than 2^32 samples in one launch");
@@ -1515,6 +1569,7 @@ extern "C" int vt_job_sample_count(const vt_job* j, int32_t* samples) {
 }
 
 extern "C" int vt_job_readback(vt_job* j, float* rgba, size_t bytes, uint32_t flags) {
+  vt::Range nvtx_range("vt.readback");
   VT_CHECK_ARG(j && rgba, "null argument");
   const size_t n = (size_t)j->w * j->h;
   VT_CHECK_ARG(bytes >= n * sizeof(float4), "output buffer too small");
@@ -1527,6 +1582,31 @@ extern "C" int vt_job_readback(vt_job* j, float* rgba, size_t bytes, uint32_t fl
                          j->ctx->stream), "resolve");
   VT_CUDA(cudaMemcpyAsync(rgba, j->staging, sizeof(float4) * n, cudaMemcpyDeviceToHost, j->ctx->stream), "readback");
   VT_CUDA(cudaStreamSynchronize(j->ctx->stream), "readback");
+  return VT_OK;
+}
+
+extern "C" int vt_job_snapshot(const vt_job* j, float* sum, float* comp, size_t bytes_each, int32_t* samples) {
+  VT_CHECK_ARG(j && sum && comp && samples, "null argument");
+  const size_t n = (size_t)j->w * j->h;
+  VT_CHECK_ARG(bytes_each >= n * sizeof(float4), "output buffers too small: width*height*4 floats each");
+  cudaSetDevice(j->ctx->device);
+  VT_CUDA(cudaMemcpyAsync(sum, j->sum, sizeof(float4) * n, cudaMemcpyDeviceToHost, j->ctx->stream), "snapshot");
+  VT_CUDA(cudaMemcpyAsync(comp, j->comp, sizeof(float4) * n, cudaMemcpyDeviceToHost, j->ctx->stream), "snapshot");
+  VT_CUDA(cudaStreamSynchronize(j->ctx->stream), "snapshot");
+  *samples = j->samples;
+  return VT_OK;
+}
+
+extern "C" int vt_job_restore(vt_job* j, const float* sum, const float* comp, size_t bytes_each, int32_t samples) {
+  VT_CHECK_ARG(j && sum && comp, "null argument");
+  const size_t n = (size_t)j->w * j->h;
+  VT_CHECK_ARG(bytes_each >= n * sizeof(float4), "input buffers too small: width*height*4 floats each");
+  VT_CHECK_ARG(samples >= 0 && samples <= j->set.max_samples, "sample count out of range [0, max_samples]");
+  cudaSetDevice(j->ctx->device);
+  VT_CUDA(cudaMemcpyAsync(j->sum, sum, sizeof(float4) * n, cudaMemcpyHostToDevice, j->ctx->stream), "restore");
+  VT_CUDA(cudaMemcpyAsync(j->comp, comp, sizeof(float4) * n, cudaMemcpyHostToDevice, j->ctx->stream), "restore");
+  VT_CUDA(cudaStreamSynchronize(j->ctx->stream), "restore");
+  j->samples = samples;
   return VT_OK;
 }
 
@@ -1566,8 +1646,8 @@ extern "C" int vt_scene_set_voxel(vt_scene* s, int32_t x, int32_t y, int32_t z, 
   vt_context* ctx = s->ctx;
   cudaSetDevice(ctx->device);
   const int64_t idx = (int64_t)x + (int64_t)s->res[0] * ((int64_t)y + (int64_t)s->res[1] * z);
-  VT_CUDA(launch_set_voxel(s->grid, s->bricks, s->res[0], s->res[1], s->bdim[0], s->bdim[1], x, y, z,
-                           (uint8_t)entry, ctx->stream), "voxel edit");
+  VT_CUDA(launch_set_voxel(s->grid, s->bricks, s->res[0], s->res[1], s->bdim[0], s->bdim[1], scene_shape(s), x, y,
+                           z, (uint8_t)entry, ctx->stream), "voxel edit");
   int rc = VT_OK;
   if (s->flags & VT_SCENE_AUTO_EMISSIVE) {
     rc = scene_emissive(ctx, s, nullptr, 0, s->flags);          // rediscover from the palette
@@ -1810,6 +1890,101 @@ extern "C" int vt_diag_builtins(vt_context* ctx, int32_t fn, const float* a, con
   return VT_OK;
 }
 
+extern "C" int vt_scene_set_brick_shape(vt_scene* s, int32_t sx, int32_t sy, int32_t sz) {
+  VT_CHECK_ARG(s, "scene is null");
+  // every extent at least 2: the padded border is then at least two voxels
+  // deep, which the DDA's look-ahead by one cell beyond an exit relies on
+  VT_CHECK_ARG(sx >= 1 && sy >= 1 && sz >= 1 && sx <= 4 && sy <= 4 && sz <= 4 && sx + sy + sz == 6,
+               "brick shape: log2 extents in [1, 4] that sum to 6 (64 voxels a brick)");
+  if (sx == s->bsh[0] && sy == s->bsh[1] && sz == s->bsh[2]) return VT_OK;
+  vt_context* ctx = s->ctx;
+  cudaSetDevice(ctx->device);
+  const int32_t old[3] = {s->bsh[0], s->bsh[1], s->bsh[2]};
+  s->bsh[0] = sx; s->bsh[1] = sy; s->bsh[2] = sz;
+  int32_t bdim[3];
+  for (int i = 0; i < 3; ++i) bdim[i] = (s->res[i] + (1 << s->bsh[i]) - 1) >> s->bsh[i];
+  const int64_t nb = (int64_t)(bdim[0] + 2) * (bdim[1] + 2) * (bdim[2] + 2);
+  unsigned long long* bricks = nullptr;
+  int rc = ctx->alloc((void**)&bricks, sizeof(unsigned long long) * nb);
+  if (rc != VT_OK) { for (int i = 0; i < 3; ++i) s->bsh[i] = old[i]; return rc; }
+  cudaError_t e = launch_build_bricks(s->grid, s->res[0], s->res[1], s->res[2], bricks, bdim[0], bdim[1], bdim[2],
+                                      scene_shape(s), nullptr, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    ctx->release(bricks);
+    for (int i = 0; i < 3; ++i) s->bsh[i] = old[i];
+    return cuda_fail(e, "brick rebuild");
+  }
+  const int64_t old_nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
+  ctx->release(s->bricks);
+  s->bricks = bricks;
+  for (int i = 0; i < 3; ++i) s->bdim[i] = bdim[i];
+  s->bytes = s->bytes - sizeof(unsigned long long) * (uint64_t)old_nb + sizeof(unsigned long long) * (uint64_t)nb;
+  s->generation++;   // jobs on this scene rebuild their frames before their next pass
+  return VT_OK;
+}
+
+extern "C" int vt_scene_get_brick_shape(const vt_scene* s, int32_t* shape) {
+  VT_CHECK_ARG(s && shape, "null argument");
+  for (int i = 0; i < 3; ++i) shape[i] = s->bsh[i];
+  return VT_OK;
+}
+
+extern "C" int vt_diag_scene_bricks(const vt_scene* s, uint64_t* out, size_t bytes, int64_t* n_words) {
+  VT_CHECK_ARG(s && n_words, "null argument");
+  const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
+  *n_words = nb;
+  if (!out) return VT_OK;
+  VT_CHECK_ARG(bytes >= sizeof(uint64_t) * (size_t)nb, "output buffer too small");
+  cudaSetDevice(s->ctx->device);
+  VT_CUDA(cudaMemcpy(out, s->bricks, sizeof(uint64_t) * (size_t)nb, cudaMemcpyDeviceToHost), "brick readback");
+  return VT_OK;
+}
+
+extern "C" int vt_diag_check_word(vt_context* ctx, uint32_t* word, int32_t* enabled) {
+  VT_CHECK_ARG(ctx && word && enabled, "null argument");
+  cudaSetDevice(ctx->device);
+  VT_CUDA(cudaStreamSynchronize(ctx->stream), "check word");
+  bool on = false;
+  VT_CUDA(read_check_word(word, &on, true), "check word");
+  *enabled = on ? 1 : 0;
+  return VT_OK;
+}
+
+extern "C" int vt_diag_l2_read_bandwidth(vt_context* ctx, int64_t bytes, int32_t reps, double* gbs) {
+  VT_CHECK_ARG(ctx && gbs && reps > 0 && bytes >= (1 << 20) && bytes <= ((int64_t)1 << 30) && bytes % 16 == 0,
+               "bytes must be a multiple of 16 in [1 MiB, 1 GiB] and reps > 0");
+  cudaSetDevice(ctx->device);
+  const int blocks = ctx->sm_count * 4;
+  const size_t out_bytes = (size_t)blocks * 512 * sizeof(uint4);
+  void* buf = nullptr;
+  void* out = nullptr;
+  int rc = ctx->alloc(&buf, (size_t)bytes);
+  if (rc != VT_OK) return rc;
+  rc = ctx->alloc(&out, out_bytes);
+  if (rc != VT_OK) { ctx->release(buf); return rc; }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  float ms = 0.0f;
+  cudaError_t e = cudaMemsetAsync(buf, 0x5a, (size_t)bytes, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  const uint32_t n = (uint32_t)(bytes / 16);
+  // one warm sweep brings the buffer into L2, then the timed launch
+  if (e == cudaSuccess) e = launch_l2_read((const uint4*)buf, n, 1, (uint4*)out, blocks, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, ctx->stream);
+  if (e == cudaSuccess) e = launch_l2_read((const uint4*)buf, n, reps, (uint4*)out, blocks, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  ctx->release(out);
+  ctx->release(buf);
+  if (e != cudaSuccess) return cuda_fail(e, "l2 read sweep");
+  *gbs = (double)bytes * reps / (ms * 1e-3) / 1e9;
+  return VT_OK;
+}
+
 extern "C" int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int32_t w, int32_t h, float* cdf_u,
                                          float* cdf_v, float* integral) {
   VT_CHECK_ARG(ctx && func && cdf_u && cdf_v && w > 0 && h > 0, "bad argument");
@@ -1842,6 +2017,16 @@ extern "C" int vt_diag_set_tuning(vt_context* ctx, int64_t slots, int32_t blocks
   if (blocks_per_sm >= 0) ctx->trace_blocks_per_sm = blocks_per_sm;
   if (steps > 0) ctx->trace_steps = steps <= 8 ? 8 : (steps <= 16 ? 16 : 32);
   if (max_items > 0) ctx->max_items = std::max<int64_t>(1024, max_items);
+  return VT_OK;
+}
+
+extern "C" int vt_diag_set_trace_tuning(vt_context* ctx, int32_t queue_chunk, int32_t refill_min) {
+  VT_CHECK_ARG(ctx, "context is null");
+  VT_CHECK_ARG(queue_chunk <= 0 || (queue_chunk >= 32 && queue_chunk <= 1024 && queue_chunk % 32 == 0),
+               "queue_chunk must be a multiple of 32 in [32, 1024]");
+  VT_CHECK_ARG(refill_min < 0 || refill_min <= 32, "refill_min must be in [0, 32]");
+  if (queue_chunk > 0) ctx->trace_chunk = queue_chunk;
+  if (refill_min >= 0) ctx->refill_min = refill_min;
   return VT_OK;
 }
 

@@ -41,36 +41,51 @@ static __device__ __align__(256) unsigned char g_fixed_scratch[kTotal];
 static std::mutex g_fixed_mu;
 static void* g_fixed_base[kMaxDevices];
 
-// Device address of g_fixed_scratch on the current device, looked up on the
-// first call per device.
-static int fixed_base(int device, char** out) {
+// Looks up the device address of g_fixed_scratch with `device` current and
+// keeps it for that device.  The CUDA runtime loads this file's device code
+// (and so reserves the array) lazily, at the first use of one of its
+// symbols; vt_create calls this for its device so that the reservation, and
+// any failure to make it, happens there rather than in a frame loop.  Each
+// vt_create looks the address up again, so a context created after a
+// cudaDeviceReset never sees an address from before the reset.
+int vt::fixed_scratch_setup(int device) {
   if (device < 0 || device >= kMaxDevices)
     return fail(VT_EINVAL, "device %d is beyond the %d devices vt_render_batch_fixed supports", device, kMaxDevices);
   std::lock_guard<std::mutex> lock(g_fixed_mu);
-  if (!g_fixed_base[device]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_fixed_scratch);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress of the fixed scratch array");
-    g_fixed_base[device] = p;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_fixed_scratch);
+  if (e != cudaSuccess) {
+    g_fixed_base[device] = nullptr;
+    return cuda_fail(e, "cudaGetSymbolAddress of the fixed scratch array");
   }
+  g_fixed_base[device] = p;
+  return VT_OK;
+}
+
+// Device address of g_fixed_scratch on the current device (set up by
+// vt_create, or here if that set-up failed).
+static int fixed_base(int device, char** out) {
+  if (device < 0 || device >= kMaxDevices)
+    return fail(VT_EINVAL, "device %d is beyond the %d devices vt_render_batch_fixed supports", device, kMaxDevices);
+  {
+    std::lock_guard<std::mutex> lock(g_fixed_mu);
+    if (g_fixed_base[device]) { *out = (char*)g_fixed_base[device]; return VT_OK; }
+  }
+  const int rc = vt::fixed_scratch_setup(device);
+  if (rc != VT_OK) return rc;
+  std::lock_guard<std::mutex> lock(g_fixed_mu);
   *out = (char*)g_fixed_base[device];
   return VT_OK;
 }
 
-static Grid fixed_grid(const vt_job* j) {
-  Grid g;
-  memset(&g, 0, sizeof(g));
-  const Frame& F = j->frame;
-  g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
-  g.bx = F.bdim[0] + 2;
-  g.bxy = (F.bdim[0] + 2) * (F.bdim[1] + 2);
-  g.max_steps = F.max_steps;
-  g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
-  g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
-  g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
-  g.bricks = j->dev.bricks + 1 + g.bx + g.bxy;   // brick (0,0,0) of the padded array
-  return g;
+// A failure after work was queued: wait for that work (it may still use the
+// shared array) before the error goes back to the caller.
+static int drain(vt_context* ctx, int rc) {
+  cudaStreamSynchronize(ctx->stream);
+  return rc;
 }
+
+static Grid fixed_grid(const vt_job* j) { return make_grid(j->frame, j->dev.bricks); }
 
 // One wavefront launch over entries[0..n) with `items` samples in total.
 static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, const Grid* grids, int n,
@@ -93,37 +108,39 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   P.n_items = (unsigned long long)items;
   P.sbuf = (float4*)(base + kSamplesOff);
   P.counters = nullptr;
+  P.trace_chunk = (uint32_t)ctx->trace_chunk;
+  P.refill_min = ctx->refill_min;
   // pageable sources: both copies have read the host tables when they return
   cudaError_t e = cudaMemcpyAsync(d_jobs, entries, sizeof(JobEntry) * n, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_fail(e, "fixed job table");
+  if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed job table"));
   e = cudaMemcpyAsync(d_grids, grids, sizeof(Grid) * n, cudaMemcpyHostToDevice, st);
-  if (e != cudaSuccess) return cuda_fail(e, "fixed grid table");
+  if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed grid table"));
   e = cudaMemsetAsync(ctl, 0, kCtlBytes, st);
-  if (e != cudaSuccess) return cuda_fail(e, "fixed control words");
+  if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed control words"));
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
   const int bps = ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy;
   const int trace_blocks = ctx->sm_count * bps;
   for (int64_t iter = 0;; ++iter) {
     const int par = (int)(iter & 1);
     e = cudaMemsetAsync(ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return cuda_fail(e, "fixed round counters");
+    if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed round counters"));
     e = launch_wf_shade(P, par, ctx->sm_count * 8, false, st);
-    if (e != cudaSuccess) return cuda_fail(e, "fixed wavefront shade");
+    if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed wavefront shade"));
     e = launch_wf_trace(P, par, trace_blocks, ctx->trace_steps, false, st);
-    if (e != cudaSuccess) return cuda_fail(e, "fixed wavefront trace");
+    if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed wavefront trace"));
     ctx->launches += 4;
     if ((iter & 7) == 7) {
       uint32_t live = 0;   // pageable: the copy has completed when it returns
       e = cudaMemcpyAsync(&live, ctl + ctl_index(par, CTL_NEXT_N), sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) return cuda_fail(e, "fixed live count");
+      if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed live count"));
       if (live == 0) break;
     }
   }
   long long max_pixels = 0;
   for (int i = 0; i < n; ++i) max_pixels = std::max<long long>(max_pixels, entries[i].n_pixels);
   e = launch_wf_accumulate(d_jobs, n, max_pixels, P.sbuf, st);
-  if (e != cudaSuccess) return cuda_fail(e, "fixed accumulate");
+  if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed accumulate"));
   ctx->launches += 1;
   return VT_OK;
 }
@@ -164,7 +181,7 @@ extern "C" int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs, int32
     if (jobs[i]->integrator == VT_INTEGRATOR_PATH_TRACER) continue;
     for (int32_t k = 0; k < np[i]; ++k) {
       e = launch_plain(jobs[i]->frame, jobs[i]->dev, jobs[i]->samples + k, 1, nullptr, ctx->stream);
-      if (e != cudaSuccess) return cuda_fail(e, "fixed edit-mode pass");
+      if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed edit-mode pass"));
     }
     ctx->launches += (uint64_t)np[i];
     done[i] = np[i];
@@ -199,7 +216,7 @@ extern "C" int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs, int32
       ++n;
     }
     rc = fixed_launch(ctx, base, entries, grids, n, items, slots_cap);
-    if (rc != VT_OK) return rc;
+    if (rc != VT_OK) return rc;   // fixed_launch has drained the stream
   }
   e = cudaStreamSynchronize(ctx->stream);   // the array is free for the next call
   if (e != cudaSuccess) return cuda_fail(e, "fixed render");

@@ -4,8 +4,10 @@
 //   grid     uint8[rx*ry*rz]        palette entry + 1 per voxel, 0 = empty,
 //                                   linear index x + y*rx + z*rx*ry
 //   bricks   uint64[(bx+2)*(by+2)*(bz+2)]  occupancy bit-bricks: one 64-bit word
-//                                   per 4x4x4 voxel block, bit (x&3)|(y&3)<<2|(z&3)<<4,
-//                                   bx = ceil(rx/4) ...; a border of one brick on
+//                                   per block of 2^sx x 2^sy x 2^sz voxels (the
+//                                   scene's brick shape, sx+sy+sz = 6; 4x4x4 by
+//                                   default), bit (x&mx)|(y&my)<<sx|(z&mz)<<(sx+sy),
+//                                   bx = ceil(rx/2^sx) ...; a border of one brick on
 //                                   every side has all bits set, as do voxels of
 //                                   the last bricks beyond the volume, so that a
 //                                   ray leaving the volume stops on a set bit
@@ -39,6 +41,7 @@ struct Frame {
   float vsize[3];            // (bmax-bmin)/res
   float vext[3];             // 1/(bmax-bmin), dda.h:16
   int32_t bdim[3];           // brick grid dimensions
+  int32_t bsh[3];            // log2 of a brick's extent along x, y, z (sum 6)
   float viewport[4];
   float frag_z;              // gl_FragCoord.z of the full-screen quad drawn at z = near
   float proj[16];            // row-major, as uploaded with transpose = GL_TRUE
@@ -54,6 +57,8 @@ struct Frame {
   float env_integral;
   int32_t env_w;
   int32_t env_h;
+  int32_t env_cdf_w;         // size of the image the CDFs describe (env_w x env_h, or
+  int32_t env_cdf_h;         // the reference's shrunk size)
   int32_t n_emissive;
   int32_t max_bounces;
   int32_t rr_start;
@@ -71,9 +76,26 @@ struct Frame {
   int32_t width;
   int32_t height;
   int32_t integrator;        // 0 path tracer (pathTracer.fs), 1 edit mode (editMode.fs)
+  int32_t n_palette;         // palette entries (bounds of the checked build)
 };
 
 // What the DDA needs of a volume: extents, bounds, brick layout, step cap.
+struct Grid;
+// Shape of a scene's bricks: log2 extents, sx + sy + sz = 6.
+struct BrickShape {
+  int32_t sx, sy, sz;
+};
+__host__ __device__ __forceinline__ int brick_bit_of(const BrickShape& b, int x, int y, int z) {
+  return (x & ((1 << b.sx) - 1)) | ((y & ((1 << b.sy) - 1)) << b.sx) | ((z & ((1 << b.sz) - 1)) << (b.sx + b.sy));
+}
+// Index in the padded brick array (bx, by bricks inside the border) of the
+// brick holding voxel (x, y, z), for voxels from -1 up to the volume's extent.
+__host__ __device__ __forceinline__ int64_t brick_index_of(const BrickShape& b, int32_t bx, int32_t by, int x, int y,
+                                                          int z) {
+  return (int64_t)((x >> b.sx) + 1) + (int64_t)(bx + 2) * ((int64_t)((y >> b.sy) + 1) +
+                                                           (int64_t)(by + 2) * (int64_t)((z >> b.sz) + 1));
+}
+
 struct Grid {
   int32_t rx, ry, rz;
   int32_t bx, bxy;           // padded brick-grid row and slice strides
@@ -81,9 +103,35 @@ struct Grid {
   float bminx, bminy, bminz;
   float vextx, vexty, vextz; // 1/(bmax-bmin), dda.h:16
   float bmaxx, bmaxy, bmaxz;
-  int32_t pad;
+  int32_t shx, shy, shz;     // log2 of the brick extents
+  int32_t shxy;              // shx + shy: bit of a brick's first z layer
+  int32_t mx, my, mz;        // brick extents - 1
+  int32_t n_words;           // words of the padded brick array (bounds of the checked build)
   const unsigned long long* bricks;   // brick (0,0,0) of the padded array
 };
+
+// Bit of voxel (x, y, z) in its brick word (brick shape shifts and masks).
+__host__ __device__ __forceinline__ int brick_bit(int x, int y, int z, int shx, int shxy, int mx, int my, int mz) {
+  return (x & mx) | ((y & my) << shx) | ((z & mz) << shxy);
+}
+
+// The DDA's view of a volume (frame uniforms + the job's brick array).
+__host__ __device__ __forceinline__ Grid make_grid(const Frame& F, const unsigned long long* bricks) {
+  Grid g;
+  g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
+  g.bx = F.bdim[0] + 2; g.bxy = (F.bdim[0] + 2) * (F.bdim[1] + 2);
+  g.max_steps = F.max_steps;
+  g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
+  g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
+  g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
+  g.shx = F.bsh[0]; g.shy = F.bsh[1]; g.shz = F.bsh[2];
+  g.shxy = F.bsh[0] + F.bsh[1];
+  g.mx = (1 << F.bsh[0]) - 1; g.my = (1 << F.bsh[1]) - 1; g.mz = (1 << F.bsh[2]) - 1;
+  const long long nw = (long long)g.bxy * (F.bdim[2] + 2);
+  g.n_words = nw < 0x7fffffffLL ? (int32_t)nw : 0x7fffffff;
+  g.bricks = bricks + 1 + g.bx + g.bxy;   // brick (0,0,0) inside the border
+  return g;
+}
 
 // Device pointers of everything one job reads and writes.
 struct JobDev {

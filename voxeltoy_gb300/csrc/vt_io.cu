@@ -395,3 +395,41 @@ extern "C" int vt_image_encode_pfm(const float* pixels, int32_t width, int32_t h
       }
   return VT_OK;
 }
+
+// Radiance RGBE (Ward, "Real Pixels", Graphics Gems II, 1991): the shared
+// exponent of the largest channel, each channel's mantissa scaled to 8 bits.
+// Negative and NaN channels are written as 0; infinities as the largest value.
+static void to_rgbe(float r, float g, float b, uint8_t* o) {
+  const float big = 1.0e38f;   // below 2^127, the largest shared exponent a byte holds
+  auto clean = [big](float v) { return v > 0.0f ? (v < big ? v : big) : 0.0f; };   // NaN fails v > 0
+  r = clean(r); g = clean(g); b = clean(b);
+  const float v = std::max(r, std::max(g, b));
+  if (v < 1e-32f) { o[0] = o[1] = o[2] = o[3] = 0; return; }
+  int e = 0;
+  const double m = std::frexp((double)v, &e);   // v = m * 2^e, m in [0.5, 1)
+  const double scale = m * 256.0 / (double)v;
+  o[0] = (uint8_t)std::min(255.0, (double)r * scale);
+  o[1] = (uint8_t)std::min(255.0, (double)g * scale);
+  o[2] = (uint8_t)std::min(255.0, (double)b * scale);
+  o[3] = (uint8_t)(e + 128);
+}
+
+extern "C" int vt_image_encode_hdr(const float* pixels, int32_t width, int32_t height, int32_t channels,
+                                   uint8_t* out, size_t out_bytes, size_t* written) {
+  if (!pixels || !written || width <= 0 || height <= 0 || (channels != 3 && channels != 4))
+    return fail(VT_EINVAL, "bad argument");
+  char head[128];
+  const int hl = snprintf(head, sizeof(head), "#?RADIANCE\nFORMAT=32-bit_rle_rgbe\n\n-Y %d +X %d\n", height, width);
+  const size_t need = (size_t)hl + (size_t)width * height * 4;
+  *written = need;
+  if (!out) return VT_OK;   // size query
+  if (out_bytes < need) return fail(VT_EINVAL, "output buffer smaller than %zu bytes", need);
+  memcpy(out, head, (size_t)hl);
+  uint8_t* o = out + hl;
+  for (int32_t y = height - 1; y >= 0; --y)   // rows bottom first in memory, top first in the file
+    for (int32_t x = 0; x < width; ++x, o += 4) {
+      const float* px = pixels + ((size_t)y * width + x) * channels;
+      to_rgbe(px[0], px[1], px[2], o);
+    }
+  return VT_OK;
+}

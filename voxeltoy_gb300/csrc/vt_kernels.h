@@ -30,10 +30,10 @@ cudaError_t launch_diag(const Frame& F, const JobDev& J, int sample, float4* out
 struct WfState {
   float4* a0;      // ro.xyz, -
   float4* a1;      // rd.xyz, item (uint bits)
-  float4* a2;      // sd.xyz, -
   float4* a3;      // L.xyz, rng word
   float4* a4;      // T.xyz, bsdf_pdf
-  float4* a5;      // nee_P.xyz (throughput * light sample), light (int bits)
+  float4* a5;      // nee_P.xyz (throughput * light sample), light (int bits); written and
+                   // read only for paths with a shadow segment
   uint32_t* flags; // bounces | primary | has_cont | ext | shadow | active | NEE mask | job
 };
 // The hits k_wf_shade keeps for k_wf_hit, in hit-list order: Lambert hits
@@ -72,10 +72,13 @@ struct WfParams {
   unsigned long long n_items;
   float4* sbuf;                    // per-item sample outputs
   unsigned long long* counters;    // nullable
+  uint32_t trace_chunk;            // queue records a trace warp takes per atomic (32-256)
+  int32_t refill_min;              // trace warps refill early once fewer lanes step (0 = every
+                                   // kTraceSteps steps only)
 };
 // Device bytes per stream position, and the carving of one allocation of
 // slots * kWfSlotBytes bytes (256-byte aligned) into the buffers of P.
-constexpr size_t kWfSlotBytes = 2 * (6 * sizeof(float4) + sizeof(uint32_t)) + 2 * sizeof(int4) +
+constexpr size_t kWfSlotBytes = 2 * (5 * sizeof(float4) + sizeof(uint32_t)) + 2 * sizeof(int4) +
                                 (4 * sizeof(float4) + sizeof(int4)) + 8 * sizeof(float4);
 void wf_carve(void* mem, size_t slots, WfParams& P);
 // Launches of at most kWfParamJobs jobs pass their job and grid records as a
@@ -116,13 +119,19 @@ cudaError_t launch_resolve(const float4* sum, int32_t w, int32_t h, int32_t samp
                            float inv_gamma, uint32_t flags, float4* out, cudaStream_t st);
 cudaError_t launch_builtins(int32_t fn, const float* a, const float* b, float* out, int64_t n,
                             cudaStream_t st);
+// `reps` L1-bypassing read sweeps of buf (n 16-byte words, n < 2^31) by
+// `blocks` blocks of 512 threads; out holds blocks*512 words.
+cudaError_t launch_l2_read(const uint4* buf, uint32_t n, int32_t reps, uint4* out, int blocks, cudaStream_t st);
+// Check word of the bounds-checked build (VT_CHECKED); release builds give
+// 0 and enabled = false.
+cudaError_t read_check_word(uint32_t* word, bool* enabled, bool reset);
 
 // ---- scene (vt_scene.cu)
 cudaError_t launch_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t rx, int32_t ry, int32_t bx, int32_t by,
-                             int32_t x, int32_t y, int32_t z, uint8_t entry, cudaStream_t st);
+                             const BrickShape& sh, int32_t x, int32_t y, int32_t z, uint8_t entry, cudaStream_t st);
 // max_entry (nullable): receives the largest palette entry of the volume.
 cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
-                                unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
+                                unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz, const BrickShape& sh,
                                 unsigned long long* max_entry, cudaStream_t st);
 cudaError_t launch_emissive_flags(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
                                   const int32_t* emissive, int64_t n, uint8_t* keep, cudaStream_t st);
@@ -146,17 +155,32 @@ struct EnvScratch {
   double* row_int;   // h row integrals
   double* marg_pre;  // h+1 marginal prefix sums
 };
-// bad: set to the smallest index of a non-finite texel (the caller sets it to ~0 first)
-cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, const EnvScratch& S, uint2* texels,
-                             float* cdf_u, float* cdf_v, float* integral, uint32_t* bad, cudaStream_t st);
+// FP16 texels of the w x h image, and the CDFs and integral of the cw x ch
+// image (the same image, or it shrunk by k_env_shrink_lum; sin_theta holds
+// ch row weights).  bad: set to the smallest index of a non-finite texel
+// (the caller sets it to ~0 first).
+cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, int32_t cw, int32_t ch, const EnvScratch& S,
+                             uint2* texels, float* cdf_u, float* cdf_v, float* integral, uint32_t* bad,
+                             cudaStream_t st);
 // CDFs of a caller-supplied function (w*h floats) without blur or weighting.
 cudaError_t launch_cdf(const float* func, int32_t w, int32_t h, const EnvScratch& S, float* cdf_u,
                        float* cdf_v, float* integral, cudaStream_t st);
 // mode 0 = THIN, 1 = FAT; reference_bounds clamps each triangle's swizzled
 // voxel range against the unswizzled resolution as the reference does.
+// bricks (nullable): the padded brick grid (bx, by bricks per row / slice
+// inside the border), prepared by launch_bricks_init; every voxel written
+// also sets its occupancy bit.  scratch: voxelize_scratch_bytes(n_tris)
+// bytes of device memory for the list of large triangles; large_blocks:
+// blocks of the block-per-triangle kernel.
+size_t voxelize_scratch_bytes(int64_t n_tris);
 cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indices, int64_t n_tris,
                             int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
-                            uint8_t* grid, uint8_t value, cudaStream_t st);
+                            uint8_t* grid, uint8_t value, unsigned long long* bricks, int32_t bx, int32_t by,
+                            const BrickShape& sh, void* scratch, int large_blocks, cudaStream_t st);
+// Bricks of an empty volume: border bricks all set, interior bricks set only
+// for the voxels beyond the volume's extent.
+cudaError_t launch_bricks_init(unsigned long long* bricks, int32_t rx, int32_t ry, int32_t rz, int32_t bx,
+                               int32_t by, int32_t bz, const BrickShape& sh, cudaStream_t st);
 cudaError_t launch_transform_vertices(const float* in, int64_t n, const float* m44_row_major,
                                       int32_t rx, int32_t ry, int32_t rz, float* out, cudaStream_t st);
 

@@ -136,9 +136,10 @@ __device__ __forceinline__ int job_of(const WfParams& P, const Tab& T, unsigned 
   return lo;
 }
 
-// Path state (WfState): a0 = (ro, -), a1 = (rd, item), a2 = (sd, -),
-// a3 = (L, rng), a4 = (T, bsdf_pdf), a5 = (nee_P, light); the job, bounces
-// and flag bits live in `flags`, and pixel and sample follow from the item.
+// Path state (WfState): a0 = (ro, -), a1 = (rd, item), a3 = (L, rng),
+// a4 = (T, bsdf_pdf), a5 = (nee_P, light) for paths with a shadow segment;
+// the job, bounces and flag bits live in `flags`, and pixel and sample
+// follow from the item.
 // k_wf_shade reads what ending a segment needs (a1, a3, a4, a5 for a shadow
 // result, a0 for a hit it keeps) and copies kept hits into hit records;
 // k_wf_hit reads only the hit records.
@@ -175,14 +176,16 @@ __device__ __forceinline__ void rng_from_item(const JobEntry& E, uint32_t item, 
   else { p.rng.call = rng; p.rng.ox = p.rng.oy = 0; }
 }
 
-__device__ __forceinline__ void store_path(const WfState& st, int i, const Frame& F, const Path& p, uint32_t item) {
+// The state the next round's shading reads (the shadow direction is only
+// needed for the segment record written beside it, so it is not stored).
+__device__ __forceinline__ void store_path(const WfState& st, int i, const Frame& F, const Path& p, uint32_t item,
+                                           bool shadow) {
   const uint32_t rng = (F.rng_mode == 1) ? ((uint32_t)p.rng.ox | ((uint32_t)p.rng.oy << 16)) : p.rng.call;
   st.a0[i] = pack4(p.ro, 0.0f);
   st.a1[i] = pack4(p.rd, __uint_as_float(item));
-  st.a2[i] = pack4(p.sd, 0.0f);
   st.a3[i] = pack4(p.L, __uint_as_float(rng));
   st.a4[i] = pack4(p.T, p.bsdf_pdf);
-  st.a5[i] = pack4(p.nee_P, __int_as_float(p.light));
+  if (shadow) st.a5[i] = pack4(p.nee_P, __int_as_float(p.light));
 }
 
 // Block-wide reservation on N counters with one atomic per counter and
@@ -302,7 +305,7 @@ __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __
       if (hit) cls = hit_class(E.F, E.J, e);
     }
     if (hit) p.ro = xyz4(src.a0[i]);
-    else P.sbuf[item] = path_output(E.F, p);
+    else if (chk(item < P.n_items, CHK_SAMPLE)) P.sbuf[item] = path_output(E.F, p);
   }
   uint32_t* const ctr[2] = {&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)], &P.ctl[ctl_index(par, CTL_HITS_OTHER)]};
   const uint32_t cnt_l = (hit && cls == 0) ? 1u : 0u, cnt_o = (hit && cls != 0) ? 1u : 0u;
@@ -364,7 +367,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
     block_reserve<1>(ctr, nn, base);
     write_segments(P, par, base[0], emit, (int)v, job, p.ro, p);
     if (mine) {
-      store_path(dst, (int)v, job_entry(P, T, job).F, p, item);
+      store_path(dst, (int)v, job_entry(P, T, job).F, p, item, (emit & 2u) != 0);
       dst.flags[v] = slot_flags(p, emit, job);
     }
   }
@@ -425,7 +428,8 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
             active = true;
             need_new = false;
           } else {
-            P.sbuf[item] = path_output(E.F, p);   // missed the volume: finished, take another item
+            if (chk(item < P.n_items, CHK_SAMPLE))
+              P.sbuf[item] = path_output(E.F, p);   // missed the volume: finished, take another item
           }
         }
       }
@@ -444,7 +448,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
     block_reserve<1>(ctr, nn, base);
     write_segments(P, par, base[0], active ? 1u : 0u, (int)pos, job, o, p);
     if (active) {
-      store_path(dst, (int)pos, job_entry(P, T, job).F, p, item);
+      store_path(dst, (int)pos, job_entry(P, T, job).F, p, item, false);   // a primary path has no shadow segment
       dst.flags[pos] = slot_flags(p, 1u, job);
     } else if (mine) {
       dst.flags[pos] = 0u;
@@ -468,13 +472,12 @@ struct GridHold<WfOneJob> {
 };
 
 // One round of tracing: every queued segment runs its DDA to the end.  Each
-// warp takes chunks of queue records with one atomic and hands them to its
-// lanes; every lane keeps the record of its next segment loaded while it
-// steps the current one, so starting a segment never waits on memory, and
-// lanes pick up a new segment every kTraceSteps steps as theirs finish.
-constexpr uint32_t kTraceChunk = 128;
-
-template <bool kCount, int kTraceSteps, class Tab>
+// warp takes chunks of P.trace_chunk queue records with one atomic and hands
+// them to its lanes; every lane keeps the record of its next segment loaded
+// while it steps the current one, so starting a segment never waits on
+// memory, and lanes pick up a new segment every kTraceSteps steps as theirs
+// finish (with kVote also as soon as fewer than P.refill_min lanes step).
+template <bool kCount, int kTraceSteps, bool kVote, class Tab>
 __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -504,11 +507,11 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
     while (need && !exhausted) {          // prefetch next records
       if (pool >= pool_end) {
         uint32_t c = 0;
-        if (lane == 0) c = atomicAdd(&P.ctl[ctl_index(par, CTL_QHEAD)], kTraceChunk);
+        if (lane == 0) c = atomicAdd(&P.ctl[ctl_index(par, CTL_QHEAD)], P.trace_chunk);
         c = __shfl_sync(FULL, c, 0);
         if (c >= n) { exhausted = true; break; }
         pool = c;
-        pool_end = min(c + kTraceChunk, n);
+        pool_end = min(c + P.trace_chunk, n);
       }
       const uint32_t avail = pool_end - pool;
       const uint32_t r = __popc(need & lt);
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
     }
     if (__ballot_sync(FULL, have || have_next) == 0u) break;
     if (have) {
-      dda_advance(gh.get(T), s, kTraceSteps, cnt);
+      dda_advance<kCount, kVote>(gh.get(T), s, kTraceSteps, cnt, P.refill_min);
       if (s.state != DDA_RUNNING) {
         P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
         have = false;
@@ -573,12 +576,18 @@ cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool
   return cudaGetLastError();
 }
 
+template <bool kVote, class Tab>
+static void wf_trace_steps(const WfParams& P, const Tab& T, int par, int blocks, int steps, cudaStream_t st) {
+  if (steps <= 8) k_wf_trace<false, 8, kVote, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else if (steps <= 16) k_wf_trace<false, 16, kVote, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else k_wf_trace<false, 32, kVote, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+}
+
 template <class Tab>
 static void wf_trace(const WfParams& P, const Tab& T, int par, int blocks, int steps, bool count, cudaStream_t st) {
-  if (count) k_wf_trace<true, 16, Tab><<<blocks, 256, 0, st>>>(P, T, par);
-  else if (steps <= 8) k_wf_trace<false, 8, Tab><<<blocks, 256, 0, st>>>(P, T, par);
-  else if (steps <= 16) k_wf_trace<false, 16, Tab><<<blocks, 256, 0, st>>>(P, T, par);
-  else k_wf_trace<false, 32, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  if (count) k_wf_trace<true, 16, false, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else if (P.refill_min > 0) wf_trace_steps<true>(P, T, par, blocks, steps, st);
+  else wf_trace_steps<false>(P, T, par, blocks, steps, st);
 }
 
 cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,
@@ -601,8 +610,8 @@ void wf_carve(void* mem, size_t S, WfParams& P) {
   float4* f = (float4*)mem;
   for (int s = 0; s < 2; ++s) {
     WfState& x = P.x[s];
-    x.a0 = f; x.a1 = f + S; x.a2 = f + 2 * S; x.a3 = f + 3 * S; x.a4 = f + 4 * S; x.a5 = f + 5 * S;
-    f += 6 * S;
+    x.a0 = f; x.a1 = f + S; x.a3 = f + 2 * S; x.a4 = f + 3 * S; x.a5 = f + 4 * S;
+    f += 5 * S;
   }
   P.hr.h0 = f; P.hr.h1 = f + S; P.hr.h2 = f + 2 * S; P.hr.h3 = f + 3 * S;
   f += 4 * S;
@@ -619,7 +628,7 @@ void wf_carve(void* mem, size_t S, WfParams& P) {
 
 int wf_trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8, WfJobTable>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8, false, WfJobTable>, 256, 0);
   return n;
 }
 
@@ -769,4 +778,66 @@ cudaError_t launch_builtins(int32_t fn, const float* a, const float* b, float* o
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------ L2 read bandwidth
+// `reps` sweeps of an L2-resident buffer in one launch, loads bypassing L1
+// (ld.global.cg), four independent 16-byte loads in flight per thread; the
+// XOR of everything read is stored per thread so that no load is dropped.
+// Each sweep starts one grid-width further on, so a thread does not read
+// the same lines in consecutive sweeps.
+__global__ void __launch_bounds__(512) k_l2_read(const uint4* __restrict__ buf, uint32_t n, int32_t reps,
+                                                 uint4* __restrict__ out) {
+  const uint32_t T = gridDim.x * blockDim.x;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+  for (int32_t r = 0; r < reps; ++r) {
+    const uint32_t base = (uint32_t)(((uint64_t)r * T + t) % n);
+    uint32_t i = 0;
+    for (; i + 3 * T < n; i += 4 * T) {
+      uint4 v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        uint32_t j = base + i + (uint32_t)k * T;
+        if (j >= n) j -= n;
+        v[k] = __ldcg(&buf[j]);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) { acc.x ^= v[k].x; acc.y ^= v[k].y; acc.z ^= v[k].z; acc.w ^= v[k].w; }
+    }
+    for (; i < n; i += T) {
+      uint32_t j = base + i;
+      if (j >= n) j -= n;
+      const uint4 v = __ldcg(&buf[j]);
+      acc.x ^= v.x; acc.y ^= v.y; acc.z ^= v.z; acc.w ^= v.w;
+    }
+  }
+  out[t] = acc;
+}
+
+cudaError_t launch_l2_read(const uint4* buf, uint32_t n, int32_t reps, uint4* out, int blocks, cudaStream_t st) {
+  if (n == 0 || reps <= 0 || blocks <= 0) return cudaSuccess;
+  k_l2_read<<<blocks, 512, 0, st>>>(buf, n, reps, out);
+  return cudaGetLastError();
+}
+
+}  // namespace vt
+
+namespace vt {
+// The check word of the bounds-checked build (0 and enabled = false in a
+// release build); reset clears it after reading.
+cudaError_t read_check_word(uint32_t* word, bool* enabled, bool reset) {
+#ifdef VT_CHECKED
+  *enabled = true;
+  cudaError_t e = cudaMemcpyFromSymbol(word, g_check_word, sizeof(uint32_t));
+  if (e == cudaSuccess && reset) {
+    const uint32_t zero = 0;
+    e = cudaMemcpyToSymbol(g_check_word, &zero, sizeof(uint32_t));
+  }
+  return e;
+#else
+  *enabled = false;
+  *word = 0;
+  (void)reset;
+  return cudaSuccess;
+#endif
+}
 }  // namespace vt

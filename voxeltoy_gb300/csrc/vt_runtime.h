@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <mutex>
 #include <unordered_map>
@@ -41,6 +42,8 @@ struct vt_context {
   int trace_blocks_per_sm = 0;   // 0 = occupancy limit
   int trace_occupancy = 0;       // occupancy limit of the DDA kernel (cached)
   int trace_steps = 16;          // DDA steps between refills of the trace kernel
+  int trace_chunk = 128;         // queue records per warp atomic of the trace kernel
+  int refill_min = 0;            // early refill of a trace warp below this many stepping lanes (0 = off)
   uint64_t launches = 0;         // render kernels launched by this context
   cudaGraphExec_t rounds_exec = nullptr;   // eight rounds of every lane, replayed
   bool use_graphs = true;
@@ -66,6 +69,7 @@ struct vt_scene {
   vt_context* ctx = nullptr;
   int32_t res[3] = {0, 0, 0};
   int32_t bdim[3] = {0, 0, 0};
+  int32_t bsh[3] = {2, 2, 2};    // brick shape: log2 extents (4x4x4)
   float bmin[3], bmax[3], vsize[3];
   uint8_t* grid = nullptr;
   unsigned long long* bricks = nullptr;
@@ -87,6 +91,7 @@ struct vt_scene {
 struct vt_env {
   vt_context* ctx = nullptr;
   int32_t w = 0, h = 0;
+  int32_t cdf_w = 0, cdf_h = 0;  // image the CDFs were built from (w, h, or the shrunk size)
   uint2* texels = nullptr;
   float* cdf_u = nullptr;
   float* cdf_v = nullptr;
@@ -113,11 +118,23 @@ struct vt_job {
 };
 
 namespace vt {
+// A named host-side range for profilers (NVTX; a no-op unless a tool such as
+// ncu --nvtx is attached): the phases of a render show up as ranges named
+// "vt.<phase>" around the kernels they launch.
+struct Range {
+  explicit Range(const char* name) { nvtxRangePushA(name); }
+  ~Range() { nvtxRangePop(); }
+  Range(const Range&) = delete;
+  Range& operator=(const Range&) = delete;
+};
 int fail(int code, const char* fmt, ...);
 int cuda_fail(cudaError_t e, const char* what);
 int build_frame(vt_job* j);
 // Frees everything a context owns (vt_destroy, and the server's own lane).
 void release_context(vt_context* ctx);
+// Locates vt_render_batch_fixed's device array on `device` (current) and
+// loads the code that holds it (vt_fixed.cu); called by vt_create.
+int fixed_scratch_setup(int device);
 // Rebuilds a job's frame when its scene was edited since (scene->generation).
 int refresh_job(vt_job* j);
 // passes[i] samples per pixel for jobs[i]; kernel 1 = plain, 2 = wavefront.

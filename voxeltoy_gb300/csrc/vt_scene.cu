@@ -3,6 +3,7 @@
 //   environment map's FP16 texels and importance-sampling CDFs (FP64 prefix
 //   sums), and the triangle/voxel-overlap voxelizer.
 #include <cuda_fp16.h>
+#include <algorithm>
 #include "vt_kernels.h"
 #include "vt_builtins.h"
 
@@ -17,20 +18,21 @@ namespace vt {
 // max-ed into *max_entry (the host checks it against the palette size).
 __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int32_t ry, int32_t rz,
                                unsigned long long* __restrict__ bricks, int32_t bx, int32_t by, int32_t bz,
-                               unsigned long long* max_entry) {
+                               const BrickShape sh, unsigned long long* max_entry) {
   const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int64_t px = bx + 2, py = by + 2, pz = bz + 2;
   unsigned top = 0;
   if (b < px * py * pz) {
-    const int x0 = ((int)(b % px) - 1) * 4;
-    const int y0 = ((int)((b / px) % py) - 1) * 4;
-    const int z0 = ((int)(b / (px * py)) - 1) * 4;
-    // rows of four voxels as one aligned 32-bit word where the brick's x
-    // range lies inside the volume and rows start on 4-byte boundaries: the
-    // sixteen row loads are independent
-    const bool words = (rx & 3) == 0 && x0 >= 0 && x0 + 4 <= rx;
+    const int ex = 1 << sh.sx, ey = 1 << sh.sy, ez = 1 << sh.sz;
+    const int x0 = ((int)(b % px) - 1) * ex;
+    const int y0 = ((int)((b / px) % py) - 1) * ey;
+    const int z0 = ((int)(b / (px * py)) - 1) * ez;
     unsigned long long w = 0ull;
     unsigned tops = 0u;   // byte-wise maximum of the word rows
+    // 4x4x4 bricks: rows of four voxels as one aligned 32-bit word where the
+    // brick's x range lies inside the volume and rows start on 4-byte
+    // boundaries; the sixteen row loads are independent
+    const bool words = sh.sx == 2 && sh.sy == 2 && (rx & 3) == 0 && x0 >= 0 && x0 + 4 <= rx;
     if (words) {
 #pragma unroll
       for (int r = 0; r < 16; ++r) {
@@ -45,18 +47,12 @@ __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int
         w |= (unsigned long long)(in ? m : 0xfu) << (4 * r);   // rows outside the volume read as set
       }
     } else {
-      for (int dz = 0; dz < 4; ++dz) {
-        const int z = z0 + dz;
-        for (int dy = 0; dy < 4; ++dy) {
-          const int y = y0 + dy;
-          for (int dx = 0; dx < 4; ++dx) {
-            const int x = x0 + dx;
-            const bool outside = x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz;
-            const unsigned v = outside ? 0u : grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)];
-            top = v > top ? v : top;
-            if (outside || v != 0) w |= 1ull << (dx | (dy << 2) | (dz << 4));
-          }
-        }
+      for (int k = 0; k < 64; ++k) {
+        const int x = x0 + (k & (ex - 1)), y = y0 + ((k >> sh.sx) & (ey - 1)), z = z0 + (k >> (sh.sx + sh.sy));
+        const bool outside = x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz;
+        const unsigned v = outside ? 0u : grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)];
+        top = v > top ? v : top;
+        if (outside || v != 0) w |= 1ull << k;
       }
     }
     for (int k = 0; k < 32; k += 8) top = max(top, (tops >> k) & 0xffu);
@@ -68,27 +64,26 @@ __global__ void k_build_bricks(const uint8_t* __restrict__ grid, int32_t rx, int
 
 // One voxel edit: its grid entry and its bit in the padded brick grid.
 __global__ void k_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t rx, int32_t ry, int32_t bx, int32_t by,
-                            int32_t x, int32_t y, int32_t z, uint8_t entry) {
+                            const BrickShape sh, int32_t x, int32_t y, int32_t z, uint8_t entry) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   grid[(size_t)x + (size_t)rx * ((size_t)y + (size_t)ry * (size_t)z)] = entry;
-  const int64_t px = bx + 2, py = by + 2;
-  const int64_t b = (int64_t)((x >> 2) + 1) + px * ((int64_t)((y >> 2) + 1) + py * (int64_t)((z >> 2) + 1));
-  const unsigned long long bit = 1ull << ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4));
+  const int64_t b = brick_index_of(sh, bx, by, x, y, z);
+  const unsigned long long bit = 1ull << brick_bit_of(sh, x, y, z);
   if (entry) atomicOr(&bricks[b], bit);
   else atomicAnd(&bricks[b], ~bit);
 }
 
 cudaError_t launch_set_voxel(uint8_t* grid, unsigned long long* bricks, int32_t rx, int32_t ry, int32_t bx, int32_t by,
-                             int32_t x, int32_t y, int32_t z, uint8_t entry, cudaStream_t st) {
-  k_set_voxel<<<1, 32, 0, st>>>(grid, bricks, rx, ry, bx, by, x, y, z, entry);
+                             const BrickShape& sh, int32_t x, int32_t y, int32_t z, uint8_t entry, cudaStream_t st) {
+  k_set_voxel<<<1, 32, 0, st>>>(grid, bricks, rx, ry, bx, by, sh, x, y, z, entry);
   return cudaGetLastError();
 }
 
 cudaError_t launch_build_bricks(const uint8_t* grid, int32_t rx, int32_t ry, int32_t rz,
-                                unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz,
+                                unsigned long long* bricks, int32_t bx, int32_t by, int32_t bz, const BrickShape& sh,
                                 unsigned long long* max_entry, cudaStream_t st) {
   const int64_t nb = (int64_t)(bx + 2) * (by + 2) * (bz + 2);
-  k_build_bricks<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(grid, rx, ry, rz, bricks, bx, by, bz, max_entry);
+  k_build_bricks<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(grid, rx, ry, rz, bricks, bx, by, bz, sh, max_entry);
   return cudaGetLastError();
 }
 
@@ -348,16 +343,48 @@ cudaError_t launch_cdf(const float* func, int32_t w, int32_t h, const EnvScratch
   return cudaGetLastError();
 }
 
-cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, const EnvScratch& S, uint2* texels,
-                             float* cdf_u, float* cdf_v, float* integral, uint32_t* bad, cudaStream_t st) {
+// The CDF image of a shrunk environment (image.cpp:308-320): each output
+// texel is the area-weighted average of the FP16 texels its footprint
+// covers (double sums, rows then columns in index order), then its Rec.709
+// luminance.  A box filter standing in for OpenImageIO's resize.
+__global__ void k_env_shrink_lum(const uint2* __restrict__ texels, int32_t w, int32_t h, int32_t ow, int32_t oh,
+                                 float* __restrict__ lum) {
+  const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (o >= (int64_t)ow * oh) return;
+  const int ox = (int)(o % ow), oy = (int)(o / ow);
+  const double sx = (double)w / (double)ow, sy = (double)h / (double)oh;
+  const double y0 = (double)oy * sy, y1 = (double)(oy + 1) * sy;
+  const double x0 = (double)ox * sx, x1 = (double)(ox + 1) * sx;
+  double acc0 = 0.0, acc1 = 0.0, acc2 = 0.0;
+  for (int j = (int)floor(y0); j < (int)ceil(y1) && j < h; ++j) {
+    const double wy = fmin(y1, (double)(j + 1)) - fmax(y0, (double)j);
+    for (int i = (int)floor(x0); i < (int)ceil(x1) && i < w; ++i) {
+      const double wx = fmin(x1, (double)(i + 1)) - fmax(x0, (double)i);
+      const double wgt = wx * wy;
+      const uint2 q = texels[(int64_t)j * w + i];
+      acc0 = acc0 + wgt * (double)vtb::h2f((uint16_t)(q.x & 0xffffu));
+      acc1 = acc1 + wgt * (double)vtb::h2f((uint16_t)(q.x >> 16));
+      acc2 = acc2 + wgt * (double)vtb::h2f((uint16_t)(q.y & 0xffffu));
+    }
+  }
+  const double area = sx * sy;
+  const float fr = (float)(acc0 / area), fg = (float)(acc1 / area), fb = (float)(acc2 / area);
+  lum[o] = (fr * 0.2126f + fg * 0.7152f) + fb * 0.0722f;
+}
+
+cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, int32_t cw, int32_t ch, const EnvScratch& S,
+                             uint2* texels, float* cdf_u, float* cdf_v, float* integral, uint32_t* bad,
+                             cudaStream_t st) {
   const int64_t n = (int64_t)w * h;
-  const unsigned blocks = (unsigned)((n + 255) / 256);
-  k_env_texels<<<blocks, 256, 0, st>>>(rgb, n, texels, S.lum, bad);
-  k_env_blur<<<blocks, 256, 0, st>>>(S.lum, S.tmp, w, h, 0, S.sin_theta);
-  k_env_blur<<<blocks, 256, 0, st>>>(S.tmp, S.func, w, h, 1, S.sin_theta);
+  k_env_texels<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rgb, n, texels, S.lum, bad);
+  const int64_t m = (int64_t)cw * ch;
+  const unsigned blocks = (unsigned)((m + 255) / 256);
+  if (cw != w || ch != h) k_env_shrink_lum<<<blocks, 256, 0, st>>>(texels, w, h, cw, ch, S.lum);
+  k_env_blur<<<blocks, 256, 0, st>>>(S.lum, S.tmp, cw, ch, 0, S.sin_theta);
+  k_env_blur<<<blocks, 256, 0, st>>>(S.tmp, S.func, cw, ch, 1, S.sin_theta);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return launch_cdf(S.func, w, h, S, cdf_u, cdf_v, integral, st);
+  return launch_cdf(S.func, cw, ch, S, cdf_u, cdf_v, integral, st);
 }
 
 // --------------------------------------------------------------- voxelizer
@@ -475,8 +502,18 @@ __device__ bool tri_setup(const float* V, const uint32_t* I, int64_t t, int32_t 
   return S.valid;
 }
 
+// Where a voxelized voxel is recorded: its grid byte and, when the scene's
+// bricks are being built alongside, its bit of the padded brick grid.
+struct VoxOut {
+  uint8_t* grid;
+  uint8_t value;
+  unsigned long long* bricks;   // nullable
+  int32_t bx, by;               // bricks per row / column inside the border
+  BrickShape sh;
+};
+
 __device__ __forceinline__ void tri_column(const TriSetup& S, int px, int py, int mode, int32_t rx, int32_t ry,
-                                           int32_t rz, uint8_t* grid, uint8_t value) {
+                                           int32_t rz, const VoxOut& O) {
   bool xy = true;
   for (int k = 0; k < 3; ++k) {
     const float dd = S.d_xy[k] + (S.n_xy[k][0] * (float)px + S.n_xy[k][1] * (float)py);
@@ -506,7 +543,9 @@ __device__ __forceinline__ void tri_column(const TriSetup& S, int px, int py, in
     else { ox = px; oy = py; oz = pz; }
     // imageStore outside the image has no effect
     if (ox < 0 || oy < 0 || oz < 0 || ox >= rx || oy >= ry || oz >= rz) continue;
-    grid[(size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz)] = value;
+    O.grid[(size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz)] = O.value;
+    if (O.bricks)
+      atomicOr(&O.bricks[brick_index_of(O.sh, O.bx, O.by, ox, oy, oz)], 1ull << brick_bit_of(O.sh, ox, oy, oz));
   }
   (void)mode;
 }
@@ -516,8 +555,8 @@ constexpr int kLargeColumns = 64;
 // One thread per triangle for triangles whose XY footprint is small; larger
 // ones are appended to a list for the block-per-triangle kernel.
 __global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restrict__ I, int64_t n_tris,
-                            int32_t rx, int32_t ry, int32_t rz, int mode, bool ref_bounds, uint8_t* grid,
-                            uint8_t value, int64_t* large, unsigned long long* n_large) {
+                            int32_t rx, int32_t ry, int32_t rz, int mode, bool ref_bounds, const VoxOut O,
+                            int64_t* large, unsigned long long* n_large) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tris) return;
   TriSetup S;
@@ -529,12 +568,12 @@ __global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restr
     return;
   }
   for (int px = S.lo[0]; px < S.hi[0]; ++px)
-    for (int py = S.lo[1]; py < S.hi[1]; ++py) tri_column(S, px, py, mode, rx, ry, rz, grid, value);
+    for (int py = S.lo[1]; py < S.hi[1]; ++py) tri_column(S, px, py, mode, rx, ry, rz, O);
 }
 
 __global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restrict__ I, const int64_t* large,
                             const unsigned long long* n_large, int32_t rx, int32_t ry, int32_t rz, int mode,
-                            bool ref_bounds, uint8_t* grid, uint8_t value) {
+                            bool ref_bounds, const VoxOut O) {
   __shared__ TriSetup S;
   const unsigned long long n = *n_large;
   for (unsigned long long k = blockIdx.x; k < n; k += gridDim.x) {
@@ -545,31 +584,65 @@ __global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restr
     const int64_t cols = (int64_t)wx * wy;
     for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) {
       const int px = S.lo[0] + (int)(c / wy), py = S.lo[1] + (int)(c % wy);
-      tri_column(S, px, py, mode, rx, ry, rz, grid, value);
+      tri_column(S, px, py, mode, rx, ry, rz, O);
     }
   }
 }
 
+size_t voxelize_scratch_bytes(int64_t n_tris) {
+  return (sizeof(int64_t) * (size_t)std::max<int64_t>(n_tris, 1) + 255) / 256 * 256 + 256;
+}
+
 cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indices, int64_t n_tris,
                             int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
-                            uint8_t* grid, uint8_t value, cudaStream_t st) {
+                            uint8_t* grid, uint8_t value, unsigned long long* bricks, int32_t bx, int32_t by,
+                            const BrickShape& sh, void* scratch, int large_blocks, cudaStream_t st) {
   if (n_tris <= 0) return cudaSuccess;
-  int64_t* large = nullptr;
-  unsigned long long* n_large = nullptr;
-  cudaError_t e = cudaMallocAsync(&large, sizeof(int64_t) * n_tris + 16, st);
+  int64_t* large = (int64_t*)scratch;
+  unsigned long long* n_large =
+      (unsigned long long*)((char*)scratch + voxelize_scratch_bytes(n_tris) - 256);   // the last 256 bytes
+  cudaError_t e = cudaMemsetAsync(n_large, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  e = cudaMallocAsync(&n_large, sizeof(unsigned long long), st);
-  if (e != cudaSuccess) { cudaFreeAsync(large, st); return e; }
-  cudaMemsetAsync(n_large, 0, sizeof(unsigned long long), st);
+  VoxOut O;
+  O.grid = grid;
+  O.value = value;
+  O.bricks = bricks ? bricks : nullptr;
+  O.bx = bx;
+  O.by = by;
+  O.sh = sh;
   k_vox_small<<<(unsigned)((n_tris + 127) / 128), 128, 0, st>>>(verts_voxel_space, indices, n_tris, rx, ry, rz,
-                                                                mode, reference_bounds, grid, value, large,
-                                                                n_large);
-  k_vox_large<<<152 * 4, 256, 0, st>>>(verts_voxel_space, indices, large, n_large, rx, ry, rz, mode,
-                                       reference_bounds, grid, value);
-  e = cudaGetLastError();
-  cudaFreeAsync(large, st);
-  cudaFreeAsync(n_large, st);
-  return e;
+                                                                mode, reference_bounds, O, large, n_large);
+  k_vox_large<<<std::max(1, large_blocks), 256, 0, st>>>(verts_voxel_space, indices, large, n_large, rx, ry, rz,
+                                                         mode, reference_bounds, O);
+  return cudaGetLastError();
+}
+
+// One thread per brick of the padded grid: all bits of border bricks, and of
+// interior bricks the bits of voxels at or beyond (rx, ry, rz).
+__global__ void k_bricks_init(unsigned long long* __restrict__ bricks, int32_t rx, int32_t ry, int32_t rz,
+                              int32_t bx, int32_t by, int32_t bz, const BrickShape sh) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t px = bx + 2, py = by + 2, pz = bz + 2;
+  if (b >= px * py * pz) return;
+  const int ex = 1 << sh.sx, ey = 1 << sh.sy, ez = 1 << sh.sz;
+  const int x0 = ((int)(b % px) - 1) * ex;
+  const int y0 = ((int)((b / px) % py) - 1) * ey;
+  const int z0 = ((int)(b / (px * py)) - 1) * ez;
+  unsigned long long w = 0ull;
+  if (x0 < 0 || y0 < 0 || z0 < 0 || x0 + ex > rx || y0 + ey > ry || z0 + ez > rz) {
+    for (int k = 0; k < 64; ++k) {
+      const int x = x0 + (k & (ex - 1)), y = y0 + ((k >> sh.sx) & (ey - 1)), z = z0 + (k >> (sh.sx + sh.sy));
+      if (x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz) w |= 1ull << k;
+    }
+  }
+  bricks[b] = w;
+}
+
+cudaError_t launch_bricks_init(unsigned long long* bricks, int32_t rx, int32_t ry, int32_t rz, int32_t bx,
+                               int32_t by, int32_t bz, const BrickShape& sh, cudaStream_t st) {
+  const int64_t nb = (int64_t)(bx + 2) * (by + 2) * (bz + 2);
+  k_bricks_init<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(bricks, rx, ry, rz, bx, by, bz, sh);
+  return cudaGetLastError();
 }
 
 }  // namespace vt

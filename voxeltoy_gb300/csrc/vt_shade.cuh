@@ -59,6 +59,32 @@ VT_D float4 mul4(const float* m, float4 v) {
   return r;
 }
 
+// ------------------------------------------------------------ checked build
+// With VT_CHECKED every data-dependent gather of the path checks its index;
+// a failed check ORs its bit into this module's check word (read by
+// vt_diag_check_word) and the gather reads a neutral value instead: no
+// trap, the launch runs to its end.  Without VT_CHECKED the checks compile
+// away.
+enum : uint32_t {
+  CHK_BRICK = 1u << 0,     // brick word outside the padded brick array
+  CHK_GRID = 1u << 1,      // voxel outside the volume
+  CHK_PALETTE = 1u << 2,   // palette entry beyond the palette
+  CHK_EMISSIVE = 1u << 3,  // emissive-list entry outside the volume
+  CHK_TEXEL = 1u << 4,     // environment texel outside the image
+  CHK_CDF = 1u << 5,       // CDF entry outside its table
+  CHK_SAMPLE = 1u << 6,    // sample-buffer item beyond the launch's items
+  CHK_NOISE = 1u << 7,     // noise-table texel outside the table
+};
+#ifdef VT_CHECKED
+static __device__ unsigned int g_check_word;
+VT_D bool chk(bool ok, uint32_t code) {
+  if (!ok) atomicOr(&g_check_word, code);
+  return ok;
+}
+#else
+VT_D bool chk(bool, uint32_t) { return true; }
+#endif
+
 // ---------------------------------------------------------------- counters
 template <bool kCount>
 struct Cnt {
@@ -116,7 +142,8 @@ VT_D void rng_init(const Frame& F, Rng& r, int px, int py, int sample) {
 // rand (random.h:20-27) or one Philox block.
 VT_D float4 rng_next(const Frame& F, const JobDev& J, Rng& r) {
   if (F.rng_mode == 1) {
-    const float4 v = __ldg(&J.noise[r.oy * kNoiseW + r.ox]);
+    const float4 v = chk((unsigned)r.ox < (unsigned)kNoiseW && (unsigned)r.oy < (unsigned)kNoiseH, CHK_NOISE)
+                         ? __ldg(&J.noise[r.oy * kNoiseW + r.ox]) : make_float4(0.f, 0.f, 0.f, 0.f);
     r.ox = (r.ox + 1) % kNoiseW;
     if (r.ox == 0) r.oy = (r.oy + 1) % kNoiseH;
     return v;
@@ -134,7 +161,9 @@ struct Mat {
   float roughness;
 };
 VT_D float hf(unsigned short h) { return __half2float(__ushort_as_half(h)); }
-VT_D Mat load_mat(const JobDev& J, int entry) {
+VT_D Mat empty_mat();
+VT_D Mat load_mat(const Frame& F, const JobDev& J, int entry) {
+  if (!chk((unsigned)entry < (unsigned)F.n_palette, CHK_PALETTE)) return empty_mat();
   const uint4 q = __ldg(&J.palette[entry]);
   Mat m;
   m.type = (int)hf((unsigned short)(q.x & 0xffffu));
@@ -154,10 +183,13 @@ VT_D Mat empty_mat() {
 template <bool kCount>
 VT_D Mat voxel_mat(const Frame& F, const JobDev& J, int x, int y, int z, Cnt<kCount>& cnt) {
   cnt.add(C_PALETTE, 1);
-  if (y < 0) return load_mat(J, F.ground_mat);
+  if (y < 0) return load_mat(F, J, F.ground_mat);
+  if (!chk((unsigned)x < (unsigned)F.res[0] && (unsigned)y < (unsigned)F.res[1] && (unsigned)z < (unsigned)F.res[2],
+           CHK_GRID))
+    return empty_mat();
   const uint8_t g = __ldg(&J.grid[(size_t)x + (size_t)F.res[0] * ((size_t)y + (size_t)F.res[1] * (size_t)z)]);
   if (g == 0) return empty_mat();
-  return load_mat(J, (int)g - 1);
+  return load_mat(F, J, (int)g - 1);
 }
 
 // -------------------------------------------------------------------- aabb
@@ -219,17 +251,7 @@ VT_D v3 world_to_local(v3 w, const Basis& b) {
 }
 
 // -------------------------------------------------------------------- dda
-VT_D Grid grid_of(const Frame& F, const JobDev& J) {
-  Grid g;
-  g.rx = F.res[0]; g.ry = F.res[1]; g.rz = F.res[2];
-  g.bx = F.bdim[0] + 2; g.bxy = (F.bdim[0] + 2) * (F.bdim[1] + 2);
-  g.max_steps = F.max_steps;
-  g.bminx = F.bmin[0]; g.bminy = F.bmin[1]; g.bminz = F.bmin[2];
-  g.vextx = F.vext[0]; g.vexty = F.vext[1]; g.vextz = F.vext[2];
-  g.bmaxx = F.bmax[0]; g.bmaxy = F.bmax[1]; g.bmaxz = F.bmax[2];
-  g.bricks = J.bricks + 1 + g.bx + g.bxy;   // brick (0,0,0) inside the border
-  return g;
-}
+VT_D Grid grid_of(const Frame& F, const JobDev& J) { return make_grid(F, J.bricks); }
 
 struct Dda {
   int32_t x, y, z;
@@ -278,8 +300,12 @@ VT_D void dda_begin(const Grid& g, Dda& s, v3 o, v3 d) {
 // bounds test folds into the occupancy test: a set bit outside [0, res) is
 // the exit the reference detects at the top of its loop, with the same
 // voxel position.  `bricks` points at brick (0, 0, 0) of the padded array.
-template <bool kCount>
-VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt) {
+// With kVote, the lanes of a warp also stop (still running, resumable) once
+// fewer than `vote_min` of them are stepping, checked every fourth step, so
+// that the caller can restart the lanes whose segments ended; the state is
+// the same as if the segment had been stepped in one call.
+template <bool kCount, bool kVote = false>
+VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt, int vote_min = 0) {
   int x = s.x, y = s.y, z = s.z, steps = s.steps, cb = s.cb;
   float dx = s.dx, dy = s.dy, dz = s.dz;
   unsigned long long bits = s.bits;
@@ -288,9 +314,14 @@ VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt) {
   if (budget > left) budget = left;
   int k = 0;
   for (; k < budget; ++k) {
-    const int b = (x >> 2) + g.bx * (y >> 2) + g.bxy * (z >> 2);
-    if (b != cb) { bits = __ldg(&g.bricks[b]); cb = b; }
-    if ((bits >> ((x & 3) | ((y & 3) << 2) | ((z & 3) << 4))) & 1ull) {
+    if (kVote && (k & 3) == 3 && __popc(__activemask()) < vote_min) break;
+    const int b = (x >> g.shx) + g.bx * (y >> g.shy) + g.bxy * (z >> g.shz);
+    if (b != cb) {
+      const long long w = (long long)b + 1 + g.bx + g.bxy;   // index in the padded array
+      bits = chk(w >= 0 && w < g.n_words, CHK_BRICK) ? __ldg(&g.bricks[b]) : ~0ull;
+      cb = b;
+    }
+    if ((bits >> brick_bit(x, y, z, g.shx, g.shxy, g.mx, g.my, g.mz)) & 1ull) {
       const bool inside = (unsigned)x < (unsigned)g.rx && (unsigned)y < (unsigned)g.ry && (unsigned)z < (unsigned)g.rz;
       if (inside) cnt.add(C_DDA_CELLS, 1);
       state = inside ? DDA_HIT : DDA_MISS;
@@ -456,7 +487,8 @@ VT_D v3 dir_from_uv(float u, float v, float rot) {
   const float st = vtb::vsin(theta);
   return mk3(st * vtb::vcos(phi), vtb::vcos(theta), st * vtb::vsin(phi));
 }
-VT_D v3 texel(const JobDev& J, int w, int i, int j) {
+VT_D v3 texel(const JobDev& J, int w, int h, int i, int j) {
+  if (!chk((unsigned)i < (unsigned)w && (unsigned)j < (unsigned)h, CHK_TEXEL)) return mk3(0.f, 0.f, 0.f);
   const uint2 q = __ldg(&J.env_texels[(size_t)j * w + i]);
   return mk3(hf((unsigned short)(q.x & 0xffffu)), hf((unsigned short)(q.x >> 16)),
              hf((unsigned short)(q.y & 0xffffu)));
@@ -473,8 +505,8 @@ VT_D v3 env_lookup(const Frame& F, const JobDev& J, float u, float v, Cnt<kCount
   int i1 = i0 + 1, j1 = j0 + 1;
   i0 = min(max(i0, 0), w - 1); i1 = min(max(i1, 0), w - 1);
   j0 = min(max(j0, 0), h - 1); j1 = min(max(j1, 0), h - 1);
-  const v3 t00 = texel(J, w, i0, j0), t10 = texel(J, w, i1, j0);
-  const v3 t01 = texel(J, w, i0, j1), t11 = texel(J, w, i1, j1);
+  const v3 t00 = texel(J, w, h, i0, j0), t10 = texel(J, w, h, i1, j0);
+  const v3 t01 = texel(J, w, h, i0, j1), t11 = texel(J, w, h, i1, j1);
   const float gx = 1.0f - fx, gy = 1.0f - fy;
   const v3 a = t00 * gx + t10 * fx;
   const v3 b = t01 * gx + t11 * fx;
@@ -514,10 +546,15 @@ template <bool kCount>
 VT_D v3 sample_env(const Frame& F, const JobDev& J, const Basis& b, float u0, float u1,
                    v3& dir, float& pdf, Cnt<kCount>& cnt) {
   if (F.use_image) {
-    const int su = F.env_w + 1, sv = F.env_h + 1;
+    const int su = F.env_cdf_w + 1, sv = F.env_cdf_h + 1;
     const int row = search_cdf(J.cdf_v, sv - 1, u1, cnt);
     const float* cu = J.cdf_u + (size_t)row * su;
     const int col = search_cdf(cu, su - 1, u0, cnt);
+    if (!chk(row >= 0 && row + 1 < sv && col >= 0 && col + 1 < su, CHK_CDF)) {
+      dir = mk3(0.f, 1.f, 0.f);
+      pdf = 0.0f;
+      return mk3(0.f, 0.f, 0.f);
+    }
     cnt.add(C_CDF_PROBES, 4);
     const float lu = __ldg(&cu[col]), hu = __ldg(&cu[col + 1]);
     const float du = (u0 - lu) / (hu - lu);
@@ -673,7 +710,9 @@ VT_D void light_sample(const Frame& F, const JobDev& J, Path& p, const Basis& b,
   float pdf;
   if (li < num_lights - 1) {
     cnt.add(C_EMISSIVE_READS, 1);
-    const int idx = __ldg(&J.emissive[li]);
+    const int idx0 = __ldg(&J.emissive[li]);
+    const bool idx_ok = chk(idx0 >= 0 && (long long)idx0 < (long long)F.res[0] * F.res[1] * F.res[2], CHK_EMISSIVE);
+    const int idx = idx_ok ? idx0 : 0;
     const int dz = F.res[0] * F.res[1], dy = F.res[0];
     const int ez = idx / dz;
     const int r1 = idx - ez * dz;
@@ -836,10 +875,13 @@ VT_D bool ext_end(const Frame& F, const JobDev& J, Path& p, SegEnd e, Cnt<kCount
 // 1 anything else (the microfacet path).  No counter: ext_hit counts the
 // material fetch.
 VT_D int hit_class(const Frame& F, const JobDev& J, SegEnd e) {
-  if (e.y < 0) return load_mat(J, F.ground_mat).type == 0 ? 0 : 1;
+  if (e.y < 0) return load_mat(F, J, F.ground_mat).type == 0 ? 0 : 1;
+  if (!chk((unsigned)e.x < (unsigned)F.res[0] && (unsigned)e.y < (unsigned)F.res[1] &&
+               (unsigned)e.z < (unsigned)F.res[2], CHK_GRID))
+    return 1;
   const uint8_t g = __ldg(&J.grid[(size_t)e.x + (size_t)F.res[0] * ((size_t)e.y + (size_t)F.res[1] * (size_t)e.z)]);
   if (g == 0) return 1;
-  return load_mat(J, (int)g - 1).type == 0 ? 0 : 1;
+  return load_mat(F, J, (int)g - 1).type == 0 ? 0 : 1;
 }
 
 // One complete sample, run to the end by a single lane (megakernel form).

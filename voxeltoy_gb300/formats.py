@@ -61,3 +61,15 @@ def encode_pfm(pixels: np.ndarray) -> bytes:
     out = (C.c_uint8 * n.value)()
     L.call("vt_image_encode_pfm", L.ptr(px), w, h, ch, out, n.value, C.byref(n))
     return bytes(out)
+
+
+def encode_hdr(pixels: np.ndarray) -> bytes:
+    """float [h, w, 3 or 4], rows bottom first (vt_job_readback's order) ->
+    Radiance RGBE bytes (rows top first in the file)."""
+    px = np.ascontiguousarray(pixels, dtype=np.float32)
+    h, w, ch = px.shape
+    n = C.c_size_t()
+    L.call("vt_image_encode_hdr", L.ptr(px), w, h, ch, None, 0, C.byref(n))
+    out = (C.c_uint8 * n.value)()
+    L.call("vt_image_encode_hdr", L.ptr(px), w, h, ch, out, n.value, C.byref(n))
+    return bytes(out)

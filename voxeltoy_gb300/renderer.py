@@ -78,10 +78,22 @@ class Context:
         """Wavefront launch parameters; 0 (or -1 for trace_blocks_per_sm) keeps a value."""
         L.call("vt_diag_set_tuning", self.h, path_slots, trace_blocks_per_sm, trace_steps, max_items)
 
+    def set_trace_tuning(self, queue_chunk: int = 0, refill_min: int = -1):
+        """DDA kernel parameters: queue records per warp atomic (32-1024, multiple
+        of 32) and the early-refill threshold (0 = off); 0 / -1 keep a value."""
+        L.call("vt_diag_set_trace_tuning", self.h, queue_chunk, refill_min)
+
     def launch_count(self) -> int:
         n = C.c_uint64()
         L.call("vt_diag_launch_count", self.h, C.byref(n))
         return n.value
+
+    def l2_read_bandwidth(self, nbytes: int = 32 << 20, reps: int = 1000) -> float:
+        """GB/s of one launch of `reps` L1-bypassing read sweeps over an
+        L2-resident buffer of `nbytes` bytes (vt_diag_l2_read_bandwidth)."""
+        g = C.c_double()
+        L.call("vt_diag_l2_read_bandwidth", self.h, nbytes, reps, C.byref(g))
+        return g.value
 
     def set_kernel(self, kernel: int):
         L.call("vt_diag_set_kernel", self.h, kernel)
@@ -210,6 +222,26 @@ class Scene:
         L.call("vt_scene_get_info", self.h, C.byref(inf))
         return inf
 
+    def set_brick_shape(self, shape):
+        """Log2 extents (sx, sy, sz) of the occupancy bricks, summing to 6."""
+        L.call("vt_scene_set_brick_shape", self.h, *[int(v) for v in shape])
+
+    def brick_shape(self) -> tuple:
+        sh = (C.c_int32 * 3)()
+        L.call("vt_scene_get_brick_shape", self.h, sh)
+        return tuple(sh)
+
+    def bricks(self) -> np.ndarray:
+        """The occupancy bit-bricks on the padded brick grid ([bz+2, by+2, bx+2] uint64)."""
+        n = C.c_int64()
+        L.call("vt_diag_scene_bricks", self.h, None, 0, C.byref(n))
+        out = np.empty(n.value, np.uint64)
+        L.call("vt_diag_scene_bricks", self.h, L.ptr(out), out.nbytes, C.byref(n))
+        rx, ry, rz = self.info().resolution
+        sx, sy, sz = self.brick_shape()
+        return out.reshape(((rz + (1 << sz) - 1) >> sz) + 2, ((ry + (1 << sy) - 1) >> sy) + 2,
+                           ((rx + (1 << sx) - 1) >> sx) + 2)
+
     def voxels(self) -> np.ndarray:
         inf = self.info()
         rx, ry, rz = inf.resolution
@@ -243,16 +275,21 @@ class Scene:
 
 
 class Env:
-    def __init__(self, ctx: Context, rgb: np.ndarray):
+    def __init__(self, ctx: Context, rgb: np.ndarray, flags: int = 0):
+        """flags: VT_ENV_CDF_REFERENCE_SIZE builds the CDFs from the image
+        shrunk to at most 512 texels on its long axis, as the reference does."""
         img = np.ascontiguousarray(rgb, dtype=np.float32)
         self.h_px, self.w_px = img.shape[:2]
         h = C.c_void_p()
-        L.call("vt_env_create_image", ctx.h, L.ptr(img), self.w_px, self.h_px, C.byref(h))
+        L.call("vt_env_create_image_ex", ctx.h, L.ptr(img), self.w_px, self.h_px, flags, C.byref(h))
         self.h = h
+        size = (C.c_int32 * 4)()
+        L.call("vt_env_get_info", self.h, size)
+        self.cdf_w, self.cdf_h = size[2], size[3]
 
     def cdf(self):
-        cu = np.empty((self.h_px, self.w_px + 1), np.float32)
-        cv = np.empty(self.h_px + 1, np.float32)
+        cu = np.empty((self.cdf_h, self.cdf_w + 1), np.float32)
+        cv = np.empty(self.cdf_h + 1, np.float32)
         integral = C.c_float()
         L.call("vt_env_read_cdf", self.h, L.ptr(cu), cu.nbytes, L.ptr(cv), cv.nbytes, C.byref(integral))
         return cu, cv, integral.value
@@ -309,6 +346,20 @@ class Job:
 
     def reset(self):
         L.call("vt_job_reset", self.h)
+
+    def snapshot(self):
+        """(sum, comp, samples): the accumulation state (vt_job_snapshot)."""
+        sum_ = np.empty((self.height, self.width, 4), np.float32)
+        comp = np.empty_like(sum_)
+        n = C.c_int32()
+        L.call("vt_job_snapshot", self.h, L.ptr(sum_), L.ptr(comp), sum_.nbytes, C.byref(n))
+        return sum_, comp, n.value
+
+    def restore(self, sum_: np.ndarray, comp: np.ndarray, samples: int):
+        """Continue from a snapshot (vt_job_restore)."""
+        s = np.ascontiguousarray(sum_, np.float32)
+        c = np.ascontiguousarray(comp, np.float32)
+        L.call("vt_job_restore", self.h, L.ptr(s), L.ptr(c), s.nbytes, samples)
 
     def set_camera(self, cam: L.Camera):
         L.call("vt_job_set_camera", self.h, C.byref(cam))
@@ -368,9 +419,9 @@ class Job:
 class Server:
     def __init__(self, ctx: Context, hbm_budget_bytes: int = 0, max_active_jobs: int = 64,
                  passes_per_round: int = 4, path_slots: int = 0, order: int = L.VT_SERVE_ARRIVAL,
-                 quick_paths: int = 0, round_paths_cap: int = 0):
+                 quick_paths: int = 0, round_paths_cap: int = 0, round_paths: int = 0):
         opts = L.ServerOpts(hbm_budget_bytes, max_active_jobs, passes_per_round, path_slots, order, quick_paths,
-                            round_paths_cap)
+                            round_paths_cap, round_paths)
         h = C.c_void_p()
         L.call("vt_server_create", ctx.h, C.byref(opts), C.byref(h))
         self.h = h
@@ -380,6 +431,24 @@ class Server:
         t = C.c_uint64()
         L.call("vt_server_submit", self.h, scene.h, env.h if env else None, C.byref(cam), C.byref(settings),
                width, height, spp, C.byref(t))
+        return t.value
+
+    def submit_dense(self, key: int, voxels: np.ndarray | None, palette, cam: L.Camera, settings: L.RenderSettings,
+                     width: int, height: int, spp: int, env: Env | None = None, flags: int = 0,
+                     shape=None) -> int:
+        """vt_server_submit_dense: a request on a volume the server keeps
+        resident under `key`; voxels may be None when the key is resident
+        (then `shape` = (rz, ry, rx) is not needed either)."""
+        t = C.c_uint64()
+        if voxels is not None:
+            v = np.ascontiguousarray(voxels, dtype=np.uint8)
+            rz, ry, rx = v.shape
+            pal = L.materials(palette)
+            L.call("vt_server_submit_dense", self.h, key, rx, ry, rz, L.ptr(v), pal, len(palette), flags,
+                   env.h if env else None, C.byref(cam), C.byref(settings), width, height, spp, C.byref(t))
+        else:
+            L.call("vt_server_submit_dense", self.h, key, 0, 0, 0, None, None, 0, flags,
+                   env.h if env else None, C.byref(cam), C.byref(settings), width, height, spp, C.byref(t))
         return t.value
 
     def poll(self, ticket: int):
@@ -536,9 +605,11 @@ class Renderer:
 
     # Renderer::saveImage (renderer.h:72): float RGB written as a PFM file
     def save_image(self, path: str):
-        from .formats import encode_pfm
+        """The accumulated image as a Radiance .hdr file (extension .hdr) or a PFM."""
+        from .formats import encode_hdr, encode_pfm
+        img = self.job.readback()                        # rows bottom first, as PFM stores them
         with open(path, "wb") as f:
-            f.write(encode_pfm(self.job.readback()))   # PFM, like the readback, stores the bottom row first
+            f.write(encode_hdr(img) if str(path).lower().endswith(".hdr") else encode_pfm(img))
 
     # Renderer::requestAction (renderer.h:106, actions.cpp:5-52): x, y and dx, dy
     # are normalised window coordinates with the origin at the top left, as
