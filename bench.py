@@ -662,6 +662,35 @@ def config1_rmse(ctx) -> dict:
     return rmse_vs_fp64(cfg, img, cfg.spp, (0, cfg.height))
 
 
+def profile_voxelize(args, local):
+    """--workload voxelize --profile: the config-5 scene (1024^3 from the
+    1.3M-triangle mesh) rendered at 2048^2 x --spp samples with the launch
+    shape given on the command line, a frame per step, for ncu captures."""
+    from voxeltoy_gb300 import Context, Job, Scene, scenes as S
+    from voxeltoy_gb300 import _lib as L
+    v, f = S.fbm_displaced_icosphere(level=8)
+    ctx = Context(local)
+    if args.slots > 0:
+        ctx.set_lanes(args.lanes)
+        ctx.set_tuning(args.slots, args.trace_bps, args.trace_steps)
+    sc = Scene.voxelize(ctx, np.ascontiguousarray(v, np.float32), np.ascontiguousarray(f, np.uint32),
+                        (1024, 1024, 1024), mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
+                        palette=[S.lambert(0.7)])
+    cfg = S.config1(edge=8, width=2048, height=2048, spp=args.spp)
+    cfg.settings.max_bounces = 8
+    job = Job(ctx, sc, None, cfg.camera, cfg.settings, 2048, 2048)
+    for k in range(args.warmup + args.steps):
+        job.reset()
+        t0 = time.perf_counter()
+        job.render(args.spp)
+        job.synchronize()
+        if k >= args.warmup:
+            print(json.dumps({"profile_step_ms": 1e3 * (time.perf_counter() - t0), "paths": 2048 * 2048 * args.spp,
+                              "launches": ctx.launch_count()}), flush=True)
+    job.close(); sc.close(); ctx.close()
+    return 0
+
+
 def run_voxelize(args, world, rank, local):
     """1.3M-triangle fBm-displaced icosphere, conservative voxelization into
     1024^3, then a 2048^2 render with config-1 materials and sky, 8 bounces."""
@@ -742,6 +771,8 @@ def main():
     from voxeltoy_gb300 import _lib as L
 
     torch.cuda.set_device(local)
+    if args.workload == "voxelize" and args.profile:
+        return profile_voxelize(args, local)
     if args.workload not in ("config2", "config1"):
         runner = {"batching": run_batching, "serving": run_serving, "voxelize": run_voxelize}[args.workload]
         line = runner(args, world, rank, local)
@@ -884,7 +915,8 @@ def main():
                   "gdda_cells_per_s": world * float(cnt[1]) / (ms * 1e-3) / 1e9},
         "counters_per_frame": {"paths": int(cnt[0]), "dda_cells": int(cnt[1]), "palette": int(cnt[2]),
                                "env_evals": int(cnt[3]), "cdf_probes": int(cnt[4]), "emissive_reads": int(cnt[5]),
-                               "segments": int(cnt[6]), "empty_brick_cells": int(cnt[7])},
+                               "segments": int(cnt[6]), "empty_brick_cells": int(cnt[7]),
+                               "stream_positions": int(cnt[8])},
         "frame_ms": {"p50": float(np.percentile(times, 50)), "p99": float(np.percentile(times, 99)),
                      "note": "device time of each timed frame (one resident job from reset to its spp target)"},
         "cpu_baseline": cpu,

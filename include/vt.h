@@ -528,7 +528,7 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
  * frame times, such as an interactive viewer, because cudaMalloc and
  * cudaFree can synchronise the whole device.  Instead, this call takes all
  * of its working memory from one array compiled into the library
- * (VT_FIXED_SCRATCH_BYTES, about 44 MB, not counted against any budget).
+ * (VT_FIXED_SCRATCH_BYTES, about 42 MB, not counted against any budget).
  * The CUDA runtime reserves it on a device when it loads the code that
  * holds it, which vt_create triggers for its device, so the reservation
  * (and a failure to make it) happens when the context is created, not in
@@ -559,7 +559,7 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
 #define VT_FIXED_MAX_JOBS 16
 #define VT_FIXED_MAX_PATH_SLOTS 65536
 #define VT_FIXED_MAX_SAMPLES (1 << 20)
-#define VT_FIXED_SCRATCH_BYTES 43528960
+#define VT_FIXED_SCRATCH_BYTES 41956096
 VT_API int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs,
                                  int32_t n_jobs, int32_t passes,
                                  int32_t path_slots, int32_t* results);

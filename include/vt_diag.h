@@ -21,8 +21,9 @@ extern "C" {
  * [0] paths, [1] DDA cells tested, [2] palette records read,
  * [3] environment texel evaluations, [4] CDF entries probed,
  * [5] emissive-list reads, [6] DDA segments started, [7] DDA cells tested
- * inside 4x4x4 bricks that hold no occupied voxel. */
-#define VT_DIAG_NUM_COUNTERS 8
+ * inside bricks that hold no occupied voxel, [8] wavefront stream positions
+ * shaded (one per path and round; 0 in the plain form). */
+#define VT_DIAG_NUM_COUNTERS 9
 
 /* Trace caller-supplied rays through the job's scene with the DDA of
  * src/shaders/shared/dda.h:7-100 (traverse with the default step cap).

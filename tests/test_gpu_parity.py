@@ -960,3 +960,26 @@ def test_full_size_config2(ctx, orc):
         ctx.set_tuning(1 << 23, 0, 16)                 # the context defaults
         close_all(job, scene, env)
 
+
+
+def test_counted_render_counters_agree_across_forms(ctx):
+    """vt_diag_render_counted: the wavefront and plain forms count the same
+    events of the same samples, and the wavefront's stream positions are one
+    per path and round (at least one per path, at most one per bounce)."""
+    cfg = small_config2(edge=40, w=48, h=40, seed=81)
+    cfg.settings.max_samples = 1 << 20
+    scene, env, job = gpu_setup(ctx, cfg)
+    try:
+        wf = job.render_counted(6)
+        job.reset()
+        ctx.set_kernel(1)
+        plain = job.render_counted(6)
+        ctx.set_kernel(2)
+        paths = 48 * 40 * 6
+        assert wf[0] == plain[0] == paths
+        np.testing.assert_array_equal(wf[:8], plain[:8])
+        assert plain[8] == 0
+        assert paths <= wf[8] <= paths * (cfg.settings.max_bounces + 1)
+    finally:
+        ctx.set_kernel(2)
+        close_all(job, scene, env)

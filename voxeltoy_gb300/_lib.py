@@ -39,7 +39,7 @@ VT_QUIRKS_REFERENCE = 0xFF
 VT_RNG_PHILOX, VT_RNG_NOISE_TABLE = 0, 1
 VT_READBACK_FLIP_Y, VT_READBACK_TONEMAP = 1, 2
 VT_REQ_QUEUED, VT_REQ_RUNNING, VT_REQ_DONE, VT_REQ_CANCELLED, VT_REQ_FAILED = 0, 1, 2, 3, 4
-VT_DIAG_NUM_COUNTERS = 8
+VT_DIAG_NUM_COUNTERS = 9
 
 f3 = C.c_float * 3
 i3 = C.c_int32 * 3

@@ -414,6 +414,9 @@ static int scene_alloc(vt_context* ctx, int32_t rx, int32_t ry, int32_t rz, vt_s
   VT_CHECK_ARG(ctx && out, "null argument");
   VT_CHECK_ARG(rx > 0 && ry > 0 && rz > 0, "resolution must be positive");
   VT_CHECK_ARG((int64_t)rx * ry * rz < ((int64_t)1 << 31), "volume exceeds 2^31 voxels");
+  // the wavefront's packed segment ends hold positions -1 .. extent
+  VT_CHECK_ARG(rx <= (1 << 20) - 2 && ry <= (1 << 20) - 2 && rz <= (1 << 19) - 2,
+               "volume extent beyond 1048574 (x, y) or 524286 (z) voxels");
   *out = nullptr;
   vt_scene* s = new vt_scene();
   s->ctx = ctx;
@@ -1378,6 +1381,8 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     }
     T = &table;
   }
+  bool all_444 = true;   // the DDA kernel's fixed-shape form applies
+  for (const Grid& g : grids) all_444 = all_444 && g.shx == 2 && g.shy == 2 && g.shz == 2;
   // Lanes: independent wavefronts over equal shares of the items, each with
   // its share of the path slots and its own stream, so that one lane's
   // memory-bound shading overlaps another's ALU-bound DDA.
@@ -1400,6 +1405,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     P[l].counters = count ? ctx->d_counters : nullptr;
     P[l].trace_chunk = (uint32_t)ctx->trace_chunk;
     P[l].refill_min = ctx->refill_min;
+    P[l].bricks_444 = all_444 ? 1 : 0;
   }
   // control words zero (first stream empty), item counters at each lane's first item
   VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, vt_context::kMaxLanes * kCtlBytes, st), "wavefront control");

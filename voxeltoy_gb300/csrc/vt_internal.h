@@ -171,7 +171,8 @@ enum Counter {
   C_EMISSIVE_READS = 5,
   C_SEGMENTS = 6,
   C_EMPTY_CELLS = 7,   // DDA cells tested inside bricks with no occupied voxel
-  C_NUM = 8
+  C_POSITIONS = 8,     // wavefront stream positions shaded (path-rounds; 0 in the plain form)
+  C_NUM = 9
 };
 
 // Per-pixel first-hit record written by the diagnostic pass: voxel x, y, z

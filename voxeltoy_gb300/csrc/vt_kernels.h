@@ -43,7 +43,7 @@ struct WfHitRecs {
   float4* h1;      // rd.xyz, flags
   float4* h2;      // L.xyz, rng word
   float4* h3;      // T.xyz, bsdf_pdf
-  int4* h4;        // hit voxel x, y, z, DDA state
+  unsigned long long* h4;   // hit voxel x, y, z and DDA state, packed (pack_end)
 };
 // Control words of a wavefront launch, per round parity: records appended to
 // the queue, records taken by the tracer, length of the stream the round
@@ -62,7 +62,8 @@ struct WfParams {
   int32_t n_jobs;
   const Grid* grids;               // device array, DDA view of each job's volume
   WfState x[2];                    // round parity par reads x[par] and writes x[par ^ 1]
-  int4* hits;                      // [2][n_slots] segment ends (extension, shadow) by position
+  unsigned long long* hits;        // [2][n_slots] segment ends (extension, shadow) by position, packed
+                                   // (pack_end: voxel x, y, z and DDA state in 64 bits)
   WfHitRecs hr;
   int32_t n_slots;                 // stream capacity (paths in flight)
   float4* queue[2];                // segment records, two float4 each:
@@ -72,14 +73,15 @@ struct WfParams {
   unsigned long long n_items;
   float4* sbuf;                    // per-item sample outputs
   unsigned long long* counters;    // nullable
+  int32_t bricks_444;              // every job's bricks are 4x4x4 (the DDA kernel's fixed-shape form)
   uint32_t trace_chunk;            // queue records a trace warp takes per atomic (32-256)
   int32_t refill_min;              // trace warps refill early once fewer lanes step (0 = every
                                    // kTraceSteps steps only)
 };
 // Device bytes per stream position, and the carving of one allocation of
 // slots * kWfSlotBytes bytes (256-byte aligned) into the buffers of P.
-constexpr size_t kWfSlotBytes = 2 * (5 * sizeof(float4) + sizeof(uint32_t)) + 2 * sizeof(int4) +
-                                (4 * sizeof(float4) + sizeof(int4)) + 8 * sizeof(float4);
+constexpr size_t kWfSlotBytes = 2 * (5 * sizeof(float4) + sizeof(uint32_t)) + 2 * sizeof(uint64_t) +
+                                (4 * sizeof(float4) + sizeof(uint64_t)) + 8 * sizeof(float4);
 void wf_carve(void* mem, size_t slots, WfParams& P);
 // Launches of at most kWfParamJobs jobs pass their job and grid records as a
 // kernel parameter as well, so the kernels read them through the constant

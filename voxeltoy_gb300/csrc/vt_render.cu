@@ -290,17 +290,16 @@ __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __
   SegEnd e;
   e.x = e.y = e.z = e.state = 0;
   if (fl & SL_ACTIVE) {
+    cnt.add(C_POSITIONS, 1);
     const uint32_t job = fl >> kSlotJobShift;
     const JobEntry& E = job_entry(P, T, job);
     load_for_shade(src, i, fl, p, item, rng_word);
     if (fl & SL_SHADOW) {
-      const int4 h = P.hits[(size_t)P.n_slots + i];
-      SegEnd se; se.x = h.x; se.y = h.y; se.z = h.z; se.state = h.w;
+      const SegEnd se = unpack_end(P.hits[(size_t)P.n_slots + i]);
       shadow_end(E.F, p, se);
     }
     if (fl & SL_EXT) {
-      const int4 h = P.hits[i];
-      e.x = h.x; e.y = h.y; e.z = h.z; e.state = h.w;
+      e = unpack_end(P.hits[i]);
       hit = ext_resolve(E.F, E.J, p, e, cnt);
       if (hit) cls = hit_class(E.F, E.J, e);
     }
@@ -319,7 +318,7 @@ __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __
     P.hr.h1[j] = pack4(p.rd, __uint_as_float(slot_flags(p, 1u, fl >> kSlotJobShift)));
     P.hr.h2[j] = pack4(p.L, rng_word);
     P.hr.h3[j] = pack4(p.T, p.bsdf_pdf);
-    P.hr.h4[j] = make_int4(e.x, e.y, e.z, e.state);
+    P.hr.h4[j] = pack_end(e.x, e.y, e.z, e.state);
   }
   flush_counters(cnt, P.counters);
 }
@@ -346,7 +345,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
     if (mine) {
       const uint32_t j = v < nl ? v : (uint32_t)P.n_slots - 1u - (v - nl);
       const float4 h0 = P.hr.h0[j], h1 = P.hr.h1[j], h2 = P.hr.h2[j], h3 = P.hr.h3[j];
-      const int4 h4 = P.hr.h4[j];
+      const unsigned long long h4 = P.hr.h4[j];
       const uint32_t fl = __float_as_uint(h1.w);
       job = fl >> kSlotJobShift;
       const JobEntry& E = job_entry(P, T, job);
@@ -357,7 +356,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
       p.T = xyz4(h3); p.bsdf_pdf = h3.w;
       load_flags(fl, p);
       rng_from_item(E, item, __float_as_uint(h2.w), p);
-      SegEnd e; e.x = h4.x; e.y = h4.y; e.z = h4.z; e.state = h4.w;
+      const SegEnd e = unpack_end(h4);
       ext_hit(E.F, E.J, p, e, cnt);
       emit = 2u | (p.has_cont ? 1u : 0u);
     }
@@ -477,7 +476,7 @@ struct GridHold<WfOneJob> {
 // while it steps the current one, so starting a segment never waits on
 // memory, and lanes pick up a new segment every kTraceSteps steps as theirs
 // finish (with kVote also as soon as fewer than P.refill_min lanes step).
-template <bool kCount, int kTraceSteps, bool kVote, class Tab>
+template <bool kCount, int kTraceSteps, bool kVote, bool k444, class Tab>
 __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -501,7 +500,7 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
       gh.set(P, T, __float_as_uint(nb.w));
       dda_begin(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
       if (s.state == DDA_RUNNING) have = true;
-      else P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
+      else P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
     }
     unsigned need = __ballot_sync(FULL, !have_next);
     while (need && !exhausted) {          // prefetch next records
@@ -525,9 +524,9 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
     }
     if (__ballot_sync(FULL, have || have_next) == 0u) break;
     if (have) {
-      dda_advance<kCount, kVote>(gh.get(T), s, kTraceSteps, cnt, P.refill_min);
+      dda_steps<kCount, kVote, k444>(gh.get(T), s, kTraceSteps, cnt, P.refill_min);
       if (s.state != DDA_RUNNING) {
-        P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = make_int4(s.x, s.y, s.z, s.state);
+        P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
         have = false;
       }
     }
@@ -576,18 +575,25 @@ cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool
   return cudaGetLastError();
 }
 
-template <bool kVote, class Tab>
+template <bool kVote, bool k444, class Tab>
 static void wf_trace_steps(const WfParams& P, const Tab& T, int par, int blocks, int steps, cudaStream_t st) {
-  if (steps <= 8) k_wf_trace<false, 8, kVote, Tab><<<blocks, 256, 0, st>>>(P, T, par);
-  else if (steps <= 16) k_wf_trace<false, 16, kVote, Tab><<<blocks, 256, 0, st>>>(P, T, par);
-  else k_wf_trace<false, 32, kVote, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  if (steps <= 8) k_wf_trace<false, 8, kVote, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else if (steps <= 16) k_wf_trace<false, 16, kVote, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else k_wf_trace<false, 32, kVote, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+}
+
+template <bool k444, class Tab>
+static void wf_trace_shape(const WfParams& P, const Tab& T, int par, int blocks, int steps, bool count,
+                           cudaStream_t st) {
+  if (count) k_wf_trace<true, 16, false, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+  else if (P.refill_min > 0) wf_trace_steps<true, k444>(P, T, par, blocks, steps, st);
+  else wf_trace_steps<false, k444>(P, T, par, blocks, steps, st);
 }
 
 template <class Tab>
 static void wf_trace(const WfParams& P, const Tab& T, int par, int blocks, int steps, bool count, cudaStream_t st) {
-  if (count) k_wf_trace<true, 16, false, Tab><<<blocks, 256, 0, st>>>(P, T, par);
-  else if (P.refill_min > 0) wf_trace_steps<true>(P, T, par, blocks, steps, st);
-  else wf_trace_steps<false>(P, T, par, blocks, steps, st);
+  if (P.bricks_444) wf_trace_shape<true>(P, T, par, blocks, steps, count, st);
+  else wf_trace_shape<false>(P, T, par, blocks, steps, count, st);
 }
 
 cudaError_t launch_wf_trace(const WfParams& P, int par, int blocks, int steps, bool count, cudaStream_t st,
@@ -618,7 +624,7 @@ void wf_carve(void* mem, size_t S, WfParams& P) {
   P.queue[0] = f;
   P.queue[1] = f + 4 * S;
   f += 8 * S;
-  int4* h = (int4*)f;
+  unsigned long long* h = (unsigned long long*)f;
   P.hits = h;
   P.hr.h4 = h + 2 * S;
   uint32_t* u = (uint32_t*)(h + 3 * S);
@@ -628,7 +634,7 @@ void wf_carve(void* mem, size_t S, WfParams& P) {
 
 int wf_trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8, false, WfJobTable>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8, false, true, WfJobTable>, 256, 0);
   return n;
 }
 

@@ -304,8 +304,12 @@ VT_D void dda_begin(const Grid& g, Dda& s, v3 o, v3 d) {
 // fewer than `vote_min` of them are stepping, checked every fourth step, so
 // that the caller can restart the lanes whose segments ended; the state is
 // the same as if the segment had been stepped in one call.
-template <bool kCount, bool kVote = false>
-VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt, int vote_min = 0) {
+// k444: the bricks are known to be 4x4x4 (shifts and masks are immediates);
+// otherwise the grid's brick shape is read at run time.
+template <bool kCount, bool kVote, bool k444>
+VT_D void dda_steps(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt, int vote_min) {
+  const int shx = k444 ? 2 : g.shx, shy = k444 ? 2 : g.shy, shz = k444 ? 2 : g.shz;
+  const int shxy = k444 ? 4 : g.shxy, mx_ = k444 ? 3 : g.mx, my_ = k444 ? 3 : g.my, mz_ = k444 ? 3 : g.mz;
   int x = s.x, y = s.y, z = s.z, steps = s.steps, cb = s.cb;
   float dx = s.dx, dy = s.dy, dz = s.dz;
   unsigned long long bits = s.bits;
@@ -315,13 +319,13 @@ VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt, int v
   int k = 0;
   for (; k < budget; ++k) {
     if (kVote && (k & 3) == 3 && __popc(__activemask()) < vote_min) break;
-    const int b = (x >> g.shx) + g.bx * (y >> g.shy) + g.bxy * (z >> g.shz);
+    const int b = (x >> shx) + g.bx * (y >> shy) + g.bxy * (z >> shz);
     if (b != cb) {
       const long long w = (long long)b + 1 + g.bx + g.bxy;   // index in the padded array
       bits = chk(w >= 0 && w < g.n_words, CHK_BRICK) ? __ldg(&g.bricks[b]) : ~0ull;
       cb = b;
     }
-    if ((bits >> brick_bit(x, y, z, g.shx, g.shxy, g.mx, g.my, g.mz)) & 1ull) {
+    if ((bits >> brick_bit(x, y, z, shx, shxy, mx_, my_, mz_)) & 1ull) {
       const bool inside = (unsigned)x < (unsigned)g.rx && (unsigned)y < (unsigned)g.ry && (unsigned)z < (unsigned)g.rz;
       if (inside) cnt.add(C_DDA_CELLS, 1);
       state = inside ? DDA_HIT : DDA_MISS;
@@ -344,6 +348,15 @@ VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt, int v
   s.state = state;
 }
 
+VT_D bool bricks_444(const Grid& g) { return g.shx == 2 && g.shy == 2 && g.shz == 2; }
+
+// The DDA loop for the grid's brick shape (the 4x4x4 loop when it applies).
+template <bool kCount, bool kVote = false>
+VT_D void dda_advance(const Grid& g, Dda& s, int budget, Cnt<kCount>& cnt, int vote_min = 0) {
+  if (bricks_444(g)) dda_steps<kCount, kVote, true>(g, s, budget, cnt, vote_min);
+  else dda_steps<kCount, kVote, false>(g, s, budget, cnt, vote_min);
+}
+
 // traverse (dda.h:63-79): voxel hit, or with the ground quirk an exit below y = 0.
 VT_D bool seg_hit(uint32_t quirks, int state, int y) {
   if (state == DDA_HIT) return true;
@@ -354,6 +367,26 @@ VT_D bool dda_hit(const Frame& F, const Dda& s) { return seg_hit(F.quirks, s.sta
 // End of one DDA segment as the shading code sees it.
 struct SegEnd { int32_t x, y, z, state; };
 VT_D SegEnd seg_end(const Dda& s) { SegEnd e; e.x = s.x; e.y = s.y; e.z = s.z; e.state = s.state; return e; }
+
+// A segment end in one 64-bit word for the wavefront's buffers: x and y as
+// 21-bit and z as a 20-bit two's-complement field, the DDA state in the top
+// two bits.  Volumes are limited so that every position a segment can end
+// on (-1 to the extent) fits; a value beyond a field saturates.
+VT_D unsigned long long pack_end(int x, int y, int z, int state) {
+  x = min(max(x, -(1 << 20)), (1 << 20) - 1);
+  y = min(max(y, -(1 << 20)), (1 << 20) - 1);
+  z = min(max(z, -(1 << 19)), (1 << 19) - 1);
+  return ((unsigned long long)((uint32_t)x & 0x1fffffu)) | ((unsigned long long)((uint32_t)y & 0x1fffffu) << 21) |
+         ((unsigned long long)((uint32_t)z & 0xfffffu) << 42) | ((unsigned long long)(uint32_t)state << 62);
+}
+VT_D SegEnd unpack_end(unsigned long long w) {
+  SegEnd e;
+  e.x = (int)((long long)(w << 43) >> 43);
+  e.y = (int)((long long)(w << 22) >> 43);
+  e.z = (int)((long long)(w << 2) >> 44);
+  e.state = (int)(w >> 62);
+  return e;
+}
 
 // --------------------------------------------------------------- sampling
 // sampling.h:2-43

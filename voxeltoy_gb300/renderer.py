@@ -325,7 +325,7 @@ class Job:
         L.call("vt_job_set_integrator", self.h, integrator)
 
     def render_counted(self, passes: int) -> np.ndarray:
-        cnt = np.zeros(8, np.uint64)
+        cnt = np.zeros(L.VT_DIAG_NUM_COUNTERS, np.uint64)
         r = C.c_int32()
         L.call("vt_diag_render_counted", self.h, passes, L.ptr(cnt), C.byref(r))
         return cnt
@@ -398,7 +398,7 @@ class Job:
         n = self.width * self.height
         rgba = np.empty((self.height, self.width, 4), np.float32)
         hits = np.empty((self.height, self.width, 4), np.int32)
-        cnt = np.zeros(8, np.uint64)
+        cnt = np.zeros(L.VT_DIAG_NUM_COUNTERS, np.uint64)
         L.call("vt_diag_samples", self.h, sample, L.ptr(rgba), L.ptr(hits), L.ptr(cnt))
         assert rgba.size == 4 * n
         return rgba, hits, cnt
