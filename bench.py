@@ -888,12 +888,14 @@ def main():
         cpu = {"value": r["value"], "unit": UNIT, "cores": os.cpu_count(), "kind": "port", "sample": r["sample"]}
 
     traffic = None
+    issue = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
         t = json.loads(tf.read_text())
         if (t.get("workload") == args.workload and t.get("grid") == args.edge and t.get("res") == args.res
                 and t.get("spp") == args.spp):
             traffic = t["dram_bytes_per_launch"]
+            issue = t.get("dda_kernel")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -906,11 +908,21 @@ def main():
                      "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                      "peak_source": pk["source"],
                      "kernel": "k_wf_shade + k_wf_hit + k_wf_regen + k_wf_trace + k_wf_accumulate (one frame = one launch)",
+                     "traffic_source": "profiles/traffic.json: small-case per-stream-position DRAM bytes scaled by the "
+                                       "frame's stream positions",
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "bytes_model": "1 B/DDA cell + 16 B/palette record + 8 B/env texel eval + 4 B/CDF probe + "
                                     "4 B/emissive read + 64 B/path framebuffer",
                      "l2": {"achieved": achieved, "peak": l2["gbs"], "unit": "GB/s", "frac": achieved / l2["gbs"],
-                            "peak_source": l2["source"]}},
+                            "peak_source": l2["source"]},
+                     # the DDA kernel (58% of the frame's kernel time) is bound by instruction issue and
+                     # brick-load latency, not by bytes: its issue-slot utilisation from the committed profile
+                     "issue": None if issue is None else
+                     {"kernel": issue["kernel"], "achieved": issue["issue_active_pct"], "peak": issue["peak_issue_pct"],
+                      "unit": "% of issue slots", "frac": issue["issue_active_pct"] / issue["peak_issue_pct"],
+                      "warp_execution_efficiency_pct": issue["warp_execution_efficiency_pct"],
+                      "thread_instructions_per_dda_cell": issue["thread_instructions_per_dda_cell"],
+                      "source": issue["source"]}},
         "rates": {"gsegments_per_s": world * float(cnt[6]) / (ms * 1e-3) / 1e9,
                   "gdda_cells_per_s": world * float(cnt[1]) / (ms * 1e-3) / 1e9},
         "counters_per_frame": {"paths": int(cnt[0]), "dda_cells": int(cnt[1]), "palette": int(cnt[2]),
