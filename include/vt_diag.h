@@ -76,7 +76,7 @@ VT_API int vt_diag_cdf_from_function(vt_context* ctx, const float* func, int32_t
  * and trace_blocks_per_sm < 0 keep their value):
  * path_slots paths in flight per launch (default 2M), trace_blocks_per_sm
  * resident blocks of the DDA kernel (0: occupancy limit, the default),
- * trace_steps DDA steps between ray-pool refills (8, 16 or 32; default 16),
+ * trace_steps DDA steps between ray-pool refills (4, 8, 16 or 32; default 16),
  * max_items samples per launch (sample-buffer entries, default 2^28). */
 VT_API int vt_diag_set_tuning(vt_context* ctx, int64_t path_slots, int32_t trace_blocks_per_sm,
                               int32_t trace_steps, int64_t max_items);
@@ -105,6 +105,13 @@ VT_API int vt_diag_check_word(vt_context* ctx, uint32_t* word, int32_t* enabled)
  * timed with CUDA events on the context's stream.  The buffer is allocated
  * and freed by the call. */
 VT_API int vt_diag_l2_read_bandwidth(vt_context* ctx, int64_t bytes, int32_t reps, double* gbs);
+
+/* Form of the wavefront's DDA kernel: 0 (the default) sets each segment up
+ * in the lane that steps it, refilling lanes every trace_steps steps; 1
+ * keeps a per-warp pool of set-up segments in shared memory, sets up a
+ * warp's worth of segments at once and refills lanes from the pool after
+ * each batch of trace_steps steps (4, 8 or 16).  Results are identical. */
+VT_API int vt_diag_set_trace_form(vt_context* ctx, int32_t form);
 
 /* Tuning of the wavefront form's DDA kernel (values <= 0, and refill_min
  * < 0, keep their setting): queue_chunk queue records a warp takes with one

@@ -983,3 +983,40 @@ def test_counted_render_counters_agree_across_forms(ctx):
     finally:
         ctx.set_kernel(2)
         close_all(job, scene, env)
+
+
+@pytest.mark.parametrize("steps", [4, 8, 16])
+def test_pooled_trace_form_is_identical(ctx, steps):
+    """The pooled DDA kernel (segment set-up for a warp's worth of records at
+    once, lanes refilled from a shared-memory pool) gives the same images and
+    event counters as the per-lane form: one job (parameter-block records),
+    three jobs (parameter table) and eleven (global table)."""
+    cfgs = [small_config2(edge=36, w=40, h=32, seed=90 + k) for k in range(11)]
+    made = [gpu_setup(ctx, c) for c in cfgs]
+    jobs = [m[2] for m in made]
+    for c in cfgs:
+        c.settings.max_samples = 1 << 20
+    try:
+        for group in (jobs[:1], jobs[:3], jobs):
+            out = {}
+            for form in (0, 1):
+                ctx.set_trace_form(form)
+                ctx.set_tuning(4096, -1, steps)
+                for j in group:
+                    j.reset()
+                ctx.render_batch(group, 3)
+                out[form] = [j.readback().view(np.uint32).copy() for j in group]
+            for a, b in zip(out[0], out[1]):
+                np.testing.assert_array_equal(a, b)
+        ctx.set_trace_form(0)
+        jobs[0].reset()
+        c0 = jobs[0].render_counted(3)
+        ctx.set_trace_form(1)
+        jobs[0].reset()
+        c1 = jobs[0].render_counted(3)
+        np.testing.assert_array_equal(c0, c1)
+    finally:
+        ctx.set_trace_form(0)
+        ctx.set_tuning(1 << 23, 0, 16)
+        for m in made:
+            close_all(m[2], m[0], m[1])

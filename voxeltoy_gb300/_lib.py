@@ -197,6 +197,7 @@ SIGNATURES = {
     "vt_diag_scene_bricks": [P, P, C.c_size_t, C.POINTER(C.c_int64)],
     "vt_diag_set_tuning": [P, C.c_int64, C.c_int32, C.c_int32, C.c_int64],
     "vt_diag_set_trace_tuning": [P, C.c_int32, C.c_int32],
+    "vt_diag_set_trace_form": [P, C.c_int32],
     "vt_diag_set_noise_table": [P, P, C.c_size_t],
     "vt_diag_get_noise_table": [P, P, C.c_size_t],
 }

@@ -1406,6 +1406,7 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     P[l].trace_chunk = (uint32_t)ctx->trace_chunk;
     P[l].refill_min = ctx->refill_min;
     P[l].bricks_444 = all_444 ? 1 : 0;
+    P[l].trace_form = ctx->trace_form;
   }
   // control words zero (first stream empty), item counters at each lane's first item
   VT_CUDA(cudaMemsetAsync(ctx->wf_ctl, 0, vt_context::kMaxLanes * kCtlBytes, st), "wavefront control");
@@ -2021,8 +2022,14 @@ extern "C" int vt_diag_set_tuning(vt_context* ctx, int64_t slots, int32_t blocks
   VT_CHECK_ARG(ctx, "context is null");
   if (slots > 0) ctx->max_slots = std::max<int64_t>(32, std::min<int64_t>(slots, (int64_t)1 << 26));
   if (blocks_per_sm >= 0) ctx->trace_blocks_per_sm = blocks_per_sm;
-  if (steps > 0) ctx->trace_steps = steps <= 8 ? 8 : (steps <= 16 ? 16 : 32);
+  if (steps > 0) ctx->trace_steps = steps <= 4 ? 4 : (steps <= 8 ? 8 : (steps <= 16 ? 16 : 32));
   if (max_items > 0) ctx->max_items = std::max<int64_t>(1024, max_items);
+  return VT_OK;
+}
+
+extern "C" int vt_diag_set_trace_form(vt_context* ctx, int32_t form) {
+  VT_CHECK_ARG(ctx && (form == 0 || form == 1), "trace form must be 0 (per-lane set-up) or 1 (pooled set-up)");
+  ctx->trace_form = form;
   return VT_OK;
 }
 

@@ -110,6 +110,7 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   P.counters = nullptr;
   P.trace_chunk = (uint32_t)ctx->trace_chunk;
   P.refill_min = ctx->refill_min;
+  P.trace_form = ctx->trace_form;
   P.bricks_444 = 1;
   for (int i = 0; i < n; ++i)
     if (grids[i].shx != 2 || grids[i].shy != 2 || grids[i].shz != 2) P.bricks_444 = 0;

@@ -74,6 +74,7 @@ struct WfParams {
   float4* sbuf;                    // per-item sample outputs
   unsigned long long* counters;    // nullable
   int32_t bricks_444;              // every job's bricks are 4x4x4 (the DDA kernel's fixed-shape form)
+  int32_t trace_form;              // DDA kernel: 0 per-lane set-up, 1 pooled set-up (k_wf_trace_pool)
   uint32_t trace_chunk;            // queue records a trace warp takes per atomic (32-256)
   int32_t refill_min;              // trace warps refill early once fewer lanes step (0 = every
                                    // kTraceSteps steps only)

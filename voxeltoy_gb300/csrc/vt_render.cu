@@ -534,6 +534,108 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
   flush_counters(cnt, P.counters);
 }
 
+// One round of tracing, pooled form: each warp keeps up to kPoolSegs
+// segments set up and ready to step in shared memory.  The segment set-up
+// (dda_begin: nudge, divisions, floor, bounds test) runs for a warp's worth
+// of queue records at once, every lane busy; a lane whose segment ended takes
+// a ready one after each batch of kTraceSteps steps, so lanes rarely wait
+// for a set-up.  Same segments, same ends, same bits as k_wf_trace.
+constexpr int kPoolSegs = 64;
+constexpr int kTraceWarps = 8;   // 256-thread blocks
+
+__device__ __forceinline__ int32_t pack_signs(const Dda& t) {
+  return (t.sx + 1) | ((t.sy + 1) << 2) | ((t.sz + 1) << 4);
+}
+
+template <bool kCount, int kTraceSteps, bool k444, class Tab>
+__global__ void __launch_bounds__(256, 4) k_wf_trace_pool(const WfParams P, const __grid_constant__ Tab T, int par) {
+  __shared__ int32_t s_i[4][kTraceWarps][kPoolSegs];    // x, y, z, packed signs
+  __shared__ float s_f[6][kTraceWarps][kPoolSegs];      // dx, dy, dz, ax, ay, az
+  __shared__ uint32_t s_u[2][kTraceWarps][kPoolSegs];   // position << 1 | kind, job
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lt = (1u << lane) - 1u;
+  const uint32_t n = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_QCOUNT)];
+  if (n == 0) return;
+  const float4* q = P.queue[par];
+  Cnt<kCount> cnt;
+#pragma unroll
+  for (int i = 0; i < C_NUM; ++i) cnt.c[i] = 0;
+  uint32_t chunk = 0, chunk_end = 0;
+  bool exhausted = false, active = false;
+  int count = 0;   // ready segments in this warp's pool (the same in every lane)
+  GridHold<Tab> gh;
+  Dda s;
+  uint32_t tag = 0;
+  for (;;) {
+    // set up new segments, a warp's worth at a time, while the pool has room
+    while (count <= kPoolSegs - 32 && !exhausted) {
+      if (chunk >= chunk_end) {
+        uint32_t c = 0;
+        if (lane == 0) c = atomicAdd(&P.ctl[ctl_index(par, CTL_QHEAD)], P.trace_chunk);
+        c = __shfl_sync(FULL, c, 0);
+        if (c >= n) { exhausted = true; break; }
+        chunk = c;
+        chunk_end = min(c + P.trace_chunk, n);
+      }
+      const uint32_t rec = chunk + (uint32_t)lane;
+      chunk = min(chunk + 32u, chunk_end);
+      bool run = false;
+      Dda t;
+      uint32_t ttag = 0, tjob = 0;
+      if (rec < chunk_end) {
+        const float4 a = __ldg(&q[2 * (size_t)rec]), b = __ldg(&q[2 * (size_t)rec + 1]);
+        ttag = __float_as_uint(b.z);
+        tjob = __float_as_uint(b.w);
+        GridHold<Tab> tg;
+        tg.set(P, T, tjob);
+        dda_begin(tg.get(T), t, mk3(a.x, a.y, a.z), mk3(a.w, b.x, b.y));
+        run = t.state == DDA_RUNNING;
+        if (!run) P.hits[(size_t)(ttag & 1u) * P.n_slots + (ttag >> 1)] = pack_end(t.x, t.y, t.z, t.state);
+      }
+      const unsigned rm = __ballot_sync(FULL, run);
+      if (run) {
+        const int at = count + __popc(rm & lt);
+        s_i[0][warp][at] = t.x; s_i[1][warp][at] = t.y; s_i[2][warp][at] = t.z; s_i[3][warp][at] = pack_signs(t);
+        s_f[0][warp][at] = t.dx; s_f[1][warp][at] = t.dy; s_f[2][warp][at] = t.dz;
+        s_f[3][warp][at] = t.ax; s_f[4][warp][at] = t.ay; s_f[5][warp][at] = t.az;
+        s_u[0][warp][at] = ttag; s_u[1][warp][at] = tjob;
+      }
+      count += __popc(rm);
+    }
+    __syncwarp();
+    // lanes without a segment take ready ones, from the top of the pool
+    const unsigned need = __ballot_sync(FULL, !active);
+    const int take = min(__popc(need), count);
+    if (!active) {
+      const int r = __popc(need & lt);
+      if (r < take) {
+        const int at = count - 1 - r;
+        s.x = s_i[0][warp][at]; s.y = s_i[1][warp][at]; s.z = s_i[2][warp][at];
+        const int32_t sg = s_i[3][warp][at];
+        s.sx = (sg & 3) - 1; s.sy = ((sg >> 2) & 3) - 1; s.sz = ((sg >> 4) & 3) - 1;
+        s.dx = s_f[0][warp][at]; s.dy = s_f[1][warp][at]; s.dz = s_f[2][warp][at];
+        s.ax = s_f[3][warp][at]; s.ay = s_f[4][warp][at]; s.az = s_f[5][warp][at];
+        s.steps = 0; s.cb = -1; s.bits = 0ull; s.state = DDA_RUNNING;
+        tag = s_u[0][warp][at];
+        gh.set(P, T, s_u[1][warp][at]);
+        active = true;
+      }
+    }
+    count -= take;
+    __syncwarp();
+    if (!__any_sync(FULL, active)) break;   // pool empty and queue exhausted
+    if (active) {
+      dda_steps<kCount, false, k444>(gh.get(T), s, kTraceSteps, cnt, 0);
+      if (s.state != DDA_RUNNING) {
+        P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
+        active = false;
+      }
+    }
+  }
+  flush_counters(cnt, P.counters);
+}
+
 // Ordered reduction of the per-sample outputs into each pixel's Kahan sums:
 // sample order within a pixel is the same as one sample per launch.
 __global__ void k_wf_accumulate(const JobEntry* jobs, const float4* sbuf) {
@@ -585,6 +687,13 @@ static void wf_trace_steps(const WfParams& P, const Tab& T, int par, int blocks,
 template <bool k444, class Tab>
 static void wf_trace_shape(const WfParams& P, const Tab& T, int par, int blocks, int steps, bool count,
                            cudaStream_t st) {
+  if (P.trace_form == 1) {   // pooled set-up
+    if (count) k_wf_trace_pool<true, 8, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+    else if (steps <= 4) k_wf_trace_pool<false, 4, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+    else if (steps <= 8) k_wf_trace_pool<false, 8, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+    else k_wf_trace_pool<false, 16, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
+    return;
+  }
   if (count) k_wf_trace<true, 16, false, k444, Tab><<<blocks, 256, 0, st>>>(P, T, par);
   else if (P.refill_min > 0) wf_trace_steps<true, k444>(P, T, par, blocks, steps, st);
   else wf_trace_steps<false, k444>(P, T, par, blocks, steps, st);

@@ -44,6 +44,7 @@ struct vt_context {
   int trace_steps = 16;          // DDA steps between refills of the trace kernel
   int trace_chunk = 128;         // queue records per warp atomic of the trace kernel
   int refill_min = 0;            // early refill of a trace warp below this many stepping lanes (0 = off)
+  int trace_form = 0;            // DDA kernel form: 0 per-lane segment set-up, 1 pooled set-up
   uint64_t launches = 0;         // render kernels launched by this context
   cudaGraphExec_t rounds_exec = nullptr;   // eight rounds of every lane, replayed
   bool use_graphs = true;

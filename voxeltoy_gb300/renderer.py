@@ -83,6 +83,10 @@ class Context:
         of 32) and the early-refill threshold (0 = off); 0 / -1 keep a value."""
         L.call("vt_diag_set_trace_tuning", self.h, queue_chunk, refill_min)
 
+    def set_trace_form(self, form: int):
+        """DDA kernel form: 0 per-lane segment set-up, 1 pooled set-up (identical results)."""
+        L.call("vt_diag_set_trace_form", self.h, form)
+
     def launch_count(self) -> int:
         n = C.c_uint64()
         L.call("vt_diag_launch_count", self.h, C.byref(n))
