@@ -725,6 +725,8 @@ def main():
     ap.add_argument("--lanes", type=int, default=2, choices=[1, 2, 3, 4], help="wavefront lanes with --slots")
     ap.add_argument("--trace-steps", type=int, default=0, help="DDA steps between refills (with --slots)")
     ap.add_argument("--trace-bps", type=int, default=-1, help="trace blocks per SM, 0 = occupancy (with --slots)")
+    ap.add_argument("--trace-form", type=int, default=-1, choices=[-1, 0, 1],
+                    help="DDA kernel form with --slots: 0 per-lane set-up, 1 pooled set-up")
     ap.add_argument("--workload", default="config2",
                     choices=["config2", "config1", "batching", "serving", "voxelize"],
                     help="config2 (default, the headline line); config1 = the small plain case; batching = 64 uneven scenes in one launch vs "
@@ -794,8 +796,10 @@ def main():
     if args.slots > 0:
         ctx.set_lanes(args.lanes)
         ctx.set_tuning(args.slots, args.trace_bps, args.trace_steps)
+        if args.trace_form >= 0:
+            ctx.set_trace_form(args.trace_form)
         tuning = {"path_slots": args.slots, "trace_blocks_per_sm": args.trace_bps, "trace_steps": args.trace_steps,
-                  "lanes": args.lanes, "source": "command line"}
+                  "lanes": args.lanes, "trace_form": max(args.trace_form, 0), "source": "command line"}
     elif not args.no_tune and args.kernel == 2:
         from voxeltoy_gb300 import autotune
         best = autotune.tune(ctx, [job], passes=cfg.spp, repeats=1, use_cache=False)

@@ -45,6 +45,9 @@ class FakeCtx:
     def set_trace_tuning(self, queue_chunk, refill_min):
         self.setting.update(queue_chunk=queue_chunk, refill_min=refill_min)
 
+    def set_trace_form(self, form):
+        self.setting["trace_form"] = form
+
     def render_batch(self, jobs, passes):
         for j in jobs:
             j.render(passes)
@@ -77,6 +80,7 @@ class FakeJob:
         cost += 0.01 * abs(s.get("queue_chunk", 128) - 64) / 64
         cost += 0.002 * abs(s.get("refill_min", 0) - 12)
         cost += 0.0 if self.scene.shape == (3, 2, 1) else 0.004
+        cost += 0.05 * s.get("trace_form", 0)
         self.clock[0] += cost * passes * self.unit
         self.renders += 1
 
@@ -96,12 +100,14 @@ def test_sweep_picks_the_fastest_setting(fake_time, tmp_path, monkeypatch):
     assert (best["path_slots"], best["trace_blocks_per_sm"], best["trace_steps"], best["lanes"],
             best["brick_shape"], best["queue_chunk"], best["refill_min"]) == (1 << 23, 3, 16, 2, (3, 2, 1), 64, 12)
     assert ctx.setting == {"path_slots": 1 << 23, "trace_blocks_per_sm": 3, "trace_steps": 16, "lanes": 2,
-                           "brick_shape": (3, 2, 1), "queue_chunk": 64, "refill_min": 12}
+                           "brick_shape": (3, 2, 1), "queue_chunk": 64, "refill_min": 12, "trace_form": 0}
+    assert best["trace_form"] == 0
     assert job.scene.shape == (3, 2, 1)
     g = autotune.DEFAULT_GRID
-    # the launch-shape grid, then bricks and the DDA kernel's knobs at the best launch shape
+    # the launch-shape grid, then bricks and the DDA kernel's knobs at the best launch shape, then the pooled form
     assert len(best["sweep"]) == len(g["path_slots"]) * len(g["trace_blocks_per_sm"]) * len(g["trace_steps"]) * \
-        len(g["lanes"]) + len(g["brick_shape"]) * len(g["queue_chunk"]) * len(g["refill_min"]) - 1
+        len(g["lanes"]) + len(g["brick_shape"]) * len(g["queue_chunk"]) * len(g["refill_min"]) - 1 + \
+        len(g["trace_form_steps"])
     assert not (tmp_path / "tune.json").exists()
 
 

@@ -13,6 +13,9 @@ and then, at the best of those, a second sweep of
   refill_min            compaction threshold: a DDA warp refills its lanes as
                         soon as fewer than this many still step (0 = only
                         every trace_steps steps)
+and last the pooled form of the DDA kernel (segment set-up for a warp's
+worth of records at once, lanes refilled from a shared-memory pool) at
+trace_form_steps steps per batch.
 and applies the fastest setting to the context.  Every setting renders the
 same bits.  Path-slot counts above the workload's samples collapse to one
 setting; frames shorter than a few milliseconds are timed several times per
@@ -37,8 +40,9 @@ DEFAULT_GRID = {
     "brick_shape": [(2, 2, 2), (3, 2, 1), (1, 3, 2), (2, 1, 3)],
     "queue_chunk": [128, 64, 256],
     "refill_min": [0, 12, 20],
+    "trace_form_steps": [8, 16],
 }
-KNOBS = "slots,bps,steps,lanes,brick,chunk,refill"
+KNOBS = "slots,bps,steps,lanes,brick,chunk,refill,form"
 
 
 def cache_path() -> Path:
@@ -59,6 +63,8 @@ def _apply(ctx, setting: dict, jobs=()):
     ctx.set_lanes(setting.get("lanes", 2))
     ctx.set_tuning(setting["path_slots"], setting["trace_blocks_per_sm"], setting["trace_steps"])
     ctx.set_trace_tuning(setting.get("queue_chunk", 128), setting.get("refill_min", 0))
+    if hasattr(ctx, "set_trace_form"):
+        ctx.set_trace_form(setting.get("trace_form", 0))
     shape = tuple(setting.get("brick_shape", (2, 2, 2)))
     for sc in {id(j.scene): j.scene for j in jobs}.values():
         if tuple(sc.brick_shape()) != shape:
@@ -113,7 +119,7 @@ def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None
                                                       grid["trace_steps"]):
         setting = {"path_slots": slots, "trace_blocks_per_sm": bps, "trace_steps": steps, "lanes": lanes,
                    "brick_shape": tuple(grid["brick_shape"][0]), "queue_chunk": grid["queue_chunk"][0],
-                   "refill_min": grid["refill_min"][0]}
+                   "refill_min": grid["refill_min"][0], "trace_form": 0}
         _apply(ctx, setting, jobs)
         results.append((_time_render(ctx, jobs, passes, reps), setting))
     results.sort(key=lambda r: r[0])
@@ -124,6 +130,13 @@ def tune(ctx, jobs, passes: int = 16, repeats: int = 2, grid: dict | None = None
         if (tuple(shape), chunk, refill) == (first["brick_shape"], first["queue_chunk"], first["refill_min"]):
             continue
         setting = dict(first, brick_shape=tuple(shape), queue_chunk=chunk, refill_min=refill)
+        _apply(ctx, setting, jobs)
+        results.append((_time_render(ctx, jobs, passes, reps), setting))
+    results.sort(key=lambda r: r[0])
+    # the pooled DDA form at the best setting so far (the compaction threshold does not apply to it)
+    second = dict(results[0][1])
+    for steps in grid.get("trace_form_steps", []):
+        setting = dict(second, trace_form=1, trace_steps=steps, refill_min=0)
         _apply(ctx, setting, jobs)
         results.append((_time_render(ctx, jobs, passes, reps), setting))
     results.sort(key=lambda r: r[0])
