@@ -543,7 +543,11 @@ __device__ __forceinline__ void tri_column(const TriSetup& S, int px, int py, in
     else { ox = px; oy = py; oz = pz; }
     // imageStore outside the image has no effect
     if (ox < 0 || oy < 0 || oz < 0 || ox >= rx || oy >= ry || oz >= rz) continue;
-    O.grid[(size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz)] = O.value;
+    uint8_t* cell = O.grid + ((size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz));
+    // a voxel another triangle already marked has its brick bit already (or
+    // about to be) set by that triangle: only the first marks set it here
+    if (*cell == O.value) continue;
+    *cell = O.value;
     if (O.bricks)
       atomicOr(&O.bricks[brick_index_of(O.sh, O.bx, O.by, ox, oy, oz)], 1ull << brick_bit_of(O.sh, ox, oy, oz));
   }
@@ -617,31 +621,36 @@ cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indi
   return cudaGetLastError();
 }
 
-// One thread per brick of the padded grid: all bits of border bricks, and of
-// interior bricks the bits of voxels at or beyond (rx, ry, rz).
+// Bricks of an empty volume, one thread per brick of the padded grid (x
+// from the thread, y and z from the block, grid-strided beyond the launch
+// limits): all bits of border bricks, and of interior bricks the bits of
+// voxels at or beyond (rx, ry, rz).
 __global__ void k_bricks_init(unsigned long long* __restrict__ bricks, int32_t rx, int32_t ry, int32_t rz,
                               int32_t bx, int32_t by, int32_t bz, const BrickShape sh) {
-  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t px = bx + 2, py = by + 2, pz = bz + 2;
-  if (b >= px * py * pz) return;
+  const int px = bx + 2, py = by + 2, pz = bz + 2;
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ix >= px) return;
   const int ex = 1 << sh.sx, ey = 1 << sh.sy, ez = 1 << sh.sz;
-  const int x0 = ((int)(b % px) - 1) * ex;
-  const int y0 = ((int)((b / px) % py) - 1) * ey;
-  const int z0 = ((int)(b / (px * py)) - 1) * ez;
-  unsigned long long w = 0ull;
-  if (x0 < 0 || y0 < 0 || z0 < 0 || x0 + ex > rx || y0 + ey > ry || z0 + ez > rz) {
-    for (int k = 0; k < 64; ++k) {
-      const int x = x0 + (k & (ex - 1)), y = y0 + ((k >> sh.sx) & (ey - 1)), z = z0 + (k >> (sh.sx + sh.sy));
-      if (x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz) w |= 1ull << k;
+  const int x0 = (ix - 1) * ex;
+  for (int iz = blockIdx.z; iz < pz; iz += gridDim.z)
+    for (int iy = blockIdx.y; iy < py; iy += gridDim.y) {
+      const int y0 = (iy - 1) * ey, z0 = (iz - 1) * ez;
+      unsigned long long w = 0ull;
+      if (x0 < 0 || y0 < 0 || z0 < 0 || x0 + ex > rx || y0 + ey > ry || z0 + ez > rz) {
+        for (int k = 0; k < 64; ++k) {
+          const int x = x0 + (k & (ex - 1)), y = y0 + ((k >> sh.sx) & (ey - 1)), z = z0 + (k >> (sh.sx + sh.sy));
+          if (x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz) w |= 1ull << k;
+        }
+      }
+      bricks[(size_t)ix + (size_t)px * ((size_t)iy + (size_t)py * (size_t)iz)] = w;
     }
-  }
-  bricks[b] = w;
 }
 
 cudaError_t launch_bricks_init(unsigned long long* bricks, int32_t rx, int32_t ry, int32_t rz, int32_t bx,
                                int32_t by, int32_t bz, const BrickShape& sh, cudaStream_t st) {
-  const int64_t nb = (int64_t)(bx + 2) * (by + 2) * (bz + 2);
-  k_bricks_init<<<(unsigned)((nb + 255) / 256), 256, 0, st>>>(bricks, rx, ry, rz, bx, by, bz, sh);
+  const dim3 grid((unsigned)((bx + 2 + 127) / 128), (unsigned)std::min(by + 2, 65535),
+                  (unsigned)std::min(bz + 2, 65535));
+  k_bricks_init<<<grid, 128, 0, st>>>(bricks, rx, ry, rz, bx, by, bz, sh);
   return cudaGetLastError();
 }
 
