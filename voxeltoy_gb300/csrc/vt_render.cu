@@ -293,17 +293,19 @@ __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __
     cnt.add(C_POSITIONS, 1);
     const uint32_t job = fl >> kSlotJobShift;
     const JobEntry& E = job_entry(P, T, job);
+    // every load of the position is issued before any of them is used (the
+    // origin is read for every extension, whether or not it hits)
+    const unsigned long long hs = (fl & SL_SHADOW) ? P.hits[(size_t)P.n_slots + i] : 0ull;
+    const unsigned long long he = (fl & SL_EXT) ? P.hits[i] : 0ull;
+    const float4 a0v = (fl & SL_EXT) ? src.a0[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     load_for_shade(src, i, fl, p, item, rng_word);
-    if (fl & SL_SHADOW) {
-      const SegEnd se = unpack_end(P.hits[(size_t)P.n_slots + i]);
-      shadow_end(E.F, p, se);
-    }
+    if (fl & SL_SHADOW) shadow_end(E.F, p, unpack_end(hs));
     if (fl & SL_EXT) {
-      e = unpack_end(P.hits[i]);
+      e = unpack_end(he);
       hit = ext_resolve(E.F, E.J, p, e, cnt);
       if (hit) cls = hit_class(E.F, E.J, e);
     }
-    if (hit) p.ro = xyz4(src.a0[i]);
+    if (hit) p.ro = xyz4(a0v);
     else if (chk(item < P.n_items, CHK_SAMPLE)) P.sbuf[item] = path_output(E.F, p);
   }
   uint32_t* const ctr[2] = {&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)], &P.ctl[ctl_index(par, CTL_HITS_OTHER)]};

@@ -543,11 +543,7 @@ __device__ __forceinline__ void tri_column(const TriSetup& S, int px, int py, in
     else { ox = px; oy = py; oz = pz; }
     // imageStore outside the image has no effect
     if (ox < 0 || oy < 0 || oz < 0 || ox >= rx || oy >= ry || oz >= rz) continue;
-    uint8_t* cell = O.grid + ((size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz));
-    // a voxel another triangle already marked has its brick bit already (or
-    // about to be) set by that triangle: only the first marks set it here
-    if (*cell == O.value) continue;
-    *cell = O.value;
+    O.grid[(size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz)] = O.value;
     if (O.bricks)
       atomicOr(&O.bricks[brick_index_of(O.sh, O.bx, O.by, ox, oy, oz)], 1ull << brick_bit_of(O.sh, ox, oy, oz));
   }
@@ -621,10 +617,10 @@ cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indi
   return cudaGetLastError();
 }
 
-// Bricks of an empty volume, one thread per brick of the padded grid (x
-// from the thread, y and z from the block, grid-strided beyond the launch
-// limits): all bits of border bricks, and of interior bricks the bits of
-// voxels at or beyond (rx, ry, rz).
+// Bricks of an empty volume, one thread per brick of a row of the padded
+// grid (x from the thread, rows y and z grid-strided over the blocks): all
+// bits of border bricks, and of interior bricks the bits of voxels at or
+// beyond (rx, ry, rz).
 __global__ void k_bricks_init(unsigned long long* __restrict__ bricks, int32_t rx, int32_t ry, int32_t rz,
                               int32_t bx, int32_t by, int32_t bz, const BrickShape sh) {
   const int px = bx + 2, py = by + 2, pz = bz + 2;
@@ -648,8 +644,9 @@ __global__ void k_bricks_init(unsigned long long* __restrict__ bricks, int32_t r
 
 cudaError_t launch_bricks_init(unsigned long long* bricks, int32_t rx, int32_t ry, int32_t rz, int32_t bx,
                                int32_t by, int32_t bz, const BrickShape& sh, cudaStream_t st) {
-  const dim3 grid((unsigned)((bx + 2 + 127) / 128), (unsigned)std::min(by + 2, 65535),
-                  (unsigned)std::min(bz + 2, 65535));
+  // a few thousand blocks that each loop over rows: one block per row would
+  // spend the launch on scheduling blocks of a single row each
+  const dim3 grid((unsigned)((bx + 2 + 127) / 128), (unsigned)std::min(by + 2, 32), (unsigned)std::min(bz + 2, 32));
   k_bricks_init<<<grid, 128, 0, st>>>(bricks, rx, ry, rz, bx, by, bz, sh);
   return cudaGetLastError();
 }
