@@ -478,8 +478,15 @@ struct GridHold<WfOneJob> {
 // while it steps the current one, so starting a segment never waits on
 // memory, and lanes pick up a new segment every kTraceSteps steps as theirs
 // finish (with kVote also as soon as fewer than P.refill_min lanes step).
+// Resident blocks the trace kernel is compiled for: six with one job (its
+// grid record is constant), five with a job table, whose per-lane grid
+// record would otherwise spill at six blocks' 40 registers.
+template <class Tab> struct TraceBlocks { static constexpr int value = 5; };
+template <> struct TraceBlocks<WfOneJob> { static constexpr int value = 6; };
+
 template <bool kCount, int kTraceSteps, bool kVote, bool k444, class Tab>
-__global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __grid_constant__ Tab T, int par) {
+__global__ void __launch_bounds__(256, TraceBlocks<Tab>::value) k_wf_trace(const WfParams P, const __grid_constant__ Tab T, int par) {
+  static_assert(kTraceSteps % 4 == 0, "the 4x4x4 loop steps four at a time");
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -526,7 +533,8 @@ __global__ void __launch_bounds__(256, 6) k_wf_trace(const WfParams P, const __g
     }
     if (__ballot_sync(FULL, have || have_next) == 0u) break;
     if (have) {
-      dda_steps<kCount, kVote, k444>(gh.get(T), s, kTraceSteps, cnt, P.refill_min);
+      if constexpr (!kCount && k444) dda_steps_444<kVote>(gh.get(T), s, kTraceSteps, P.refill_min);
+      else dda_steps<kCount, kVote, k444>(gh.get(T), s, kTraceSteps, cnt, P.refill_min);
       if (s.state != DDA_RUNNING) {
         P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
         have = false;
@@ -551,6 +559,7 @@ __device__ __forceinline__ int32_t pack_signs(const Dda& t) {
 
 template <bool kCount, int kTraceSteps, bool k444, class Tab>
 __global__ void __launch_bounds__(256, 4) k_wf_trace_pool(const WfParams P, const __grid_constant__ Tab T, int par) {
+  static_assert(kTraceSteps % 4 == 0, "the 4x4x4 loop steps four at a time");
   __shared__ int32_t s_i[4][kTraceWarps][kPoolSegs];    // x, y, z, packed signs
   __shared__ float s_f[6][kTraceWarps][kPoolSegs];      // dx, dy, dz, ax, ay, az
   __shared__ uint32_t s_u[2][kTraceWarps][kPoolSegs];   // position << 1 | kind, job
@@ -628,7 +637,8 @@ __global__ void __launch_bounds__(256, 4) k_wf_trace_pool(const WfParams P, cons
     __syncwarp();
     if (!__any_sync(FULL, active)) break;   // pool empty and queue exhausted
     if (active) {
-      dda_steps<kCount, false, k444>(gh.get(T), s, kTraceSteps, cnt, 0);
+      if constexpr (!kCount && k444) dda_steps_444<false>(gh.get(T), s, kTraceSteps, 0);
+      else dda_steps<kCount, false, k444>(gh.get(T), s, kTraceSteps, cnt, 0);
       if (s.state != DDA_RUNNING) {
         P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
         active = false;
@@ -745,7 +755,7 @@ void wf_carve(void* mem, size_t S, WfParams& P) {
 
 int wf_trace_blocks_per_sm() {
   int n = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8, false, true, WfJobTable>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_wf_trace<false, 8, false, true, WfOneJob>, 256, 0);
   return n;
 }
 

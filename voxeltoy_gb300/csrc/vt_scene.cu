@@ -512,8 +512,26 @@ struct VoxOut {
   BrickShape sh;
 };
 
+// Brick bits a thread has set, gathered while they fall in one brick and
+// OR'ed into the brick grid with one atomic when the brick changes.
+struct BrickAcc {
+  int64_t b = -1;
+  unsigned long long bits = 0ull;
+  __device__ __forceinline__ void add(const VoxOut& O, int64_t nb, unsigned long long bit) {
+    if (nb != b) {
+      flush(O);
+      b = nb;
+    }
+    bits |= bit;
+  }
+  __device__ __forceinline__ void flush(const VoxOut& O) {
+    if (bits) atomicOr(&O.bricks[b], bits);
+    bits = 0ull;
+  }
+};
+
 __device__ __forceinline__ void tri_column(const TriSetup& S, int px, int py, int mode, int32_t rx, int32_t ry,
-                                           int32_t rz, const VoxOut& O) {
+                                           int32_t rz, const VoxOut& O, BrickAcc& acc) {
   bool xy = true;
   for (int k = 0; k < 3; ++k) {
     const float dd = S.d_xy[k] + (S.n_xy[k][0] * (float)px + S.n_xy[k][1] * (float)py);
@@ -544,8 +562,7 @@ __device__ __forceinline__ void tri_column(const TriSetup& S, int px, int py, in
     // imageStore outside the image has no effect
     if (ox < 0 || oy < 0 || oz < 0 || ox >= rx || oy >= ry || oz >= rz) continue;
     O.grid[(size_t)ox + (size_t)rx * ((size_t)oy + (size_t)ry * (size_t)oz)] = O.value;
-    if (O.bricks)
-      atomicOr(&O.bricks[brick_index_of(O.sh, O.bx, O.by, ox, oy, oz)], 1ull << brick_bit_of(O.sh, ox, oy, oz));
+    if (O.bricks) acc.add(O, brick_index_of(O.sh, O.bx, O.by, ox, oy, oz), 1ull << brick_bit_of(O.sh, ox, oy, oz));
   }
   (void)mode;
 }
@@ -567,8 +584,10 @@ __global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restr
     large[slot] = t;
     return;
   }
+  BrickAcc acc;
   for (int px = S.lo[0]; px < S.hi[0]; ++px)
-    for (int py = S.lo[1]; py < S.hi[1]; ++py) tri_column(S, px, py, mode, rx, ry, rz, O);
+    for (int py = S.lo[1]; py < S.hi[1]; ++py) tri_column(S, px, py, mode, rx, ry, rz, O, acc);
+  if (O.bricks) acc.flush(O);
 }
 
 __global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restrict__ I, const int64_t* large,
@@ -582,10 +601,12 @@ __global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restr
     __syncthreads();
     const int wx = S.hi[0] - S.lo[0], wy = S.hi[1] - S.lo[1];
     const int64_t cols = (int64_t)wx * wy;
+    BrickAcc acc;
     for (int64_t c = threadIdx.x; c < cols; c += blockDim.x) {
       const int px = S.lo[0] + (int)(c / wy), py = S.lo[1] + (int)(c % wy);
-      tri_column(S, px, py, mode, rx, ry, rz, O);
+      tri_column(S, px, py, mode, rx, ry, rz, O, acc);
     }
+    if (O.bricks) acc.flush(O);
   }
 }
 
@@ -617,37 +638,56 @@ cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indi
   return cudaGetLastError();
 }
 
-// Bricks of an empty volume, one thread per brick of a row of the padded
-// grid (x from the thread, rows y and z grid-strided over the blocks): all
-// bits of border bricks, and of interior bricks the bits of voxels at or
-// beyond (rx, ry, rz).
-__global__ void k_bricks_init(unsigned long long* __restrict__ bricks, int32_t rx, int32_t ry, int32_t rz,
-                              int32_t bx, int32_t by, int32_t bz, const BrickShape sh) {
-  const int px = bx + 2, py = by + 2, pz = bz + 2;
-  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ix >= px) return;
+// Word of brick (ix, iy, iz) of the padded grid of an empty volume: all bits
+// of a border brick, and of an interior brick the bits of voxels at or
+// beyond (rx, ry, rz); zero for every other brick.
+__device__ __forceinline__ unsigned long long empty_brick_word(int ix, int iy, int iz, int32_t px, int32_t py,
+                                                               int32_t pz, int32_t rx, int32_t ry, int32_t rz,
+                                                               const BrickShape& sh) {
+  if (ix == 0 || iy == 0 || iz == 0 || ix == px - 1 || iy == py - 1 || iz == pz - 1) return ~0ull;   // border
   const int ex = 1 << sh.sx, ey = 1 << sh.sy, ez = 1 << sh.sz;
-  const int x0 = (ix - 1) * ex;
-  for (int iz = blockIdx.z; iz < pz; iz += gridDim.z)
-    for (int iy = blockIdx.y; iy < py; iy += gridDim.y) {
-      const int y0 = (iy - 1) * ey, z0 = (iz - 1) * ez;
-      unsigned long long w = 0ull;
-      if (x0 < 0 || y0 < 0 || z0 < 0 || x0 + ex > rx || y0 + ey > ry || z0 + ez > rz) {
-        for (int k = 0; k < 64; ++k) {
-          const int x = x0 + (k & (ex - 1)), y = y0 + ((k >> sh.sx) & (ey - 1)), z = z0 + (k >> (sh.sx + sh.sy));
-          if (x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz) w |= 1ull << k;
-        }
-      }
-      bricks[(size_t)ix + (size_t)px * ((size_t)iy + (size_t)py * (size_t)iz)] = w;
+  const int x0 = (ix - 1) * ex, y0 = (iy - 1) * ey, z0 = (iz - 1) * ez;
+  unsigned long long w = 0ull;
+  if (x0 < 0 || y0 < 0 || z0 < 0 || x0 + ex > rx || y0 + ey > ry || z0 + ez > rz) {
+    for (int k = 0; k < 64; ++k) {
+      const int x = x0 + (k & (ex - 1)), y = y0 + ((k >> sh.sx) & (ey - 1)), z = z0 + (k >> (sh.sx + sh.sy));
+      if (x < 0 || y < 0 || z < 0 || x >= rx || y >= ry || z >= rz) w |= 1ull << k;
     }
+  }
+  return w;
+}
+
+// The bricks of an empty volume that are not zero, over a zeroed array: the
+// border and the last interior brick along each axis (the only interior
+// bricks that can reach past the volume).  One warp per row of the padded
+// grid: rows in the y or z shell are written whole, the others at their
+// three x-shell bricks (0, px - 2, px - 1).
+__global__ void k_bricks_shell(unsigned long long* __restrict__ bricks, int32_t rx, int32_t ry, int32_t rz,
+                               int32_t bx, int32_t by, int32_t bz, const BrickShape sh) {
+  const int px = bx + 2, py = by + 2, pz = bz + 2;
+  const int lane = threadIdx.x & 31;
+  const int64_t rows = (int64_t)py * pz;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < rows; r += warps) {
+    const int iz = (int)(r / py), iy = (int)(r - (int64_t)iz * py);
+    unsigned long long* row = bricks + r * px;
+    if (iy == 0 || iy >= py - 2 || iz == 0 || iz >= pz - 2) {
+      for (int ix = lane; ix < px; ix += 32) row[ix] = empty_brick_word(ix, iy, iz, px, py, pz, rx, ry, rz, sh);
+    } else if (lane < 3) {
+      const int ix = lane == 0 ? 0 : px - 3 + lane;
+      row[ix] = empty_brick_word(ix, iy, iz, px, py, pz, rx, ry, rz, sh);
+    }
+  }
 }
 
 cudaError_t launch_bricks_init(unsigned long long* bricks, int32_t rx, int32_t ry, int32_t rz, int32_t bx,
                                int32_t by, int32_t bz, const BrickShape& sh, cudaStream_t st) {
-  // a few thousand blocks that each loop over rows: one block per row would
-  // spend the launch on scheduling blocks of a single row each
-  const dim3 grid((unsigned)((bx + 2 + 127) / 128), (unsigned)std::min(by + 2, 32), (unsigned)std::min(bz + 2, 32));
-  k_bricks_init<<<grid, 128, 0, st>>>(bricks, rx, ry, rz, bx, by, bz, sh);
+  // a linear zero fill runs at copy bandwidth; the shell is a few rows' worth
+  const int64_t px = bx + 2, py = by + 2, pz = bz + 2;
+  cudaError_t e = cudaMemsetAsync(bricks, 0, sizeof(unsigned long long) * (size_t)(px * py * pz), st);
+  if (e != cudaSuccess) return e;
+  const int64_t blocks = std::min<int64_t>((py * pz + 7) / 8, 8192);
+  k_bricks_shell<<<(unsigned)blocks, 256, 0, st>>>(bricks, rx, ry, rz, bx, by, bz, sh);
   return cudaGetLastError();
 }
 
