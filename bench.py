@@ -664,8 +664,9 @@ def config1_rmse(ctx) -> dict:
 
 def profile_voxelize(args, local):
     """--workload voxelize --profile: the config-5 scene (1024^3 from the
-    1.3M-triangle mesh) rendered at 2048^2 x --spp samples with the launch
-    shape given on the command line, a frame per step, for ncu captures."""
+    1.3M-triangle mesh, voxelized 1 + --warmup times, each scene but the last
+    closed) rendered at 2048^2 x --spp samples with the launch shape given on
+    the command line, a frame per step, for ncu captures."""
     from voxeltoy_gb300 import Context, Job, Scene, scenes as S
     from voxeltoy_gb300 import _lib as L
     v, f = S.fbm_displaced_icosphere(level=8)
@@ -673,9 +674,15 @@ def profile_voxelize(args, local):
     if args.slots > 0:
         ctx.set_lanes(args.lanes)
         ctx.set_tuning(args.slots, args.trace_bps, args.trace_steps)
-    sc = Scene.voxelize(ctx, np.ascontiguousarray(v, np.float32), np.ascontiguousarray(f, np.uint32),
-                        (1024, 1024, 1024), mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
-                        palette=[S.lambert(0.7)])
+    sc = None
+    for k in range(1 + args.warmup):
+        if sc is not None:
+            sc.close()
+        t0 = time.perf_counter()
+        sc = Scene.voxelize(ctx, np.ascontiguousarray(v, np.float32), np.ascontiguousarray(f, np.uint32),
+                            (1024, 1024, 1024), mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE,
+                            palette=[S.lambert(0.7)])
+        print(json.dumps({"voxelize_ms": 1e3 * (time.perf_counter() - t0)}), flush=True)
     cfg = S.config1(edge=8, width=2048, height=2048, spp=args.spp)
     cfg.settings.max_bounces = 8
     job = Job(ctx, sc, None, cfg.camera, cfg.settings, 2048, 2048)

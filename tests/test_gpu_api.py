@@ -242,6 +242,32 @@ def test_obj_scene_matches_mesh_voxelization(ctx):
             a.close(); b.close()
 
 
+def test_voxelize_rejects_out_of_range_indices(ctx):
+    """A triangle index at or past the vertex count fails the call with
+    VT_EINVAL naming the largest such index (the check runs on the device,
+    which skips those triangles); the context stays usable."""
+    v, f = S.icosphere(2)
+    v = np.ascontiguousarray(v, np.float32)
+    bad = np.array(f, np.uint32)
+    bad[5, 1] = len(v)
+    bad[9, 2] = len(v) + 7
+    sc = Scene.voxelize(ctx, v, f, (40, 40, 40), mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE)
+    want = sc.voxels()
+    sc.close()
+    base = ctx.memory()   # the context's scratch is sized for this mesh now
+    for placement in (L.VT_MESH_FIT_UNIT_CUBE, L.VT_MESH_VOXEL_SPACE):
+        with pytest.raises(L.VtError) as e:
+            Scene.voxelize(ctx, v * 10 + 20, bad, (40, 40, 40), mode=L.VT_VOXELIZE_FAT, placement=placement)
+        assert e.value.code == L.VT_EINVAL and f"index {len(v) + 7} out of range" in str(e.value)
+        assert ctx.memory() == base
+    sc = Scene.voxelize(ctx, v, f, (40, 40, 40), mode=L.VT_VOXELIZE_FAT, placement=L.VT_MESH_FIT_UNIT_CUBE)
+    try:
+        assert np.count_nonzero(want) > 0
+        np.testing.assert_array_equal(sc.voxels(), want)
+    finally:
+        sc.close()
+
+
 def test_voxel_edits_match_a_rebuilt_scene(ctx):
     """set_voxel keeps grid, bricks and the emissive list equal to a scene
     built from the edited volume: same voxels, same emissive list, same image."""

@@ -497,35 +497,6 @@ extern "C" int vt_scene_create_from_offsets(vt_context* ctx, int32_t rx, int32_t
   return rc;
 }
 
-// computeMeshTransform (src/renderer/import.cpp:46-64) followed by the vertex
-// shader's modelTransform * v, * voxelResolution (voxelize.vs:20-27).
-static void fit_unit_cube(const float* v, int64_t nv, int32_t rx, int32_t ry, int32_t rz, std::vector<float>& out) {
-  float bmin[3] = {INFINITY, INFINITY, INFINITY}, bmax[3] = {-INFINITY, -INFINITY, -INFINITY};
-  for (int64_t i = 0; i < nv; ++i)
-    for (int c = 0; c < 3; ++c) {
-      bmin[c] = std::min(bmin[c], v[3 * i + c]);
-      bmax[c] = std::max(bmax[c], v[3 * i + c]);
-    }
-  const float res[3] = {(float)rx, (float)ry, (float)rz};
-  float size[3], margin[3];
-  for (int c = 0; c < 3; ++c) { size[c] = bmax[c] - bmin[c]; margin[c] = 1.0f / res[c]; }
-  int major = 0;
-  if (size[1] > size[major]) major = 1;
-  if (size[2] > size[major]) major = 2;
-  const float s = (float)((1.0f - 2.0 * (double)margin[major]) / (double)size[major]);
-  float t[3];
-  for (int c = 0; c < 3; ++c) t[c] = -bmin[c] + margin[c] / s;
-  float M[16] = {s, 0, 0, t[0] * s, 0, s, 0, t[1] * s, 0, 0, s, t[2] * s, 0, 0, 0, 1.0f};
-  out.resize(3 * nv);
-  for (int64_t i = 0; i < nv; ++i) {
-    const float x = v[3 * i], y = v[3 * i + 1], z = v[3 * i + 2];
-    for (int r = 0; r < 3; ++r) {
-      const float p = ((M[4 * r] * x + M[4 * r + 1] * y) + M[4 * r + 2] * z) + M[4 * r + 3] * 1.0f;
-      out[3 * i + r] = p * res[r];
-    }
-  }
-}
-
 extern "C" int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices, int64_t n_vertices,
                                       const uint32_t* indices, int64_t n_triangles, int32_t rx, int32_t ry,
                                       int32_t rz, int32_t mode, int32_t placement, const vt_material* palette,
@@ -538,20 +509,14 @@ extern "C" int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices, in
                    (mode & ~VT_VOXELIZE_REFERENCE_BOUNDS) == VT_VOXELIZE_FAT,
                "unknown voxelization mode");
   VT_CHECK_ARG(palette && n_palette >= 1 && n_palette <= 255, "palette needs 1..255 entries");
-  for (int64_t i = 0; i < 3 * n_triangles; ++i)
-    if ((int64_t)indices[i] >= n_vertices) return fail(VT_EINVAL, "triangle index %u out of range", indices[i]);
   vt_scene* s = nullptr;
   int rc = scene_alloc(ctx, rx, ry, rz, out, &s);
   if (rc != VT_OK) return rc;
   const int64_t nvox = (int64_t)rx * ry * rz;
-  std::vector<float> vs;
-  const float* vsrc = vertices;
-  if (placement == VT_MESH_FIT_UNIT_CUBE && n_vertices > 0) {
-    fit_unit_cube(vertices, n_vertices, rx, ry, rz, vs);
-    vsrc = vs.data();
-  }
   // mesh and the large-triangle list through the budgeted allocator; the
-  // voxelizer sets the brick bits itself, so no separate brick pass follows
+  // indices are checked and computeMeshTransform (import.cpp:46-64) applied
+  // on the device, and the voxelizer sets the brick bits itself, so no
+  // host pass over the mesh and no separate brick pass follow
   float* d_v = nullptr;
   uint32_t* d_i = nullptr;
   const int64_t nb = (int64_t)(s->bdim[0] + 2) * (s->bdim[1] + 2) * (s->bdim[2] + 2);
@@ -564,17 +529,28 @@ extern "C" int vt_scene_voxelize_mesh(vt_context* ctx, const float* vertices, in
   if (e == cudaSuccess)
     e = launch_bricks_init(s->bricks, rx, ry, rz, s->bdim[0], s->bdim[1], s->bdim[2], scene_shape(s), ctx->stream);
   if (e == cudaSuccess && n_vertices)
-    e = cudaMemcpyAsync(d_v, vsrc, sizeof(float) * 3 * n_vertices, cudaMemcpyHostToDevice, ctx->stream);
+    e = cudaMemcpyAsync(d_v, vertices, sizeof(float) * 3 * n_vertices, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && n_triangles)
     e = cudaMemcpyAsync(d_i, indices, sizeof(uint32_t) * 3 * n_triangles, cudaMemcpyHostToDevice, ctx->stream);
+  MeshPrep* prep = voxelize_prep_record(ctx->scratch, n_triangles);
   if (e == cudaSuccess)
-    e = launch_voxelize(d_v, d_i, n_triangles, rx, ry, rz, mode & 1, (mode & VT_VOXELIZE_REFERENCE_BOUNDS) != 0,
-                        s->grid, 1, s->bricks, s->bdim[0], s->bdim[1], scene_shape(s), ctx->scratch,
-                        ctx->sm_count * 4, ctx->stream);
+    e = launch_mesh_prep(d_v, n_vertices, d_i, n_triangles, placement == VT_MESH_FIT_UNIT_CUBE, rx, ry, rz, prep,
+                         ctx->sm_count, ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_voxelize(d_v, n_vertices, d_i, n_triangles, rx, ry, rz, mode & 1,
+                        (mode & VT_VOXELIZE_REFERENCE_BOUNDS) != 0, s->grid, 1, s->bricks, s->bdim[0], s->bdim[1],
+                        scene_shape(s), ctx->scratch, ctx->sm_count * 4, ctx->stream);
+  unsigned long long bad = 0ull;   // pageable destination: written when the copy returns
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&bad, &prep->bad, sizeof(bad), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   ctx->release(d_v);
   ctx->release(d_i);
   if (e != cudaSuccess) { delete s; return cuda_fail(e, "voxelization"); }
+  if (bad) {
+    delete s;
+    return fail(VT_EINVAL, "triangle index %u out of range (%lld vertices)", (unsigned)(bad & 0xffffffffu),
+                (long long)n_vertices);
+  }
   rc = scene_finish(ctx, s, palette, n_palette, nullptr, 0, VT_SCENE_AUTO_EMISSIVE | VT_SCENE_PRUNE_EMISSIVE,
                     /*bricks_built=*/true);
   if (rc != VT_OK) { delete s; return rc; }

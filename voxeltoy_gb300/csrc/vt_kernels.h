@@ -168,23 +168,34 @@ cudaError_t launch_env_build(const float* rgb, int32_t w, int32_t h, int32_t cw,
 // CDFs of a caller-supplied function (w*h floats) without blur or weighting.
 cudaError_t launch_cdf(const float* func, int32_t w, int32_t h, const EnvScratch& S, float* cdf_u,
                        float* cdf_v, float* integral, cudaStream_t st);
+// Mesh input checks and placement on the device.  bad: (1 << 32 | index) of
+// the largest triangle index at or past the vertex count, 0 if none.
+struct MeshPrep {
+  uint32_t kmin[3], kmax[3];   // order-preserving keys of the vertex bounds
+  unsigned long long bad;
+};
+// The MeshPrep record inside a voxelization's scratch.
+MeshPrep* voxelize_prep_record(void* scratch, int64_t n_tris);
+// Checks the indices against nv and, with fit, applies computeMeshTransform
+// and the scaling to voxel space to the nv vertices at V in place.
+cudaError_t launch_mesh_prep(float* V, int64_t nv, const uint32_t* I, int64_t n_tris, bool fit, int32_t rx,
+                             int32_t ry, int32_t rz, MeshPrep* P, int sm_count, cudaStream_t st);
 // mode 0 = THIN, 1 = FAT; reference_bounds clamps each triangle's swizzled
-// voxel range against the unswizzled resolution as the reference does.
+// voxel range against the unswizzled resolution as the reference does;
+// triangles with an index at or past n_vertices are skipped.
 // bricks (nullable): the padded brick grid (bx, by bricks per row / slice
 // inside the border), prepared by launch_bricks_init; every voxel written
 // also sets its occupancy bit.  scratch: voxelize_scratch_bytes(n_tris)
 // bytes of device memory for the list of large triangles; large_blocks:
 // blocks of the block-per-triangle kernel.
 size_t voxelize_scratch_bytes(int64_t n_tris);
-cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indices, int64_t n_tris,
-                            int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
+cudaError_t launch_voxelize(const float* verts_voxel_space, int64_t n_vertices, const uint32_t* indices,
+                            int64_t n_tris, int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
                             uint8_t* grid, uint8_t value, unsigned long long* bricks, int32_t bx, int32_t by,
                             const BrickShape& sh, void* scratch, int large_blocks, cudaStream_t st);
 // Bricks of an empty volume: border bricks all set, interior bricks set only
 // for the voxels beyond the volume's extent.
 cudaError_t launch_bricks_init(unsigned long long* bricks, int32_t rx, int32_t ry, int32_t rz, int32_t bx,
                                int32_t by, int32_t bz, const BrickShape& sh, cudaStream_t st);
-cudaError_t launch_transform_vertices(const float* in, int64_t n, const float* m44_row_major,
-                                      int32_t rx, int32_t ry, int32_t rz, float* out, cudaStream_t st);
 
 }  // namespace vt

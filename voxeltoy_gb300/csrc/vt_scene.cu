@@ -430,11 +430,12 @@ __device__ __forceinline__ float edge_d(const float* nrm, float pa, float pb, in
   return (-(nrm[0] * pa + nrm[1] * pb) + vtb::gmax(0.0f, nrm[0])) + vtb::gmax(0.0f, nrm[1]);
 }
 
-__device__ bool tri_setup(const float* V, const uint32_t* I, int64_t t, int32_t rx, int32_t ry, int32_t rz,
-                          int mode, bool ref_bounds, TriSetup& S) {
+__device__ bool tri_setup(const float* V, int64_t nv, const uint32_t* I, int64_t t, int32_t rx, int32_t ry,
+                          int32_t rz, int mode, bool ref_bounds, TriSetup& S) {
   float v[3][3];
   for (int k = 0; k < 3; ++k) {
     const uint32_t vi = I[3 * t + k];
+    if ((int64_t)vi >= nv) return false;   // recorded by k_mesh_scan; the call fails
     v[k][0] = V[3 * (int64_t)vi]; v[k][1] = V[3 * (int64_t)vi + 1]; v[k][2] = V[3 * (int64_t)vi + 2];
   }
   // n = cross(v1 - v0, v2 - v1)   (voxelize.gs:62)
@@ -571,13 +572,13 @@ constexpr int kLargeColumns = 64;
 
 // One thread per triangle for triangles whose XY footprint is small; larger
 // ones are appended to a list for the block-per-triangle kernel.
-__global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restrict__ I, int64_t n_tris,
-                            int32_t rx, int32_t ry, int32_t rz, int mode, bool ref_bounds, const VoxOut O,
-                            int64_t* large, unsigned long long* n_large) {
+__global__ void k_vox_small(const float* __restrict__ V, int64_t nv, const uint32_t* __restrict__ I,
+                            int64_t n_tris, int32_t rx, int32_t ry, int32_t rz, int mode, bool ref_bounds,
+                            const VoxOut O, int64_t* large, unsigned long long* n_large) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n_tris) return;
   TriSetup S;
-  if (!tri_setup(V, I, t, rx, ry, rz, mode, ref_bounds, S)) return;
+  if (!tri_setup(V, nv, I, t, rx, ry, rz, mode, ref_bounds, S)) return;
   const int64_t cols = (int64_t)(S.hi[0] - S.lo[0]) * (int64_t)(S.hi[1] - S.lo[1]);
   if (cols > kLargeColumns) {
     const unsigned long long slot = atomicAdd(n_large, 1ull);
@@ -590,14 +591,14 @@ __global__ void k_vox_small(const float* __restrict__ V, const uint32_t* __restr
   if (O.bricks) acc.flush(O);
 }
 
-__global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restrict__ I, const int64_t* large,
-                            const unsigned long long* n_large, int32_t rx, int32_t ry, int32_t rz, int mode,
-                            bool ref_bounds, const VoxOut O) {
+__global__ void k_vox_large(const float* __restrict__ V, int64_t nv, const uint32_t* __restrict__ I,
+                            const int64_t* large, const unsigned long long* n_large, int32_t rx, int32_t ry,
+                            int32_t rz, int mode, bool ref_bounds, const VoxOut O) {
   __shared__ TriSetup S;
   const unsigned long long n = *n_large;
   for (unsigned long long k = blockIdx.x; k < n; k += gridDim.x) {
     __syncthreads();
-    if (threadIdx.x == 0) tri_setup(V, I, large[k], rx, ry, rz, mode, ref_bounds, S);
+    if (threadIdx.x == 0) tri_setup(V, nv, I, large[k], rx, ry, rz, mode, ref_bounds, S);   // listed: valid
     __syncthreads();
     const int wx = S.hi[0] - S.lo[0], wy = S.hi[1] - S.lo[1];
     const int64_t cols = (int64_t)wx * wy;
@@ -610,18 +611,141 @@ __global__ void k_vox_large(const float* __restrict__ V, const uint32_t* __restr
   }
 }
 
-size_t voxelize_scratch_bytes(int64_t n_tris) {
-  return (sizeof(int64_t) * (size_t)std::max<int64_t>(n_tris, 1) + 255) / 256 * 256 + 256;
+// Scratch of a voxelization: the large-triangle list, then 256 bytes for its
+// length, then 256 bytes for the MeshPrep record.
+static size_t large_list_bytes(int64_t n_tris) {
+  return (sizeof(int64_t) * (size_t)std::max<int64_t>(n_tris, 1) + 255) / 256 * 256;
+}
+size_t voxelize_scratch_bytes(int64_t n_tris) { return large_list_bytes(n_tris) + 512; }
+MeshPrep* voxelize_prep_record(void* scratch, int64_t n_tris) {
+  return (MeshPrep*)((char*)scratch + large_list_bytes(n_tris) + 256);
 }
 
-cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indices, int64_t n_tris,
-                            int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
+// Order-preserving 32-bit keys of floats (not NaN): unsigned comparison of
+// keys is float comparison, with -0 below +0.
+__device__ __forceinline__ uint32_t fkey(float f) {
+  const uint32_t b = __float_as_uint(f);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_value(uint32_t k) {
+  return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// Triangle indices at or past the vertex count (the largest one is kept),
+// and with `bounds` the vertices' bounding box (NaN coordinates ignored, as
+// the left-to-right min / max of import.cpp:49-52 ignores them).
+__global__ void __launch_bounds__(256) k_mesh_scan(const float* __restrict__ V, int64_t nv,
+                                                   const uint32_t* __restrict__ I, int64_t n_idx, bool bounds,
+                                                   MeshPrep* P) {
+  uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  unsigned long long bad = 0ull;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n_idx; i += stride) {
+    const uint32_t vi = I[i];
+    if ((int64_t)vi >= nv) bad = max(bad, (1ull << 32) | vi);
+  }
+  if (bounds)
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride)
+      for (int c = 0; c < 3; ++c) {
+        const float f = V[3 * i + c];
+        if (f == f) {
+          lo[c] = min(lo[c], fkey(f));
+          hi[c] = max(hi[c], fkey(f));
+        }
+      }
+  // warp, then block (256 threads), then one atomic per value and block
+  for (int o = 16; o > 0; o >>= 1) {
+    bad = max(bad, __shfl_xor_sync(0xffffffffu, bad, o));
+    for (int c = 0; c < 3; ++c) {
+      lo[c] = min(lo[c], __shfl_xor_sync(0xffffffffu, lo[c], o));
+      hi[c] = max(hi[c], __shfl_xor_sync(0xffffffffu, hi[c], o));
+    }
+  }
+  __shared__ unsigned long long s_bad[8];
+  __shared__ uint32_t s_lo[3][8], s_hi[3][8];
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    s_bad[warp] = bad;
+    for (int c = 0; c < 3; ++c) { s_lo[c][warp] = lo[c]; s_hi[c][warp] = hi[c]; }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      bad = max(bad, s_bad[w]);
+      for (int c = 0; c < 3; ++c) { lo[c] = min(lo[c], s_lo[c][w]); hi[c] = max(hi[c], s_hi[c][w]); }
+    }
+    if (bad) atomicMax(&P->bad, bad);
+    if (bounds)
+      for (int c = 0; c < 3; ++c) {
+        if (lo[c] != 0xffffffffu) atomicMin(&P->kmin[c], lo[c]);
+        if (hi[c] != 0u) atomicMax(&P->kmax[c], hi[c]);
+      }
+  }
+}
+
+// computeMeshTransform (import.cpp:46-64) from the scanned bounds, in the
+// host's float and double arithmetic, then the vertex shader's
+// modelTransform * v * voxelResolution (voxelize.vs:20-27) on every vertex in
+// place.  One block; every thread computes the same matrix.
+__global__ void k_mesh_fit(float* __restrict__ V, int64_t nv, int32_t rx, int32_t ry, int32_t rz,
+                           const MeshPrep* P) {
+  float bmin[3], bmax[3];
+  for (int c = 0; c < 3; ++c) {   // an axis whose coordinates are all NaN keeps +inf / -inf, as on the host
+    bmin[c] = P->kmin[c] == 0xffffffffu ? INFINITY : fkey_value(P->kmin[c]);
+    bmax[c] = P->kmax[c] == 0u ? -INFINITY : fkey_value(P->kmax[c]);
+  }
+  const float res[3] = {(float)rx, (float)ry, (float)rz};
+  float size[3], margin[3];
+  for (int c = 0; c < 3; ++c) { size[c] = bmax[c] - bmin[c]; margin[c] = 1.0f / res[c]; }
+  int major = 0;
+  if (size[1] > size[major]) major = 1;
+  if (size[2] > size[major]) major = 2;
+  const float sc = (float)((1.0f - 2.0 * (double)margin[major]) / (double)size[major]);
+  float M[12];
+  for (int r = 0; r < 3; ++r) {
+    const float t = -bmin[r] + margin[r] / sc;
+    M[4 * r] = r == 0 ? sc : 0.0f;
+    M[4 * r + 1] = r == 1 ? sc : 0.0f;
+    M[4 * r + 2] = r == 2 ? sc : 0.0f;
+    M[4 * r + 3] = t * sc;
+  }
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride) {
+    const float x = V[3 * i], y = V[3 * i + 1], z = V[3 * i + 2];
+    for (int r = 0; r < 3; ++r) {
+      const float p = ((M[4 * r] * x + M[4 * r + 1] * y) + M[4 * r + 2] * z) + M[4 * r + 3] * 1.0f;
+      V[3 * i + r] = p * res[r];
+    }
+  }
+}
+
+cudaError_t launch_mesh_prep(float* V, int64_t nv, const uint32_t* I, int64_t n_tris, bool fit, int32_t rx,
+                             int32_t ry, int32_t rz, MeshPrep* P, int sm_count, cudaStream_t st) {
+  MeshPrep init;
+  for (int c = 0; c < 3; ++c) { init.kmin[c] = 0xffffffffu; init.kmax[c] = 0u; }
+  init.bad = 0ull;
+  // pageable source: read when the copy returns
+  cudaError_t e = cudaMemcpyAsync(P, &init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  const int64_t work = std::max<int64_t>(3 * n_tris, fit ? nv : 0);
+  if (work <= 0) return cudaSuccess;
+  const int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)sm_count * 8);
+  k_mesh_scan<<<blocks, 256, 0, st>>>(V, nv, I, 3 * n_tris, fit, P);   // 256 threads: eight warps
+  if (fit && nv > 0) {
+    // the matrix needs the whole scan: a second launch, each block rebuilds it
+    const int fb = (int)std::min<int64_t>((nv + 255) / 256, (int64_t)sm_count * 8);
+    k_mesh_fit<<<fb, 256, 0, st>>>(V, nv, rx, ry, rz, P);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_voxelize(const float* verts_voxel_space, int64_t n_vertices, const uint32_t* indices,
+                            int64_t n_tris, int32_t rx, int32_t ry, int32_t rz, int32_t mode, bool reference_bounds,
                             uint8_t* grid, uint8_t value, unsigned long long* bricks, int32_t bx, int32_t by,
                             const BrickShape& sh, void* scratch, int large_blocks, cudaStream_t st) {
   if (n_tris <= 0) return cudaSuccess;
   int64_t* large = (int64_t*)scratch;
-  unsigned long long* n_large =
-      (unsigned long long*)((char*)scratch + voxelize_scratch_bytes(n_tris) - 256);   // the last 256 bytes
+  unsigned long long* n_large = (unsigned long long*)((char*)scratch + large_list_bytes(n_tris));
   cudaError_t e = cudaMemsetAsync(n_large, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
   VoxOut O;
@@ -631,10 +755,10 @@ cudaError_t launch_voxelize(const float* verts_voxel_space, const uint32_t* indi
   O.bx = bx;
   O.by = by;
   O.sh = sh;
-  k_vox_small<<<(unsigned)((n_tris + 127) / 128), 128, 0, st>>>(verts_voxel_space, indices, n_tris, rx, ry, rz,
-                                                                mode, reference_bounds, O, large, n_large);
-  k_vox_large<<<std::max(1, large_blocks), 256, 0, st>>>(verts_voxel_space, indices, large, n_large, rx, ry, rz,
-                                                         mode, reference_bounds, O);
+  k_vox_small<<<(unsigned)((n_tris + 127) / 128), 128, 0, st>>>(verts_voxel_space, n_vertices, indices, n_tris, rx,
+                                                                ry, rz, mode, reference_bounds, O, large, n_large);
+  k_vox_large<<<std::max(1, large_blocks), 256, 0, st>>>(verts_voxel_space, n_vertices, indices, large, n_large, rx,
+                                                         ry, rz, mode, reference_bounds, O);
   return cudaGetLastError();
 }
 
