@@ -515,7 +515,8 @@ def serving_record(ctx, rate: float, duration: float, order: str = "arrival", qu
                                          "p99": float(np.percentile(lat, 99) * 1e3), "max": float(lat.max() * 1e3)},
                       "completed": int(stats.completed), "failed": int(stats.failed), "rounds": int(stats.rounds),
                       "scene_uploads": int(stats.scene_uploads), "scene_hits": int(stats.scene_hits),
-                      "scene_evictions": int(stats.scene_evictions)},
+                      "scene_evictions": int(stats.scene_evictions),
+                      "round_s": stats.round_us / 1e6, "between_rounds_s": stats.between_us / 1e6},
            "settings": {"order": order, "quick_paths": quick_paths, "round_cap": round_cap,
                         "round_paths": round_paths or (1 << 26),
                         "hbm_budget_bytes": 60 << 30, "passes_per_round": 4, "max_active_jobs": 64,

@@ -609,6 +609,9 @@ typedef struct vt_server_stats {
   uint64_t scene_evictions;    /* resident scenes evicted to make room                */
   int32_t scenes_resident;
   int32_t pad;
+  uint64_t round_us;           /* loop time in rounds: launch to completion            */
+  uint64_t between_us;         /* loop time between consecutive rounds (retiring,
+                                  admission, composing the next round)                 */
 } vt_server_stats;
 
 /* Start a request loop thread that admits jobs as slots and budget free up

@@ -177,6 +177,7 @@ def test_server_budget_cancel_and_timeout(ctx):
         assert np.isfinite(img).all() and secs > 0
         st = srv.stats()
         assert st.failed == 1 and st.cancelled == 2 and st.completed == 1
+        assert st.rounds > 0 and st.round_us > 0
     finally:
         srv.close()
         scene.close()

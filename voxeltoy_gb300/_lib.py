@@ -94,7 +94,8 @@ class ServerStats(C.Structure):
                 ("failed", C.c_uint64), ("paths_traced", C.c_uint64), ("rounds", C.c_uint64),
                 ("bytes_in_use", C.c_uint64), ("active", C.c_int32), ("queued", C.c_int32),
                 ("scene_uploads", C.c_uint64), ("scene_hits", C.c_uint64), ("scene_evictions", C.c_uint64),
-                ("scenes_resident", C.c_int32), ("pad", C.c_int32)]
+                ("scenes_resident", C.c_int32), ("pad", C.c_int32), ("round_us", C.c_uint64),
+                ("between_us", C.c_uint64)]
 
 
 P = C.c_void_p

@@ -195,6 +195,7 @@ void vt_server::run() {
   std::vector<vt_job*> jobs;
   std::vector<int32_t> passes;
   std::vector<Request*> round;
+  double last_end = 0.0;   // end of the previous round, 0 after waiting for work
   for (;;) {
     {
       std::unique_lock<std::mutex> g(mu);
@@ -241,6 +242,7 @@ void vt_server::run() {
       changed.notify_all();
       if (active.empty()) {
         if (stop) return;
+        last_end = 0.0;
         wake.wait_for(g, std::chrono::milliseconds(20));
         continue;
       }
@@ -255,10 +257,14 @@ void vt_server::run() {
       paths += (uint64_t)round[i]->w * round[i]->h * (uint64_t)passes[i];
     }
     vt::Range round_range("vt.server_round");
+    const double t0 = now_s();
     int rc = render_jobs(&lane, jobs.data(), (int32_t)jobs.size(), passes.data(), 2, opts.path_slots, 0, false);
     if (rc == VT_OK && cudaStreamSynchronize(lane.stream) != cudaSuccess) rc = VT_EDEVICE;
+    const double t1 = now_s();
     std::unique_lock<std::mutex> g(mu);
     stats.rounds++;
+    stats.round_us += (uint64_t)(1e6 * (t1 - t0));
+    if (last_end > 0.0) stats.between_us += (uint64_t)(1e6 * (t0 - last_end));
     for (size_t i = 0; i < round.size(); ++i) {
       Request* r = round[i];
       if (rc != VT_OK) {
@@ -281,6 +287,7 @@ void vt_server::run() {
     active.erase(std::remove_if(active.begin(), active.end(), [](Request* r) { return r->state != VT_REQ_RUNNING; }),
                  active.end());
     changed.notify_all();
+    last_end = t1;
   }
 }
 
