@@ -51,7 +51,10 @@ struct WfHitRecs {
 // entries of the hit list.  Each word has its own 128-byte line, so atomics
 // on different counters never queue behind each other in one L2 sector.
 enum { CTL_QCOUNT = 0, CTL_QHEAD = 1, CTL_NEXT_N = 2, CTL_ITEM_SNAP = 3, CTL_HITS_LAMBERT = 4,
-       CTL_HITS_OTHER = 5, CTL_PER_PARITY = 8 };
+       CTL_HITS_OTHER = 5, CTL_REGEN_N = 6, CTL_PER_PARITY = 8 };
+// Segment record tag of a queue entry that holds no segment (a new-path
+// position that found no item).
+constexpr uint32_t kNoSegment = 0xffffffffu;
 constexpr int kCtlStride = 32;                                   // words per counter line
 constexpr int kCtlNextItem = 2 * CTL_PER_PARITY * kCtlStride;    // word index of the item counter
 constexpr size_t kCtlBytes = (size_t)(2 * CTL_PER_PARITY + 1) * kCtlStride * sizeof(uint32_t);

@@ -333,6 +333,14 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
   const uint32_t nl = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)];
   const uint32_t no = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_OTHER)];
   const uint32_t n_hits = nl + no;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // items [taken, taken + m) go to k_wf_regen's m positions, position k
+    // taking item taken + k first; its lanes claim further items only after
+    const unsigned long long taken = *(volatile unsigned long long*)&P.ctl[ctl_index(par, CTL_ITEM_SNAP)];
+    const unsigned long long left = P.n_items > taken ? P.n_items - taken : 0ull;
+    const uint32_t m = (uint32_t)min((unsigned long long)((uint32_t)P.n_slots - n_hits), left);
+    if (m) atomicAdd(P.next_item, (unsigned long long)m);
+  }
   const WfState& dst = P.x[par ^ 1];
   Cnt<kCount> cnt;
 #pragma unroll
@@ -376,25 +384,31 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
 }
 
 // New paths at positions [hits, hits + m) of the next stream, m = the free
-// capacity or the items left, whichever is smaller.  Each lane takes items
-// until one enters its job's volume (a path that misses the volume is
-// finished at once) or the items run out (the position stays empty).  The
-// primary segment starts at the volume entry point.  A block-uniform
-// grid-stride loop; the first item of every position is claimed for the
-// whole block with one atomic.
+// capacity or the items left, whichever is smaller.  Position k starts with
+// item taken + k (reserved by k_wf_hit); a lane whose path misses its job's
+// volume (finished at once) claims further items with one atomic per warp,
+// until a path enters the volume or the items run out (the position stays
+// empty).  The primary segment starts at the volume entry point; position
+// k's queue record is entry QCOUNT + k of the round's queue (the hit
+// kernel's records come first), a record without a segment for an empty
+// position, so that the kernel needs no block-wide reservation.
 template <bool kCount, class Tab>
 __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  __shared__ unsigned long long s_item;
   const uint32_t n_hits = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_LAMBERT)] +
                           *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_HITS_OTHER)];
   const unsigned long long taken = *(volatile unsigned long long*)&P.ctl[ctl_index(par, CTL_ITEM_SNAP)];
   const unsigned long long left = P.n_items > taken ? P.n_items - taken : 0ull;
   const uint32_t m = (uint32_t)min((unsigned long long)((uint32_t)P.n_slots - n_hits), left);
-  if (blockIdx.x == 0 && threadIdx.x == 0) P.ctl[ctl_index(par, CTL_NEXT_N)] = n_hits + m;
+  const uint32_t qbase = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_QCOUNT)];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    P.ctl[ctl_index(par, CTL_NEXT_N)] = n_hits + m;
+    P.ctl[ctl_index(par, CTL_REGEN_N)] = m;
+  }
   const WfState& dst = P.x[par ^ 1];
+  float4* const q = P.queue[par];
   Cnt<kCount> cnt;
 #pragma unroll
   for (int k = 0; k < C_NUM; ++k) cnt.c[k] = 0;
@@ -403,10 +417,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
     const uint32_t k = b0 + threadIdx.x;
     const bool mine = k < m;
     const uint32_t pos = n_hits + k;
-    if (threadIdx.x == 0) s_item = atomicAdd(P.next_item, (unsigned long long)min(blockDim.x, m - b0));
-    __syncthreads();
-    unsigned long long my = s_item + threadIdx.x;
-    __syncthreads();
+    unsigned long long my = taken + k;
     bool need_new = mine, active = false;
     Path p;
     uint32_t job = 0, item = 0;
@@ -442,17 +453,18 @@ __global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __g
       base = __shfl_sync(FULL, base, leader);
       my = base + __popc(want & lt);
     }
-    const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
-    uint32_t* const ctr[1] = {&P.ctl[ctl_index(par, CTL_QCOUNT)]};
-    const uint32_t nn[1] = {active ? 1u : 0u};
-    uint32_t base[1];
-    block_reserve<1>(ctr, nn, base);
-    write_segments(P, par, base[0], active ? 1u : 0u, (int)pos, job, o, p);
-    if (active) {
-      store_path(dst, (int)pos, job_entry(P, T, job).F, p, item, false);   // a primary path has no shadow segment
-      dst.flags[pos] = slot_flags(p, 1u, job);
-    } else if (mine) {
-      dst.flags[pos] = 0u;
+    if (mine) {
+      const size_t at = 2 * (size_t)(qbase + k);
+      if (active) {
+        const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
+        q[at] = make_float4(o.x, o.y, o.z, p.rd.x);
+        q[at + 1] = make_float4(p.rd.y, p.rd.z, __uint_as_float((uint32_t)pos << 1), __uint_as_float(job));
+        store_path(dst, (int)pos, job_entry(P, T, job).F, p, item, false);   // a primary path has no shadow segment
+        dst.flags[pos] = slot_flags(p, 1u, job);
+      } else {
+        q[at + 1] = make_float4(0.0f, 0.0f, __uint_as_float(kNoSegment), 0.0f);
+        dst.flags[pos] = 0u;
+      }
     }
   }
   flush_counters(cnt, P.counters);
@@ -490,7 +502,8 @@ __global__ void __launch_bounds__(256, TraceBlocks<Tab>::value) k_wf_trace(const
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const uint32_t n = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_QCOUNT)];
+  const uint32_t n = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_QCOUNT)] +
+                     *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_REGEN_N)];   // hit, then new-path records
   if (n == 0) return;
   const float4* q = P.queue[par];
   Cnt<kCount> cnt;
@@ -506,10 +519,12 @@ __global__ void __launch_bounds__(256, TraceBlocks<Tab>::value) k_wf_trace(const
     if (!have && have_next) {            // start the prefetched segment
       have_next = false;
       tag = __float_as_uint(nb.z);
-      gh.set(P, T, __float_as_uint(nb.w));
-      dda_begin(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
-      if (s.state == DDA_RUNNING) have = true;
-      else P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
+      if (tag != kNoSegment) {
+        gh.set(P, T, __float_as_uint(nb.w));
+        dda_begin(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
+        if (s.state == DDA_RUNNING) have = true;
+        else P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
+      }
     }
     unsigned need = __ballot_sync(FULL, !have_next);
     while (need && !exhausted) {          // prefetch next records
@@ -566,7 +581,8 @@ __global__ void __launch_bounds__(256, 4) k_wf_trace_pool(const WfParams P, cons
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
-  const uint32_t n = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_QCOUNT)];
+  const uint32_t n = *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_QCOUNT)] +
+                     *(volatile uint32_t*)&P.ctl[ctl_index(par, CTL_REGEN_N)];   // hit, then new-path records
   if (n == 0) return;
   const float4* q = P.queue[par];
   Cnt<kCount> cnt;
@@ -594,7 +610,7 @@ __global__ void __launch_bounds__(256, 4) k_wf_trace_pool(const WfParams P, cons
       bool run = false;
       Dda t;
       uint32_t ttag = 0, tjob = 0;
-      if (rec < chunk_end) {
+      if (rec < chunk_end && __float_as_uint(__ldg(&q[2 * (size_t)rec + 1]).z) != kNoSegment) {
         const float4 a = __ldg(&q[2 * (size_t)rec]), b = __ldg(&q[2 * (size_t)rec + 1]);
         ttag = __float_as_uint(b.z);
         tjob = __float_as_uint(b.w);
