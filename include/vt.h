@@ -66,8 +66,13 @@ typedef struct vt_server vt_server;   /* continuous-batching render server     *
 typedef struct vt_device_opts {
   int32_t device;            /* CUDA ordinal                                  */
   uint64_t hbm_budget_bytes; /* 0 = no budget; allocations beyond it fail     */
-  uint32_t flags;            /* reserved, 0                                   */
+  uint32_t flags;            /* VT_DEVICE_* flags, 0 by default               */
 } vt_device_opts;
+/* Device memory a context releases (scenes, environments, jobs destroyed)
+ * is kept for its next allocations, up to 2 GiB, instead of returned at
+ * once; live plus kept bytes stay within the budget.  This flag returns
+ * every release at once; vt_context_trim returns the kept blocks. */
+#define VT_DEVICE_NO_ALLOC_CACHE 1u
 
 /* Renderer::initialize (src/renderer/renderer.h:31, renderer.cpp:76-140).
  * opts may be NULL (device 0, no budget). */
@@ -79,8 +84,12 @@ VT_API const char* vt_last_error(void);
 /* Renderer::setLogger (src/renderer/renderer.h:99; src/log/logger.h:7-11). */
 typedef void (*vt_log_fn)(const char* message, void* user);
 VT_API int vt_set_log_callback(vt_context* ctx, vt_log_fn fn, void* user);
-/* Bytes of device memory the context currently holds. */
+/* Bytes of device memory the context currently holds for live objects
+ * (blocks kept for reuse are not counted). */
 VT_API int vt_context_memory(const vt_context* ctx, uint64_t* bytes_in_use);
+/* Returns the device memory kept for reuse; released: bytes freed
+ * (nullable). */
+VT_API int vt_context_trim(vt_context* ctx, uint64_t* released);
 
 /* ------------------------------------------------------------- materials -- */
 /* Material::MaterialType (src/renderer/material/material.h:8-13). */

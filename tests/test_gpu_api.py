@@ -608,3 +608,32 @@ def test_server_does_not_charge_caller_owned_scenes(ctx):
     finally:
         srv.close()
         sc.close()
+
+
+def test_released_memory_is_reused_and_trimmed():
+    """A destroyed scene's device blocks serve the next scene of the same
+    size without a new cudaMalloc; trim returns them; the budget counts live
+    plus kept blocks; VT_DEVICE_NO_ALLOC_CACHE keeps nothing."""
+    torch = pytest.importorskip("torch")
+    g = np.zeros((256, 256, 256), np.uint8)
+    g[:, :8, :] = 1
+    with Context(0) as ctx:
+        base = ctx.memory()
+        Scene.dense(ctx, g, [S.lambert(0.5)]).close()
+        assert ctx.memory() == base
+        free1 = torch.cuda.mem_get_info(0)[0]
+        sc = Scene.dense(ctx, g, [S.lambert(0.5)])
+        free2 = torch.cuda.mem_get_info(0)[0]
+        assert free1 - free2 < (4 << 20)   # the 16 MiB grid came from the kept blocks
+        sc.close()
+        assert ctx.trim() >= (16 << 20)
+        assert torch.cuda.mem_get_info(0)[0] - free2 >= (16 << 20)
+        assert ctx.trim() == 0
+    with Context(0, hbm_budget_bytes=40 << 20) as ctx:
+        Scene.dense(ctx, g, [S.lambert(0.5)]).close()                  # ~19 MiB kept
+        g2 = np.zeros((320, 256, 256), np.uint8)
+        sc = Scene.dense(ctx, g2, [S.lambert(0.5)])                  # ~22 MiB: fits after the kept blocks go
+        sc.close()
+    with Context(0, flags=L.VT_DEVICE_NO_ALLOC_CACHE) as ctx:
+        Scene.dense(ctx, g, [S.lambert(0.5)]).close()
+        assert ctx.trim() == 0

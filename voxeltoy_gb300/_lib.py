@@ -24,6 +24,7 @@ VT_MESH_VOXEL_SPACE, VT_MESH_FIT_UNIT_CUBE = 0, 1
 VT_LENS_PINHOLE, VT_LENS_THIN_LENS, VT_LENS_ORTHOGRAPHIC = 0, 1, 2
 VT_SERVE_ARRIVAL, VT_SERVE_LEAST_WORK = 0, 1
 VT_ENV_CDF_REFERENCE_SIZE = 1
+VT_DEVICE_NO_ALLOC_CACHE = 1
 VT_INTEGRATOR_PATH_TRACER, VT_INTEGRATOR_EDIT_MODE = 0, 1
 VT_BUTTON_ROTATE, VT_BUTTON_PAN = 1, 2
 VT_KEY_FORWARD, VT_KEY_BACK, VT_KEY_RIGHT, VT_KEY_LEFT = 0, 1, 2, 3
@@ -109,6 +110,7 @@ SIGNATURES = {
     "vt_destroy": [P],
     "vt_set_log_callback": [P, LOG_FN, P],
     "vt_context_memory": [P, C.POINTER(C.c_uint64)],
+    "vt_context_trim": [P, C.POINTER(C.c_uint64)],
     "vt_scene_create": [P, C.c_int32, C.c_int32, C.c_int32, P, C.POINTER(Material), C.c_int32, P, C.c_int64,
                         C.c_uint32, PP],
     "vt_scene_create_from_offsets": [P, C.c_int32, C.c_int32, C.c_int32, P, P, C.c_int64, P, C.c_int64, C.c_uint32,

@@ -58,15 +58,46 @@ void vt_context::log(const char* fmt, ...) {
   log_fn(buf, log_user);
 }
 
+// Frees cached blocks, largest first, until at most `keep` bytes stay cached
+// (the caller holds mu).
+static uint64_t trim_locked(vt_context* ctx, uint64_t keep) {
+  uint64_t freed = 0;
+  if (ctx->cached > keep) cudaSetDevice(ctx->device);
+  while (ctx->cached > keep && !ctx->cache.empty()) {
+    auto it = std::prev(ctx->cache.end());
+    cudaFree(it->second);
+    ctx->cached -= it->first;
+    freed += it->first;
+    ctx->cache.erase(it);
+  }
+  return freed;
+}
+
 int vt_context::alloc(void** ptr, size_t bytes) {
   *ptr = nullptr;
   if (bytes == 0) bytes = 16;
+  bytes = (bytes + 511) / 512 * 512;
   std::lock_guard<std::mutex> g(mu);
   if (budget && in_use + bytes > budget)
     return fail(VT_EBUDGET, "device-memory budget exceeded: %llu + %llu > %llu bytes",
                 (unsigned long long)in_use, (unsigned long long)bytes, (unsigned long long)budget);
+  auto hit = cache.lower_bound(bytes);
+  if (hit != cache.end() && hit->first <= bytes + bytes / 4 && (!budget || in_use + hit->first <= budget)) {
+    *ptr = hit->second;
+    sizes[*ptr] = hit->first;
+    in_use += hit->first;
+    cached -= hit->first;
+    cache.erase(hit);
+    return VT_OK;
+  }
+  if (budget) trim_locked(this, in_use + bytes <= budget ? budget - in_use - bytes : 0);
   cudaSetDevice(device);
   cudaError_t e = cudaMalloc(ptr, bytes);
+  if (e == cudaErrorMemoryAllocation && cached) {   // the cache first, then the device
+    cudaGetLastError();
+    trim_locked(this, 0);
+    e = cudaMalloc(ptr, bytes);
+  }
   if (e != cudaSuccess) { *ptr = nullptr; return cuda_fail(e, "cudaMalloc"); }
   sizes[*ptr] = bytes;
   in_use += bytes;
@@ -77,8 +108,22 @@ void vt_context::release(void* ptr) {
   if (!ptr) return;
   std::lock_guard<std::mutex> g(mu);
   auto it = sizes.find(ptr);
-  if (it != sizes.end()) { in_use -= it->second; sizes.erase(it); }
-  cudaFree(ptr);
+  if (it == sizes.end()) { cudaFree(ptr); return; }
+  const size_t sz = it->second;
+  in_use -= sz;
+  sizes.erase(it);
+  cudaSetDevice(device);
+  if (!caching || sz > cache_limit || !stream) { cudaFree(ptr); return; }
+  // no kernel of this context still uses the block when another takes it
+  if (cudaStreamSynchronize(stream) != cudaSuccess) { cudaGetLastError(); cudaFree(ptr); return; }
+  cache.emplace(sz, ptr);
+  cached += sz;
+  trim_locked(this, cache_limit);
+}
+
+uint64_t vt_context::trim(uint64_t keep) {
+  std::lock_guard<std::mutex> g(mu);
+  return trim_locked(this, keep);
 }
 
 int vt_context::ensure_scratch(size_t bytes) {
@@ -126,6 +171,7 @@ extern "C" int vt_create(const vt_device_opts* opts, vt_context** out) {
   vt_context* c = new vt_context();
   c->device = dev;
   c->budget = opts ? opts->hbm_budget_bytes : 0;
+  c->caching = !(opts && (opts->flags & VT_DEVICE_NO_ALLOC_CACHE));
   c->sm_count = prop.multiProcessorCount;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
@@ -158,6 +204,7 @@ void vt::release_context(vt_context* ctx) {
   ctx->release(ctx->wf_mem);
   ctx->release(ctx->sbuf);
   ctx->release(ctx->wf_ctl);
+  ctx->trim(0);
   if (ctx->h_live) cudaFreeHost(ctx->h_live);
   if (ctx->rounds_exec) cudaGraphExecDestroy(ctx->rounds_exec);
   if (ctx->lane_ready) cudaEventDestroy(ctx->lane_ready);
@@ -174,6 +221,13 @@ void vt::release_context(vt_context* ctx) {
     ctx->lane_stream[l] = nullptr;
   }
   ctx->stream = nullptr;
+}
+
+extern "C" int vt_context_trim(vt_context* ctx, uint64_t* released) {
+  VT_CHECK_ARG(ctx, "null argument");
+  const uint64_t n = ctx->trim(0);
+  if (released) *released = n;
+  return VT_OK;
 }
 
 extern "C" int vt_destroy(vt_context* ctx) {

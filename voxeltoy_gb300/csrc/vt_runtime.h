@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
 
+#include <map>
 #include <mutex>
 #include <unordered_map>
 #include <vector>
@@ -59,8 +60,18 @@ struct vt_context {
   unsigned long long* d_queue = nullptr;
   int32_t* d_error = nullptr;
 
-  int alloc(void** ptr, size_t bytes);   // budget-checked cudaMalloc
+  // Device memory: budget-checked, with released blocks kept for reuse.  A
+  // released block waits for the context's stream to go idle and joins the
+  // cache (up to cache_limit bytes); alloc takes the smallest cached block of
+  // the rounded size up to a quarter larger before it calls cudaMalloc, and
+  // live plus cached bytes stay within the budget.
+  int alloc(void** ptr, size_t bytes);
   void release(void* ptr);
+  uint64_t trim(uint64_t keep);           // free cached blocks down to `keep` bytes; returns bytes freed
+  bool caching = true;
+  std::multimap<size_t, void*> cache;     // size -> block
+  uint64_t cached = 0;
+  uint64_t cache_limit = 2ull << 30;
   int ensure_scratch(size_t bytes);
   int ensure_noise();
   void log(const char* fmt, ...);

@@ -40,9 +40,9 @@ def camera_uniforms(cam: L.Camera, width: int, height: int) -> dict:
 
 
 class Context:
-    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0, flags: int = 0):
         L.load()
-        opts = L.DeviceOpts(device, hbm_budget_bytes, 0)
+        opts = L.DeviceOpts(device, hbm_budget_bytes, flags)
         h = C.c_void_p()
         L.call("vt_create", C.byref(opts), C.byref(h))
         self.h = h
@@ -64,8 +64,15 @@ class Context:
         L.call("vt_set_log_callback", self.h, self._log_cb, None)
 
     def memory(self) -> int:
+        """Device bytes held for live objects (blocks kept for reuse excluded)."""
         v = C.c_uint64()
         L.call("vt_context_memory", self.h, C.byref(v))
+        return v.value
+
+    def trim(self) -> int:
+        """Return the device memory kept for reuse; the bytes freed."""
+        v = C.c_uint64()
+        L.call("vt_context_trim", self.h, C.byref(v))
         return v.value
 
     def stream(self) -> int:
