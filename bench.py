@@ -811,7 +811,8 @@ def main():
     elif not args.no_tune and args.kernel == 2:
         from voxeltoy_gb300 import autotune
         best = autotune.tune(ctx, [job], passes=cfg.spp, repeats=1, use_cache=False)
-        tuning = {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps", "lanes")}
+        tuning = {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps", "lanes", "trace_form",
+                                       "queue_chunk", "refill_min", "brick_shape") if k in best}
         for r in best.get("sweep", [])[:12]:
             print("tune", json.dumps(r), file=sys.stderr)
     if args.profile:
