@@ -1505,8 +1505,20 @@ static int wf_launch(vt_context* ctx, std::vector<JobEntry>& entries, const std:
     cudaGraphDestroy(graph);
   }
   // Groups run until every lane's next stream is empty (its items are done;
-  // a finished lane's rounds find nothing to do).
-  for (;;) {
+  // a finished lane's rounds find nothing to do).  A path ends within
+  // max_bounces + 2 rounds of its start, so every such span of rounds frees
+  // a full lane's slots for new paths while items remain: a lane drains
+  // within (items / slots + 2) * (max_bounces + 2) rounds.  Four times that
+  // bounds the loop, so a fault in the kernels' bookkeeping ends the call
+  // with an error instead of looping.
+  int32_t max_b = 0;
+  for (const JobEntry& e : entries) max_b = std::max(max_b, e.F.max_bounces);
+  const int64_t lane_items = (items + lanes - 1) / lanes;
+  const int64_t drain_rounds = (lane_items / (int64_t)lane_slots + 2) * ((int64_t)max_b + 2);
+  const int64_t max_groups = 4 * (drain_rounds + 7) / 8 + 4;
+  for (int64_t group_n = 0;; ++group_n) {
+    if (group_n >= max_groups)
+      return fail(VT_EDEVICE, "wavefront did not drain within %lld rounds", (long long)(8 * max_groups));
     vt::Range rounds_range("vt.rounds");   // eight rounds of every lane, then the live-count check
     if (ctx->use_graphs) {
       VT_CUDA(cudaGraphLaunch(ctx->rounds_exec, st), "wavefront rounds");

@@ -124,7 +124,14 @@ static int fixed_launch(vt_context* ctx, char* base, const JobEntry* entries, co
   if (ctx->trace_occupancy <= 0) ctx->trace_occupancy = std::max(1, wf_trace_blocks_per_sm());
   const int bps = ctx->trace_blocks_per_sm > 0 ? ctx->trace_blocks_per_sm : ctx->trace_occupancy;
   const int trace_blocks = ctx->sm_count * bps;
+  // the bound of the wavefront launch's loop: a path ends within
+  // max_bounces + 2 rounds of its start
+  int32_t max_b = 0;
+  for (int i = 0; i < n; ++i) max_b = std::max(max_b, entries[i].F.max_bounces);
+  const int64_t max_rounds = 4 * (items / slots + 2) * ((int64_t)max_b + 2) + 16;
   for (int64_t iter = 0;; ++iter) {
+    if (iter >= max_rounds) return drain(ctx, fail(VT_EDEVICE, "wavefront did not drain within %lld rounds",
+                                                   (long long)max_rounds));
     const int par = (int)(iter & 1);
     e = cudaMemsetAsync(ctl + ctl_index(par, 0), 0, CTL_PER_PARITY * kCtlStride * sizeof(uint32_t), st);
     if (e != cudaSuccess) return drain(ctx, cuda_fail(e, "fixed round counters"));
