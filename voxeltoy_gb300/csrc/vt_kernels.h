@@ -104,7 +104,8 @@ struct WfOneJob {
 };
 // One round's shading: k_wf_shade over the stream, then k_wf_hit over the
 // hits it keeps and k_wf_regen filling the rest of the next stream with new
-// paths (persist_blocks blocks of 128 each).
+// paths (persist_blocks blocks of 128 each for k_wf_hit, a multiple of 8;
+// k_wf_regen scales it to its own residency).
 // T (nullable): the launch's job and grid records; a one-job launch uses
 // the WfOneJob form.
 cudaError_t launch_wf_shade(const WfParams& P, int par, int persist_blocks, bool count, cudaStream_t st,

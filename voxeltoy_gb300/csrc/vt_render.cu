@@ -263,10 +263,10 @@ __device__ __forceinline__ uint32_t slot_flags(const Path& p, uint32_t emit, uin
 //   k_wf_regen  new paths in positions [hits, capacity) of the next stream,
 //               primary segments to the queue
 //   k_wf_trace  the queue: DDA of every segment, ends stored by position
-// Every state access is to consecutive positions.  k_wf_hit and k_wf_regen
-// keep eight resident blocks per SM (64 registers): the extra warps hide
-// more of the load latency than the few spills cost; the lighter k_wf_shade
-// fits twelve.
+// Every state access is to consecutive positions.  k_wf_hit keeps eight
+// resident blocks per SM (64 registers): the extra warps hide more of the
+// load latency than the few spills cost; the lighter k_wf_shade and (with one
+// job) k_wf_regen fit twelve.
 template <bool kCount, class Tab>
 __global__ void __launch_bounds__(128, 12) k_wf_shade(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
@@ -392,8 +392,13 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
 // k's queue record is entry QCOUNT + k of the round's queue (the hit
 // kernel's records come first), a record without a segment for an empty
 // position, so that the kernel needs no block-wide reservation.
+// Resident blocks the new-path kernel is compiled for: twelve with one job
+// (40 registers, no spill), eight with a job table (whose records need more).
+template <class Tab> struct RegenBlocks { static constexpr int value = 8; };
+template <> struct RegenBlocks<WfOneJob> { static constexpr int value = 12; };
+
 template <bool kCount, class Tab>
-__global__ void __launch_bounds__(128, 8) k_wf_regen(const WfParams P, const __grid_constant__ Tab T, int par) {
+__global__ void __launch_bounds__(128, RegenBlocks<Tab>::value) k_wf_regen(const WfParams P, const __grid_constant__ Tab T, int par) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -682,11 +687,11 @@ static void wf_shade(const WfParams& P, const Tab& T, int par, int persist_block
   if (count) {
     k_wf_shade<true, Tab><<<blocks, 128, 0, st>>>(P, T, par);
     k_wf_hit<true, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
-    k_wf_regen<true, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
+    k_wf_regen<true, Tab><<<persist_blocks / 8 * RegenBlocks<Tab>::value, 128, 0, st>>>(P, T, par);
   } else {
     k_wf_shade<false, Tab><<<blocks, 128, 0, st>>>(P, T, par);
     k_wf_hit<false, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
-    k_wf_regen<false, Tab><<<persist_blocks, 128, 0, st>>>(P, T, par);
+    k_wf_regen<false, Tab><<<persist_blocks / 8 * RegenBlocks<Tab>::value, 128, 0, st>>>(P, T, par);
   }
 }
 
