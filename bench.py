@@ -623,6 +623,14 @@ def config5_record(ctx, spp: int = 1024, steps: int = 3, check: bool = False, rm
     cfg = S.config1(edge=8, width=2048, height=2048, spp=spp)
     cfg.settings.max_bounces = 8
     job = Job(ctx, sc, None, cfg.camera, cfg.settings, 2048, 2048)
+    # the launch shape for this scene (its segments are longer than config 2's):
+    # a short sweep at 64 spp per setting
+    from voxeltoy_gb300 import autotune
+    best = autotune.tune(ctx, [job], passes=64, repeats=1, use_cache=False,
+                         grid={"path_slots": [1 << 25, 1 << 26], "trace_blocks_per_sm": [0], "trace_steps": [16, 32],
+                               "lanes": [3], "brick_shape": [(2, 2, 2)], "queue_chunk": [128, 64],
+                               "refill_min": [0], "trace_form_steps": []})
+    tuning = {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps", "lanes", "queue_chunk")}
     timer = EventTimer(ctx, ctx_device(ctx))
     job.render(4)
     job.reset()
@@ -639,7 +647,7 @@ def config5_record(ctx, spp: int = 1024, steps: int = 3, check: bool = False, rm
            "voxelize_ms": {"median": float(np.median(vox_ms)), "min": float(min(vox_ms))},
            "voxelize_mtris_s": len(f) / (np.median(vox_ms) * 1e-3) / 1e6,
            "render_ms": timer.ms, "render_mpaths_s": paths / (timer.ms * 1e-3) / 1e6,
-           "image_finite": bool(np.isfinite(img).all())}
+           "image_finite": bool(np.isfinite(img).all()), "tuning": tuning}
     if rmse_rows > 0:
         r0 = (2048 - rmse_rows) // 2
         rec["rmse_vs_fp64"] = rmse_vs_fp64(cfg, img, spp, (r0, r0 + rmse_rows))
