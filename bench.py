@@ -315,8 +315,9 @@ def batching_record(ctx, n_scenes: int, steps: int, rmse_scenes: int = 4, e2e: b
     jobs = [m[1] for m in made]
     paths = sum(j.width * j.height for j in jobs) * spp
     best = autotune.tune(ctx, jobs, passes=16, repeats=1, use_cache=False,
-                         grid={"path_slots": [1 << 22, 1 << 23, 1 << 24], "trace_blocks_per_sm": [0],
-                               "trace_steps": [16], "lanes": [2]})
+                         grid={"path_slots": [1 << 24, 1 << 25], "trace_blocks_per_sm": [0],
+                               "trace_steps": [16, 32], "lanes": [2, 3], "brick_shape": [(2, 2, 2)],
+                               "queue_chunk": [128, 64], "refill_min": [0], "trace_form_steps": []})
     timer = EventTimer(ctx, ctx_device(ctx))
 
     def reset():
@@ -361,7 +362,7 @@ def batching_record(ctx, n_scenes: int, steps: int, rmse_scenes: int = 4, e2e: b
            "batched_vs_plain": out["plain_loop"]["ms"] / out["batched"]["ms"],
            "batched_vs_per_scene": out["per_scene_wavefront"]["ms"] / out["batched"]["ms"],
            "identical_images": bool(same), "rmse_vs_fp64": rmse,
-           "tuning": {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps", "lanes")}}
+           "tuning": {k: best[k] for k in ("path_slots", "trace_blocks_per_sm", "trace_steps", "lanes", "queue_chunk")}}
     vox_h = [torch.from_numpy(np.ascontiguousarray(m[2].voxels)).pin_memory().numpy() for m in made] if e2e else []
     cfgs = [m[2] for m in made]
     for sc, j, _c in made:

@@ -624,7 +624,9 @@ typedef struct vt_server_stats {
 } vt_server_stats;
 
 /* Start a request loop thread that admits jobs as slots and budget free up
- * and traces all admitted jobs together each round. */
+ * and traces all admitted jobs together each round.  The rounds take ctx's
+ * wavefront launch settings at this call (lanes, DDA kernel form, blocks,
+ * refill interval, queue chunk). */
 VT_API int vt_server_create(vt_context* ctx, const vt_server_opts* opts,
                             vt_server** out);
 /* Submit a render request on a scene the caller created and owns; the

@@ -308,6 +308,15 @@ extern "C" int vt_server_create(vt_context* ctx, const vt_server_opts* opts, vt_
   L.kernel = 2;
   L.log_fn = ctx->log_fn;
   L.log_user = ctx->log_user;
+  // the rounds take the creating context's launch shape (lanes, DDA kernel
+  // form and grid, refill interval, queue chunk), tuned or not
+  L.lanes = ctx->lanes;
+  L.trace_blocks_per_sm = ctx->trace_blocks_per_sm;
+  L.trace_steps = ctx->trace_steps;
+  L.trace_chunk = ctx->trace_chunk;
+  L.refill_min = ctx->refill_min;
+  L.trace_form = ctx->trace_form;
+  L.use_graphs = ctx->use_graphs;
   cudaSetDevice(L.device);
   cudaError_t e = cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete s; return cuda_fail(e, "server stream"); }
