@@ -568,7 +568,7 @@ VT_API int vt_render_batch(vt_context* ctx, vt_job* const* jobs, int32_t n_jobs,
 #define VT_FIXED_MAX_JOBS 16
 #define VT_FIXED_MAX_PATH_SLOTS 65536
 #define VT_FIXED_MAX_SAMPLES (1 << 20)
-#define VT_FIXED_SCRATCH_BYTES 41956096
+#define VT_FIXED_SCRATCH_BYTES 41956608
 VT_API int vt_render_batch_fixed(vt_context* ctx, vt_job* const* jobs,
                                  int32_t n_jobs, int32_t passes,
                                  int32_t path_slots, int32_t* results);

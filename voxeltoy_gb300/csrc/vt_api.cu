@@ -1147,6 +1147,10 @@ int vt::build_frame(vt_job* j) {
   const float len = std::sqrt(((float)s->res[0] * (float)s->res[0] + (float)s->res[1] * (float)s->res[1]) +
                               (float)s->res[2] * (float)s->res[2]);
   F.max_steps = (int32_t)(2.0f * std::ceil(len));
+  F.m_res0 = udiv_magic((uint32_t)s->res[0]);
+  F.m_res01 = udiv_magic((uint32_t)s->res[0] * (uint32_t)s->res[1]);
+  F.m_width = udiv_magic((uint32_t)j->w);
+  F.m_pixels = udiv_magic((uint32_t)j->w * (uint32_t)j->h);
   vt_camera_uniforms U;
   int rc = vt_camera_compute_uniforms(&j->cam, j->w, j->h, &U);
   if (rc != VT_OK) return rc;

@@ -77,7 +77,25 @@ struct Frame {
   int32_t height;
   int32_t integrator;        // 0 path tracer (pathTracer.fs), 1 edit mode (editMode.fs)
   int32_t n_palette;         // palette entries (bounds of the checked build)
+  // multipliers for dividing by the frame's invariant integers (udiv_magic):
+  // res[0], res[0] * res[1], width, width * height
+  uint64_t m_res0, m_res01, m_width, m_pixels;
 };
+
+// Division by an integer d fixed for a frame, as one high multiply:
+// floor(n / d) = floor(n * M / 2^64) with M = ceil(2^64 / d) for every
+// n < 2^32 and 2 <= d < 2^32, since n * (M - 2^64 / d) / 2^64 < n / 2^64 < 1 / d
+// keeps n * M / 2^64 below the next integer (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", 1994).  M = 0
+// stands for d = 1.
+__host__ __device__ __forceinline__ uint64_t udiv_magic(uint32_t d) {
+  return d <= 1u ? 0ull : (~0ull / d) + 1ull;
+}
+#if defined(__CUDACC__)
+__device__ __forceinline__ uint32_t udiv(uint32_t n, uint64_t m) {
+  return m ? (uint32_t)__umul64hi((unsigned long long)n, m) : n;
+}
+#endif
 
 // What the DDA needs of a volume: extents, bounds, brick layout, step cap.
 struct Grid;

@@ -168,8 +168,8 @@ __device__ __forceinline__ void load_for_shade(const WfState& st, int i, uint32_
 __device__ __forceinline__ void rng_from_item(const JobEntry& E, uint32_t item, uint32_t rng, Path& p) {
   // item - tile_begin = pass * n_pixels + pixel (< 2^32 items per launch)
   const uint32_t r = item - (uint32_t)E.tile_begin;
-  const uint32_t np = (uint32_t)E.n_pixels;
-  const uint32_t pass = r / np;
+  const uint32_t np = (uint32_t)E.n_pixels;   // = width * height
+  const uint32_t pass = udiv(r, E.F.m_pixels);
   p.rng.pixel = r - pass * np;
   p.rng.sample = (uint32_t)E.sample_base + pass;
   if (E.F.rng_mode == 1) { p.rng.ox = (int32_t)(rng & 0xffffu); p.rng.oy = (int32_t)(rng >> 16); p.rng.call = 0; }
@@ -436,11 +436,11 @@ __global__ void __launch_bounds__(128, RegenBlocks<Tab>::value) k_wf_regen(const
           job = (uint32_t)job_of(P, T, my);
           const JobEntry& E = job_entry(P, T, job);
           const uint32_t r = (uint32_t)(my - (unsigned long long)E.tile_begin);   // < 2^32 items per launch
-          const uint32_t np = (uint32_t)E.n_pixels;
-          const uint32_t pass = r / np;
+          const uint32_t np = (uint32_t)E.n_pixels;   // = width * height
+          const uint32_t pass = udiv(r, E.F.m_pixels);
           const uint32_t pixel = r - pass * np;
           const uint32_t w = (uint32_t)E.F.width;
-          const int py = (int)(pixel / w), px = (int)(pixel - (uint32_t)py * w);
+          const int py = (int)udiv(pixel, E.F.m_width), px = (int)(pixel - (uint32_t)py * w);
           if (path_start(E.F, E.J, p, px, py, E.sample_base + (int)pass, cnt, t_enter)) {
             active = true;
             need_new = false;

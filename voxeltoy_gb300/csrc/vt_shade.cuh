@@ -800,9 +800,9 @@ VT_D void light_sample(const Frame& F, const JobDev& J, Path& p, const Basis& b,
     const bool idx_ok = chk(idx0 >= 0 && (long long)idx0 < (long long)F.res[0] * F.res[1] * F.res[2], CHK_EMISSIVE);
     const int idx = idx_ok ? idx0 : 0;
     const int dz = F.res[0] * F.res[1], dy = F.res[0];
-    const int ez = idx / dz;
+    const int ez = (int)udiv((uint32_t)idx, F.m_res01);
     const int r1 = idx - ez * dz;
-    const int ey = r1 / dy;
+    const int ey = (int)udiv((uint32_t)r1, F.m_res0);
     const int ex = r1 - ey * dy;
     const Mat lm = voxel_mat(F, J, ex, ey, ez, cnt);
     Ll = mk3(F.nee_scale, F.nee_scale, F.nee_scale) * lm.emission;
@@ -844,9 +844,9 @@ VT_D void shadow_end(const Frame& F, Path& p, SegEnd e) {
   bool visible;
   if (p.light >= 0) {
     const int dz = F.res[0] * F.res[1], dy = F.res[0];
-    const int ez = p.light / dz;
+    const int ez = (int)udiv((uint32_t)p.light, F.m_res01);
     const int r1 = p.light - ez * dz;
-    const int ey = r1 / dy;
+    const int ey = (int)udiv((uint32_t)r1, F.m_res0);
     const int ex = r1 - ey * dy;
     visible = hit && e.x == ex && e.y == ey && e.z == ez;
   } else {
