@@ -1020,3 +1020,44 @@ def test_pooled_trace_form_is_identical(ctx, steps):
         ctx.set_tuning(1 << 23, 0, 16)
         for m in made:
             close_all(m[2], m[0], m[1])
+
+
+def test_volume_extent_limits_and_longest_rays(ctx, orc):
+    """Volumes up to the documented extents (1,048,574 voxels along x and y,
+    524,286 along z) are accepted, one more is refused with VT_EINVAL, and
+    rays across the whole longest volume (a million DDA steps, distances in
+    the millions) reach the same voxel as the oracle's."""
+    pal = [S.lambert(0.5)]
+    for shape in ((1, 1, 1048575), (1, 1048575, 1), (524287, 1, 1)):
+        with pytest.raises(L.VtError) as e:
+            Scene.dense(ctx, np.zeros(shape, np.uint8), pal)
+        assert e.value.code == L.VT_EINVAL
+    for shape in ((1, 1048574, 1), (524286, 1, 1)):
+        Scene.dense(ctx, np.zeros(shape, np.uint8), pal).close()
+    g = np.zeros((2, 2, 1048574), np.uint8)
+    g[:, :, -1] = 1          # a wall at the far end
+    g[1, 1, 700001] = 1      # and one voxel on the way
+    cfg = small_config1(edge=8, w=8, h=8)
+    cfg.voxels = g
+    cfg.palette = pal
+    scene, env, job = gpu_setup(ctx, cfg, env_rgb=None)
+    try:
+        inf = scene.info()
+        lo, hi = np.array(inf.bounds_min, np.float32), np.array(inf.bounds_max, np.float32)
+        c = (lo + hi) / 2
+        q = (hi - lo) / 4
+        x_near, x_far = lo[0] + 1e-3, lo[0] + np.float32(0.9) * (hi[0] - lo[0])
+        o = np.array([[x_near, c[1] - q[1], c[2] - q[2]], [x_near, c[1] + q[1], c[2] + q[2]],
+                      [x_far, c[1] + q[1], c[2] + q[2]], [x_near, c[1] + q[1], c[2] - q[2]]], np.float32)
+        # long directions: dda.h raises a component below 1e-5 to 1e-5, so a
+        # unit-length axis-aligned ray would leave the two-voxel rod after
+        # 1e5 steps; with |d.x| = 1000 it drifts 1e-8 of a voxel per step
+        d = np.array([[1000, 0, 0], [1000, 0, 0], [-1000, 0, 0], [1000, 1, 0]], np.float32)
+        got = job.trace_rays(o, d)
+        want = orc.trace_rays(orc.Scene(g, pal), o, d, 0)
+        np.testing.assert_array_equal(got, want)
+        hit = (got[:, 3] >> 8) & 1
+        # the far wall 1,048,571 steps away; the voxel on the way, from either side
+        assert hit[:3].all() and got[0, 0] == 1048573 and got[1, 0] == 700001 and got[2, 0] == 700001
+    finally:
+        close_all(job, scene, env)
