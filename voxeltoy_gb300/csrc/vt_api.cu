@@ -1159,6 +1159,9 @@ int vt::build_frame(vt_job* j) {
   memcpy(F.inv_proj, U.inv_proj, sizeof(F.inv_proj));
   memcpy(F.inv_mv, U.inv_model_view, sizeof(F.inv_mv));
   F.frag_z = 0.5f * j->cam.near_distance + 0.5f;
+  // screen_to_eye_persp's depth terms at frag_z, in its operation order
+  F.persp_ndc_z = ((2.0f * F.frag_z - 0.0f) - 1.0f) / (1.0f - 0.0f);
+  F.persp_cw = F.proj[11] / (F.persp_ndc_z - (F.proj[10] / F.proj[14]));
   F.lens_radius = j->cam.lens_radius;
   F.focal_distance = j->cam.focal_distance;
   F.lens_model = j->cam.lens_model;

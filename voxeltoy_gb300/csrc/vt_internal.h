@@ -77,6 +77,9 @@ struct Frame {
   int32_t height;
   int32_t integrator;        // 0 path tracer (pathTracer.fs), 1 edit mode (editMode.fs)
   int32_t n_palette;         // palette entries (bounds of the checked build)
+  // screenToEyeSpacePerspective's depth terms for fragments at frag_z (the
+  // camera rays): ndc z and the clip w, computed once per frame
+  float persp_ndc_z, persp_cw;
   // multipliers for dividing by the frame's invariant integers (udiv_magic):
   // res[0], res[0] * res[1], width, width * height
   uint64_t m_res0, m_res01, m_width, m_pixels;

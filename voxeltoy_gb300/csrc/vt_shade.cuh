@@ -134,6 +134,8 @@ VT_D void rng_init(const Frame& F, Rng& r, int px, int py, int sample) {
   r.pixel = (uint32_t)(py * F.width + px);
   r.sample = (uint32_t)sample;
   r.call = 0;
+  r.ox = r.oy = 0;
+  if (F.rng_mode != 1) return;   // the walk position matters only to the noise table
   const uint32_t off = (uint32_t)(wang_hash(px + py * kNoiseW) ^ wang_hash(sample));
   r.ox = (int32_t)(off % (uint32_t)kNoiseW);
   r.oy = (int32_t)((off / (uint32_t)kNoiseW) % (uint32_t)kNoiseH);
@@ -662,12 +664,20 @@ VT_D v3 sample_env(const Frame& F, const JobDev& J, const Basis& b, float u0, fl
 // ------------------------------------------------------------------ camera
 // screenToEyeSpacePerspective / Orthographic (coordinates.h:1-27) with
 // gl_DepthRange = [0, 1].
+// kAtFragZ: w.z is the frame's frag_z, whose depth terms the frame holds.
+template <bool kAtFragZ = false>
 VT_D float4 screen_to_eye_persp(const Frame& F, v3 w) {
   v3 ndc;
   ndc.x = ((2.0f * w.x) - (2.0f * F.viewport[0])) / F.viewport[2] - 1.0f;
   ndc.y = ((2.0f * w.y) - (2.0f * F.viewport[1])) / F.viewport[3] - 1.0f;
-  ndc.z = ((2.0f * w.z - 0.0f) - 1.0f) / (1.0f - 0.0f);
-  const float cw = F.proj[11] / (ndc.z - (F.proj[10] / F.proj[14]));
+  float cw;
+  if (kAtFragZ) {
+    ndc.z = F.persp_ndc_z;
+    cw = F.persp_cw;
+  } else {
+    ndc.z = ((2.0f * w.z - 0.0f) - 1.0f) / (1.0f - 0.0f);
+    cw = F.proj[11] / (ndc.z - (F.proj[10] / F.proj[14]));
+  }
   return mul4(F.inv_proj, make_float4(ndc.x * cw, ndc.y * cw, ndc.z * cw, cw));
 }
 VT_D float4 screen_to_eye_ortho(const Frame& F, v3 w) {
@@ -679,13 +689,15 @@ VT_D float4 screen_to_eye_ortho(const Frame& F, v3 w) {
 }
 VT_D v3 xyz(float4 v) { return mk3(v.x, v.y, v.z); }
 
-// generateRay (generateRay.h:1-123).  frag = gl_FragCoord.xyz.
+// generateRay (generateRay.h:1-123).  frag = gl_FragCoord.xyz; kAtFragZ:
+// frag.z is the frame's frag_z (the camera rays of a pass).
+template <bool kAtFragZ = false>
 VT_D void generate_ray(const Frame& F, const JobDev& J, v3 frag, Rng& rng, v3& o, v3& d) {
   const float* M = F.inv_mv;
   if (F.lens_model == 0) {                                         // pinhole :10-26
     const float4 u = rng_next(F, J, rng);
     const v3 jit = mk3(u.x - 0.5f, u.y - 0.5f, 0.0f);
-    const float4 es = screen_to_eye_persp(F, frag + jit);
+    const float4 es = screen_to_eye_persp<kAtFragZ>(F, frag + jit);
     o = xyz(mul4(M, make_float4(0.0f, 0.0f, 0.0f, 1.0f)));
     const v3 n = normalize(mk3(es.x, es.y, es.z));
     const float4 w = mul4(M, make_float4(n.x, n.y, n.z, 0.0f));
@@ -697,7 +709,7 @@ VT_D void generate_ray(const Frame& F, const JobDev& J, v3 frag, Rng& rng, v3& o
     const v3 lens = mk3(disk.x * F.lens_radius, disk.y * F.lens_radius, 0.0f);
     v3 fp = frag;
     if (!(F.quirks & Q_THINLENS_NO_JITTER)) fp = frag + mk3(u.z - 0.5f, u.w - 0.5f, 0.0f);
-    const v3 eo = xyz(screen_to_eye_persp(F, fp));
+    const v3 eo = xyz(screen_to_eye_persp<kAtFragZ>(F, fp));
     const v3 ed = normalize(eo);
     const float t = F.focal_distance / -(ed.z);
     const v3 ef = eo + ed * t;
@@ -767,7 +779,7 @@ VT_D bool path_start(const Frame& F, const JobDev& J, Path& p, int px, int py, i
   p.nee_P = mk3(0.0f, 0.0f, 0.0f);
   p.nee_nf = 0;
   v3 o, d;
-  generate_ray(F, J, mk3((float)px + 0.5f, (float)py + 0.5f, F.frag_z), p.rng, o, d);
+  generate_ray<true>(F, J, mk3((float)px + 0.5f, (float)py + 0.5f, F.frag_z), p.rng, o, d);
   p.ro = o;
   p.rd = d;
   p.sd = d;
