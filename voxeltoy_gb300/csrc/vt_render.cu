@@ -259,9 +259,10 @@ __device__ __forceinline__ uint32_t slot_flags(const Path& p, uint32_t emit, uin
 //               BSDF
 //   k_wf_hit    the hit records: vertex shading, light and BSDF samples;
 //               writes its paths to positions [0, hits) of the next stream
-//               and their next segments to the queue
+//               and their next segments to the queue; reserves the first
+//               items of the new paths
 //   k_wf_regen  new paths in positions [hits, capacity) of the next stream,
-//               primary segments to the queue
+//               primary segments to the queue after the hit kernel's
 //   k_wf_trace  the queue: DDA of every segment, ends stored by position
 // Every state access is to consecutive positions.  k_wf_hit keeps eight
 // resident blocks per SM (64 registers): the extra warps hide more of the
