@@ -221,7 +221,10 @@ __device__ __forceinline__ void block_reserve(uint32_t* const (&ctr)[N], const u
 }
 
 // Write this warp's next segments (queue entries from `base`) as 32-byte ray
-// records {o.xyz, d.x} {d.yz, slot << 1 | kind, job}: the warp's extension
+// records {o.xyz, inc.x} {inc.yz, slot << 1 | kind, job | nudge << 26} (the
+// direction as seg_dir gives it to the DDA set-up, so that the reciprocals
+// are taken here, in coherent warps, rather than by the DDA kernel's lanes
+// as they start segments at different times): the warp's extension
 // records first, then its shadow records.  emit: 1 extension (from
 // `ext_o`), 2 shadow.
 __device__ __forceinline__ void write_segments(const WfParams& P, int par, uint32_t base, uint32_t emit, int slot,
@@ -233,13 +236,15 @@ __device__ __forceinline__ void write_segments(const WfParams& P, int par, uint3
   float4* q = P.queue[par];
   if (n1) {
     const size_t at = 2 * (size_t)(base + __popc(b1 & lt));
-    q[at] = make_float4(ext_o.x, ext_o.y, ext_o.z, p.rd.x);
-    q[at + 1] = make_float4(p.rd.y, p.rd.z, __uint_as_float((uint32_t)slot << 1), __uint_as_float(job));
+    const SegDir sd = seg_dir(p.rd);
+    q[at] = make_float4(ext_o.x, ext_o.y, ext_o.z, sd.inc.x);
+    q[at + 1] = make_float4(sd.inc.y, sd.inc.z, __uint_as_float((uint32_t)slot << 1), __uint_as_float(job | (sd.nudge << 26)));
   }
   if (n2) {
     const size_t at = 2 * (size_t)(base + __popc(b1) + __popc(b2 & lt));
-    q[at] = make_float4(p.ro.x, p.ro.y, p.ro.z, p.sd.x);
-    q[at + 1] = make_float4(p.sd.y, p.sd.z, __uint_as_float(((uint32_t)slot << 1) | 1u), __uint_as_float(job));
+    const SegDir sd = seg_dir(p.sd);
+    q[at] = make_float4(p.ro.x, p.ro.y, p.ro.z, sd.inc.x);
+    q[at + 1] = make_float4(sd.inc.y, sd.inc.z, __uint_as_float(((uint32_t)slot << 1) | 1u), __uint_as_float(job | (sd.nudge << 26)));
   }
 }
 
@@ -463,8 +468,9 @@ __global__ void __launch_bounds__(128, RegenBlocks<Tab>::value) k_wf_regen(const
       const size_t at = 2 * (size_t)(qbase + k);
       if (active) {
         const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
-        q[at] = make_float4(o.x, o.y, o.z, p.rd.x);
-        q[at + 1] = make_float4(p.rd.y, p.rd.z, __uint_as_float((uint32_t)pos << 1), __uint_as_float(job));
+        const SegDir sd = seg_dir(p.rd);
+        q[at] = make_float4(o.x, o.y, o.z, sd.inc.x);
+        q[at + 1] = make_float4(sd.inc.y, sd.inc.z, __uint_as_float((uint32_t)pos << 1), __uint_as_float(job | (sd.nudge << 26)));
         store_path(dst, (int)pos, job_entry(P, T, job).F, p, item, false);   // a primary path has no shadow segment
         dst.flags[pos] = slot_flags(p, 1u, job);
       } else {
@@ -526,8 +532,8 @@ __global__ void __launch_bounds__(256, TraceBlocks<Tab>::value) k_wf_trace(const
       have_next = false;
       tag = __float_as_uint(nb.z);
       if (tag != kNoSegment) {
-        gh.set(P, T, __float_as_uint(nb.w));
-        dda_begin(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
+        gh.set(P, T, __float_as_uint(nb.w) & 0x03ffffffu);
+        dda_begin_inc(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y), __float_as_uint(nb.w) >> 26);
         if (s.state == DDA_RUNNING) have = true;
         else P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
       }
@@ -619,10 +625,10 @@ __global__ void __launch_bounds__(256, 4) k_wf_trace_pool(const WfParams P, cons
       if (rec < chunk_end && __float_as_uint(__ldg(&q[2 * (size_t)rec + 1]).z) != kNoSegment) {
         const float4 a = __ldg(&q[2 * (size_t)rec]), b = __ldg(&q[2 * (size_t)rec + 1]);
         ttag = __float_as_uint(b.z);
-        tjob = __float_as_uint(b.w);
+        tjob = __float_as_uint(b.w) & 0x03ffffffu;
         GridHold<Tab> tg;
         tg.set(P, T, tjob);
-        dda_begin(tg.get(T), t, mk3(a.x, a.y, a.z), mk3(a.w, b.x, b.y));
+        dda_begin_inc(tg.get(T), t, mk3(a.x, a.y, a.z), mk3(a.w, b.x, b.y), __float_as_uint(b.w) >> 26);
         run = t.state == DDA_RUNNING;
         if (!run) P.hits[(size_t)(ttag & 1u) * P.n_slots + (ttag >> 1)] = pack_end(t.x, t.y, t.z, t.state);
       }

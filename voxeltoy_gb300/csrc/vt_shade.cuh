@@ -296,6 +296,45 @@ VT_D void dda_begin(const Grid& g, Dda& s, v3 o, v3 d) {
   s.sx = (int32_t)sg.x; s.sy = (int32_t)sg.y; s.sz = (int32_t)sg.z;
 }
 
+// A segment record's direction in the form the DDA set-up uses: the
+// reciprocals of the direction with components of magnitude at most 1e-5
+// raised to +1e-5 (dda.h:29-31), and the signs of the original components
+// (for the origin nudge, dda.h:19) in two bits each: 0 zero, 1 plus, 2 minus.
+struct SegDir { v3 inc; uint32_t nudge; };
+VT_D SegDir seg_dir(v3 d) {
+  SegDir r;
+  r.nudge = (d.x > 0.0f ? 1u : (d.x < 0.0f ? 2u : 0u)) | (d.y > 0.0f ? 4u : (d.y < 0.0f ? 8u : 0u)) |
+            (d.z > 0.0f ? 16u : (d.z < 0.0f ? 32u : 0u));
+  d.x = vtb::gstep(fabsf(d.x), 1e-5f) ? 1e-5f : d.x;
+  d.y = vtb::gstep(fabsf(d.y), 1e-5f) ? 1e-5f : d.y;
+  d.z = vtb::gstep(fabsf(d.z), 1e-5f) ? 1e-5f : d.z;
+  r.inc = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  return r;
+}
+VT_D float nudge_sign(uint32_t bits) { return bits == 1u ? 1.0f : (bits == 2u ? -1.0f : 0.0f); }
+// dda_begin from a SegDir: the same operations on the same values.
+VT_D void dda_begin_inc(const Grid& g, Dda& s, v3 o, v3 inc, uint32_t nudge) {
+  const v3 bmin = mk3(g.bminx, g.bminy, g.bminz);
+  o = o + mk3(nudge_sign(nudge & 3u), nudge_sign((nudge >> 2) & 3u), nudge_sign((nudge >> 4) & 3u)) * 0.001f;
+  const v3 vo = ((o - bmin) * mk3(g.vextx, g.vexty, g.vextz)) * mk3((float)g.rx, (float)g.ry, (float)g.rz);
+  const v3 vp = mk3(floorf(vo.x), floorf(vo.y), floorf(vo.z));
+  s.x = (int32_t)vp.x; s.y = (int32_t)vp.y; s.z = (int32_t)vp.z;
+  s.steps = 0;
+  s.cb = -1;
+  s.bits = 0ull;
+  if (vp.x < 0.0f || vp.y < 0.0f || vp.z < 0.0f || vp.x >= (float)g.rx || vp.y >= (float)g.ry ||
+      vp.z >= (float)g.rz) {
+    s.state = DDA_MISS;
+    return;
+  }
+  s.state = DDA_RUNNING;
+  const v3 sg = mk3(inc.x > 0.0f ? 1.0f : -1.0f, inc.y > 0.0f ? 1.0f : -1.0f, inc.z > 0.0f ? 1.0f : -1.0f);
+  const v3 dis = (((vp - vo) + mk3(0.5f, 0.5f, 0.5f)) + sg * 0.5f) * inc;
+  s.dx = dis.x; s.dy = dis.y; s.dz = dis.z;
+  s.ax = sg.x * inc.x; s.ay = sg.y * inc.y; s.az = sg.z * inc.z;
+  s.sx = (int32_t)sg.x; s.sy = (int32_t)sg.y; s.sz = (int32_t)sg.z;
+}
+
 // DDA loop (dda.h:38-57): at most `budget` iterations of
 // bounds test -> occupancy test -> advance every minimal axis.
 // The brick grid carries a one-brick border whose voxels are all set, so the
