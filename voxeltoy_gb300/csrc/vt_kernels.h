@@ -91,7 +91,7 @@ void wf_carve(void* mem, size_t slots, WfParams& P);
 // kernel parameter as well, so the kernels read them through the constant
 // cache instead of global memory.
 constexpr int kWfParamJobs = 8;
-constexpr int kWfMaxJobs = 1 << 15;   // jobs per wavefront launch (bits of the slot flags; < 2^26 for queue records)
+constexpr int kWfMaxJobs = 1 << 15;   // jobs per wavefront launch (bits of the slot flags)
 struct WfJobTable {
   JobEntry e[kWfParamJobs];
   Grid g[kWfParamJobs];

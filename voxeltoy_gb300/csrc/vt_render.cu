@@ -221,14 +221,14 @@ __device__ __forceinline__ void block_reserve(uint32_t* const (&ctr)[N], const u
 }
 
 // Write this warp's next segments (queue entries from `base`) as 32-byte ray
-// records {o.xyz, inc.x} {inc.yz, slot << 1 | kind, job | nudge << 26} (the
-// direction as seg_dir gives it to the DDA set-up, so that the reciprocals
-// are taken here, in coherent warps, rather than by the DDA kernel's lanes
-// as they start segments at different times): the warp's extension
+// records {vo.xyz, inc.x} {inc.yz, slot << 1 | kind, job}: the origin in
+// voxel space and the reciprocal direction as seg_rec gives them to the DDA
+// set-up, computed here in coherent warps rather than by the DDA kernel's
+// lanes as they start segments at different times.  The warp's extension
 // records first, then its shadow records.  emit: 1 extension (from
 // `ext_o`), 2 shadow.
 __device__ __forceinline__ void write_segments(const WfParams& P, int par, uint32_t base, uint32_t emit, int slot,
-                                               uint32_t job, v3 ext_o, const Path& p) {
+                                               uint32_t job, v3 ext_o, const Path& p, const Frame& F) {
   const unsigned FULL = 0xffffffffu;
   const unsigned lt = (1u << (threadIdx.x & 31)) - 1u;
   const uint32_t n1 = (emit & 1u) ? 1u : 0u, n2 = (emit & 2u) ? 1u : 0u;
@@ -236,15 +236,15 @@ __device__ __forceinline__ void write_segments(const WfParams& P, int par, uint3
   float4* q = P.queue[par];
   if (n1) {
     const size_t at = 2 * (size_t)(base + __popc(b1 & lt));
-    const SegDir sd = seg_dir(p.rd);
-    q[at] = make_float4(ext_o.x, ext_o.y, ext_o.z, sd.inc.x);
-    q[at + 1] = make_float4(sd.inc.y, sd.inc.z, __uint_as_float((uint32_t)slot << 1), __uint_as_float(job | (sd.nudge << 26)));
+    const SegRec sr = seg_rec(F, ext_o, p.rd);
+    q[at] = make_float4(sr.vo.x, sr.vo.y, sr.vo.z, sr.inc.x);
+    q[at + 1] = make_float4(sr.inc.y, sr.inc.z, __uint_as_float((uint32_t)slot << 1), __uint_as_float(job));
   }
   if (n2) {
     const size_t at = 2 * (size_t)(base + __popc(b1) + __popc(b2 & lt));
-    const SegDir sd = seg_dir(p.sd);
-    q[at] = make_float4(p.ro.x, p.ro.y, p.ro.z, sd.inc.x);
-    q[at + 1] = make_float4(sd.inc.y, sd.inc.z, __uint_as_float(((uint32_t)slot << 1) | 1u), __uint_as_float(job | (sd.nudge << 26)));
+    const SegRec sr = seg_rec(F, p.ro, p.sd);
+    q[at] = make_float4(sr.vo.x, sr.vo.y, sr.vo.z, sr.inc.x);
+    q[at + 1] = make_float4(sr.inc.y, sr.inc.z, __uint_as_float(((uint32_t)slot << 1) | 1u), __uint_as_float(job));
   }
 }
 
@@ -380,7 +380,7 @@ __global__ void __launch_bounds__(128, 8) k_wf_hit(const WfParams P, const __gri
     const uint32_t nn[1] = {(emit & 1u) + (emit >> 1)};
     uint32_t base[1];
     block_reserve<1>(ctr, nn, base);
-    write_segments(P, par, base[0], emit, (int)v, job, p.ro, p);
+    write_segments(P, par, base[0], emit, (int)v, job, p.ro, p, job_entry(P, T, job).F);
     if (mine) {
       store_path(dst, (int)v, job_entry(P, T, job).F, p, item, (emit & 2u) != 0);
       dst.flags[v] = slot_flags(p, emit, job);
@@ -468,9 +468,9 @@ __global__ void __launch_bounds__(128, RegenBlocks<Tab>::value) k_wf_regen(const
       const size_t at = 2 * (size_t)(qbase + k);
       if (active) {
         const v3 o = p.ro + t_enter * p.rd;   // the primary segment starts at the volume entry point
-        const SegDir sd = seg_dir(p.rd);
-        q[at] = make_float4(o.x, o.y, o.z, sd.inc.x);
-        q[at + 1] = make_float4(sd.inc.y, sd.inc.z, __uint_as_float((uint32_t)pos << 1), __uint_as_float(job | (sd.nudge << 26)));
+        const SegRec sr = seg_rec(job_entry(P, T, job).F, o, p.rd);
+        q[at] = make_float4(sr.vo.x, sr.vo.y, sr.vo.z, sr.inc.x);
+        q[at + 1] = make_float4(sr.inc.y, sr.inc.z, __uint_as_float((uint32_t)pos << 1), __uint_as_float(job));
         store_path(dst, (int)pos, job_entry(P, T, job).F, p, item, false);   // a primary path has no shadow segment
         dst.flags[pos] = slot_flags(p, 1u, job);
       } else {
@@ -532,8 +532,8 @@ __global__ void __launch_bounds__(256, TraceBlocks<Tab>::value) k_wf_trace(const
       have_next = false;
       tag = __float_as_uint(nb.z);
       if (tag != kNoSegment) {
-        gh.set(P, T, __float_as_uint(nb.w) & 0x03ffffffu);
-        dda_begin_inc(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y), __float_as_uint(nb.w) >> 26);
+        gh.set(P, T, __float_as_uint(nb.w));
+        dda_begin_rec(gh.get(T), s, mk3(na.x, na.y, na.z), mk3(na.w, nb.x, nb.y));
         if (s.state == DDA_RUNNING) have = true;
         else P.hits[(size_t)(tag & 1u) * P.n_slots + (tag >> 1)] = pack_end(s.x, s.y, s.z, s.state);
       }
@@ -625,10 +625,10 @@ __global__ void __launch_bounds__(256, 4) k_wf_trace_pool(const WfParams P, cons
       if (rec < chunk_end && __float_as_uint(__ldg(&q[2 * (size_t)rec + 1]).z) != kNoSegment) {
         const float4 a = __ldg(&q[2 * (size_t)rec]), b = __ldg(&q[2 * (size_t)rec + 1]);
         ttag = __float_as_uint(b.z);
-        tjob = __float_as_uint(b.w) & 0x03ffffffu;
+        tjob = __float_as_uint(b.w);
         GridHold<Tab> tg;
         tg.set(P, T, tjob);
-        dda_begin_inc(tg.get(T), t, mk3(a.x, a.y, a.z), mk3(a.w, b.x, b.y), __float_as_uint(b.w) >> 26);
+        dda_begin_rec(tg.get(T), t, mk3(a.x, a.y, a.z), mk3(a.w, b.x, b.y));
         run = t.state == DDA_RUNNING;
         if (!run) P.hits[(size_t)(ttag & 1u) * P.n_slots + (ttag >> 1)] = pack_end(t.x, t.y, t.z, t.state);
       }

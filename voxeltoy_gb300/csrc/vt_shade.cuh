@@ -296,27 +296,23 @@ VT_D void dda_begin(const Grid& g, Dda& s, v3 o, v3 d) {
   s.sx = (int32_t)sg.x; s.sy = (int32_t)sg.y; s.sz = (int32_t)sg.z;
 }
 
-// A segment record's direction in the form the DDA set-up uses: the
-// reciprocals of the direction with components of magnitude at most 1e-5
-// raised to +1e-5 (dda.h:29-31), and the signs of the original components
-// (for the origin nudge, dda.h:19) in two bits each: 0 zero, 1 plus, 2 minus.
-struct SegDir { v3 inc; uint32_t nudge; };
-VT_D SegDir seg_dir(v3 d) {
-  SegDir r;
-  r.nudge = (d.x > 0.0f ? 1u : (d.x < 0.0f ? 2u : 0u)) | (d.y > 0.0f ? 4u : (d.y < 0.0f ? 8u : 0u)) |
-            (d.z > 0.0f ? 16u : (d.z < 0.0f ? 32u : 0u));
+// A segment record in the form the DDA set-up uses (dda.h:15-31): the
+// origin nudged by 0.001 along the direction's signs and taken to voxel
+// space, and the reciprocals of the direction with components of magnitude
+// at most 1e-5 raised to +1e-5.  The same operations as dda_begin's.
+struct SegRec { v3 vo, inc; };
+VT_D SegRec seg_rec(const Frame& F, v3 o, v3 d) {
+  SegRec r;
+  o = o + mk3(vtb::gsign(d.x), vtb::gsign(d.y), vtb::gsign(d.z)) * 0.001f;
+  r.vo = ((o - ld3(F.bmin)) * ld3(F.vext)) * mk3((float)F.res[0], (float)F.res[1], (float)F.res[2]);
   d.x = vtb::gstep(fabsf(d.x), 1e-5f) ? 1e-5f : d.x;
   d.y = vtb::gstep(fabsf(d.y), 1e-5f) ? 1e-5f : d.y;
   d.z = vtb::gstep(fabsf(d.z), 1e-5f) ? 1e-5f : d.z;
   r.inc = mk3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
   return r;
 }
-VT_D float nudge_sign(uint32_t bits) { return bits == 1u ? 1.0f : (bits == 2u ? -1.0f : 0.0f); }
-// dda_begin from a SegDir: the same operations on the same values.
-VT_D void dda_begin_inc(const Grid& g, Dda& s, v3 o, v3 inc, uint32_t nudge) {
-  const v3 bmin = mk3(g.bminx, g.bminy, g.bminz);
-  o = o + mk3(nudge_sign(nudge & 3u), nudge_sign((nudge >> 2) & 3u), nudge_sign((nudge >> 4) & 3u)) * 0.001f;
-  const v3 vo = ((o - bmin) * mk3(g.vextx, g.vexty, g.vextz)) * mk3((float)g.rx, (float)g.ry, (float)g.rz);
+// dda_begin from a SegRec: the rest of its operations on the same values.
+VT_D void dda_begin_rec(const Grid& g, Dda& s, v3 vo, v3 inc) {
   const v3 vp = mk3(floorf(vo.x), floorf(vo.y), floorf(vo.z));
   s.x = (int32_t)vp.x; s.y = (int32_t)vp.y; s.z = (int32_t)vp.z;
   s.steps = 0;
